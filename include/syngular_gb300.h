@@ -1,0 +1,203 @@
+/*
+ * syngular_gb300 -- C ABI of the GB300 (sm_103a) matrix-product library.
+ *
+ * Conventions
+ *   - Every pointer argument named for a core, matrix or result is a DEVICE
+ *     pointer, except arrays of pointers/shapes (`const double* const* cores`,
+ *     `const int64_t* shape`), which live in HOST memory and hold device
+ *     pointers / sizes.
+ *   - Cores are dense row-major: MPS core (l, p, r); MPO core (l, in, out, r).
+ *     Where an operation treats an MPO core as an MPS core (rounding,
+ *     orthonormalisation, overlap of vectorised operators) it passes
+ *     p = in * out, exactly as the reference's left matricization does.
+ *   - `shape` arrays are flattened triples (l_k, p_k, r_k), k = 0..n-1.
+ *   - `stream` is a cudaStream_t (NULL = legacy default stream).  Calls are
+ *     asynchronous unless stated otherwise; they never synchronise the device.
+ *   - Scratch memory is caller-provided: query `*_workspace_size`, pass a
+ *     device buffer of at least that many bytes (256-byte aligned).  The
+ *     library allocates nothing and frees nothing.
+ *   - Return value: SGT_OK or an SGT_ERR_* code; `sgt_last_error()` gives the
+ *     message of the last failure on the calling thread.  No C++ exception
+ *     crosses this boundary.
+ *
+ * Each entry point names the reference function (antoine311200/Syngular,
+ * path:line) it replaces.  Reference paths: mps = tensor/matrix_product_state.py,
+ * mpo = tensor/matrix_product_operator.py.
+ */
+#ifndef SYNGULAR_GB300_H
+#define SYNGULAR_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#if defined(__GNUC__)
+#define SGT_API __attribute__((visibility("default")))
+#else
+#define SGT_API
+#endif
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define SGT_OK 0
+#define SGT_ERR_INVALID 1        /* bad argument (shape mismatch, null pointer, ...) */
+#define SGT_ERR_NOT_CONVERGED 2  /* an iterative kernel hit its sweep cap */
+#define SGT_ERR_CUDA 3           /* a CUDA runtime call failed */
+#define SGT_ERR_WORKSPACE 4      /* workspace smaller than the size query returned */
+#define SGT_ERR_SHAPE 5          /* the reference would fail to reshape (e.g. l*p < dim) */
+
+/* Arithmetic of the rounding / contraction entry points that take a `precision`. */
+#define SGT_PREC_F64 0     /* plain FP64 everywhere */
+#define SGT_PREC_TF32 1    /* GEMM-shaped work on tcgen05 kind::tf32, FP32 accumulate */
+#define SGT_PREC_BF16 2    /* GEMM-shaped work on tcgen05 kind::f16 with bf16 inputs */
+#define SGT_PREC_BF16X3 3  /* split bf16 (hi*hi + hi*lo + lo*hi) on tcgen05, FP32 accumulate */
+
+SGT_API int sgt_version(void);
+SGT_API const char* sgt_last_error(void);
+
+/* ----------------------------------------------------------------------
+ * Site contractions (raw products, no rounding)
+ * -------------------------------------------------------------------- */
+
+/* MPO x MPS site: P[(a,b), o, (a2,b2)] = sum_i X[a,i,a2] * W[b,i,o,b2],
+ * fused bond index a*B + b.  Replaces the per-site `contract` of
+ * MatrixProductOperator.__matmul__ (mpo:183-191). */
+SGT_API int sgt_site_contract_mpo_mps(const double* X, int64_t a, int64_t p, int64_t a2,
+                              const double* W, int64_t b, int64_t o, int64_t b2,
+                              double* P, void* stream);
+
+/* MPO x MPO site: P[(b,c), i, o, (b2,c2)] = sum_m A[b,i,m,b2] * B[c,m,o,c2],
+ * fused bond index b*C + c.  Replaces mpo:279-288 (output leg uses B's
+ * `out`, where the reference's reshape assumes A.out == B.out). */
+SGT_API int sgt_site_contract_mpo_mpo(const double* A, int64_t b, int64_t i, int64_t m, int64_t b2,
+                              const double* B, int64_t c, int64_t o, int64_t c2,
+                              double* P, void* stream);
+
+/* ----------------------------------------------------------------------
+ * Direct sum (bond concatenation) -- MatrixProductState.__add__ (mps:75-100),
+ * MatrixProductOperator.__add__ (mpo:84-108).
+ * position: 0 = first site ([A | B] along r), 1 = middle (block diagonal),
+ *           2 = last site (stacked along l), 3 = single-site chain (A + B).
+ * Output shape: first (la, phys, ra+rb), middle (la+lb, phys, ra+rb),
+ *               last (la+lb, phys, ra), single (la, phys, ra).
+ * -------------------------------------------------------------------- */
+SGT_API int sgt_bond_concat(const double* A, int64_t la, int64_t phys, int64_t ra,
+                    const double* B, int64_t lb, int64_t rb, int position,
+                    double* out, void* stream);
+
+/* All sites of a chain in one launch (same layout rules as above). */
+SGT_API int sgt_bond_concat_chain(int n, const double* const* A, const int64_t* ashape,
+                          const double* const* B, const int64_t* bshape,
+                          double* const* out, void* ws, size_t ws_bytes, void* stream);
+SGT_API size_t sgt_bond_concat_chain_workspace_size(int n);
+
+/* ----------------------------------------------------------------------
+ * Overlap <X|Y> without conjugation -- MatrixProductState.__or__ (mps:116-127).
+ * Transfer sweep E_{k+1} = sum_p X_k[:,p,:]^T E_k Y_k[:,p,:] with per-site
+ * rescaling.  `result` (device, 2 doubles) receives (mantissa, log_scale):
+ * <X|Y> = mantissa * exp(log_scale).
+ * -------------------------------------------------------------------- */
+SGT_API size_t sgt_overlap_workspace_size(int n, const int64_t* xshape, const int64_t* yshape);
+SGT_API int sgt_overlap_sweep(int n, const double* const* X, const int64_t* xshape,
+                      const double* const* Y, const int64_t* yshape,
+                      double* result, void* ws, size_t ws_bytes, void* stream);
+
+/* ----------------------------------------------------------------------
+ * Reference rounding `>> dim` = compress(dim, strict=True), left mode
+ * (mps:432-468, mpo:544-580): for k = 0..n-2, complete Householder QR of the
+ * left unfolding L_k, core_k <- Q[:, :dim], core_{k+1} <- R[:dim, :] @ R_{k+1}.
+ * The caller applies the early exit (dim >= min(bond_shape), mps:367) itself.
+ * `out[k]` must hold (l'_k, p_k, r'_k) with r'_k = dim (k < n-1), l'_k = dim
+ * (k > 0).  Returns SGT_ERR_SHAPE when some l'_k * p_k < dim.
+ * -------------------------------------------------------------------- */
+SGT_API size_t sgt_qr_truncate_workspace_size(int n, const int64_t* shape, int64_t dim);
+SGT_API int sgt_qr_truncate_sweep(int n, const double* const* cores, const int64_t* shape, int64_t dim,
+                          double* const* out, void* ws, size_t ws_bytes, void* stream);
+
+/* ----------------------------------------------------------------------
+ * Dense tensor -> cores: decompose (mps:296-350, mpo:418-453).
+ * `tensor` holds prod(phys) doubles in row-major order of the (already
+ * interleaved, for an operator) site legs; bonds has n-1 entries.  out[k] has
+ * shape (bonds[k-1], phys[k], bonds[k]).  mode 0 = "left" (truncated complete
+ * QR sweep from the first site), 1 = "right" (from the last site on the
+ * transposed unfoldings, mps:324-347).
+ * -------------------------------------------------------------------- */
+SGT_API size_t sgt_decompose_workspace_size(int n, const int64_t* phys, const int64_t* bonds,
+                                            int mode);
+SGT_API int sgt_decompose(const double* tensor, int n, const int64_t* phys, const int64_t* bonds,
+                          int mode, double* const* out, void* ws, size_t ws_bytes, void* stream);
+
+/* Divide a core by its Frobenius norm in place -- normalize (mps:252-256).
+ * `norm` (device, 1 double) receives the norm. */
+SGT_API int sgt_normalize(double* core, int64_t count, double* norm, void* stream);
+
+/* ----------------------------------------------------------------------
+ * In-place left / right orthonormalisation -- left_orthonormalization
+ * (mps:554-566, mpo:673-694), right_orthonormalization (mps:568-580,
+ * mpo:696-719).  Shapes are kept (the reference requires l*p >= r, resp.
+ * p*r >= l; SGT_ERR_SHAPE otherwise).
+ * -------------------------------------------------------------------- */
+SGT_API size_t sgt_orthonormalize_workspace_size(int n, const int64_t* shape);
+SGT_API int sgt_left_orthonormalize(int n, double* const* cores, const int64_t* shape,
+                            void* ws, size_t ws_bytes, void* stream);
+SGT_API int sgt_right_orthonormalize(int n, double* const* cores, const int64_t* shape,
+                             void* ws, size_t ws_bytes, void* stream);
+
+/* Gram matrix of one core -- left_orthogonality (mps:624-626) with side 0:
+ * out (r x r) = L^T L, L = (l*p, r); right_orthogonality (mps:628-630) with
+ * side 1: out (l x l) = R R^T, R = (l, p*r). */
+SGT_API int sgt_orthogonality(const double* core, int64_t l, int64_t p, int64_t r, int side,
+                      double* out, void* stream);
+
+/* ----------------------------------------------------------------------
+ * TT-SVD rounding to bond chi (no reference counterpart: the reference's `>>`
+ * is the QR truncation above).  Left Householder-QR sweep (bonds reduced to
+ * the left rank bound), then right-to-left truncated SVD via one-sided Jacobi.
+ * `out_shape` (3n) is filled by sgt_svd_round_shapes.  `spectra` (device,
+ * may be NULL) receives, bond after bond k = 1..n-1, the full singular
+ * values of that bond's unfolding (sgt_svd_round_shapes gives the counts in
+ * `spec_count`); `discarded` (device, n-1 doubles, may be NULL) the
+ * discarded weight sum(dropped s^2)/sum(s^2) per bond.  `status` (device
+ * int, may be NULL) receives the largest Jacobi sweep count over the bonds,
+ * or -1 if some bond's Jacobi SVD reached its sweep cap.
+ * -------------------------------------------------------------------- */
+SGT_API int sgt_svd_round_shapes(int n, const int64_t* shape, int64_t chi, int64_t* out_shape,
+                         int64_t* spec_count);
+SGT_API size_t sgt_svd_round_workspace_size(int n, const int64_t* shape, int64_t chi, int precision);
+SGT_API int sgt_svd_round(int n, const double* const* cores, const int64_t* shape, int64_t chi,
+                  int precision, double* const* out, double* spectra, double* discarded,
+                  int* status, void* ws, size_t ws_bytes, void* stream);
+
+/* ----------------------------------------------------------------------
+ * Dense primitives (exported for composition and tests)
+ * -------------------------------------------------------------------- */
+
+/* C = alpha * op(A) op(B) + beta * C, row-major, batched with element strides.
+ * op(A) is M x K (A stored K x M when transA), op(B) is K x N. */
+SGT_API int sgt_gemm_f64(int transA, int transB, int64_t M, int64_t N, int64_t K, double alpha,
+                 const double* A, int64_t lda, int64_t strideA,
+                 const double* B, int64_t ldb, int64_t strideB, double beta,
+                 double* C, int64_t ldc, int64_t strideC, int64_t batch, void* stream);
+
+/* Householder QR of row-major A (m x n, leading dim lda) in place (R on and
+ * above the diagonal, reflectors below), tau gets min(m,n) scalars; then
+ * Q (m x keep, keep <= m) = first `keep` columns of the complete Q. */
+SGT_API size_t sgt_qr_workspace_size(int64_t m, int64_t n, int64_t keep);
+SGT_API int sgt_qr(double* A, int64_t m, int64_t n, int64_t lda, double* tau, double* Q, int64_t keep,
+           void* ws, size_t ws_bytes, void* stream);
+
+/* One-sided Jacobi SVD of row-major A (m x n, m >= n): on return A holds
+ * U*diag(s) with columns in descending order of s, V (n x n, row-major) the
+ * right singular vectors as columns, s the singular values in descending
+ * order.  `status` (device int, may be NULL) gets the number of sweeps used,
+ * or -1 if the sweep cap was reached; the call itself never waits for the
+ * device, so a caller that needs the verdict reads `status` after a sync. */
+SGT_API size_t sgt_jacobi_svd_workspace_size(int64_t m, int64_t n);
+SGT_API int sgt_jacobi_svd(double* A, int64_t m, int64_t n, double* V, double* s, int* status,
+                   void* ws, size_t ws_bytes, void* stream);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* SYNGULAR_GB300_H */

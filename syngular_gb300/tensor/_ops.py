@@ -1,0 +1,315 @@
+"""Chain-level operations on lists of device cores, each one C-ABI call.
+
+A core is a contiguous ``torch.float64`` CUDA tensor of rank >= 3 whose first
+and last axes are the bonds; the middle axes form the physical leg (an MPO core
+``(l, in, out, r)`` is handled as ``(l, in*out, r)`` wherever the reference
+reshapes it that way).  Every function here enqueues work on the current CUDA
+stream; only the ones returning Python scalars or host arrays synchronise.
+"""
+from __future__ import annotations
+
+import ctypes
+import math
+from typing import List, Sequence, Tuple
+
+import numpy as np
+import torch
+
+from .. import _lib as L
+
+Cores = List[torch.Tensor]
+
+
+def shape3(t: torch.Tensor) -> Tuple[int, int, int]:
+    s = tuple(t.shape)
+    return int(s[0]), int(np.prod(s[1:-1], dtype=np.int64)) if len(s) > 2 else 1, int(s[-1])
+
+
+def _check(cores: Sequence[torch.Tensor]):
+    for c in cores:
+        if not (c.is_cuda and c.dtype == torch.float64 and c.is_contiguous()):
+            raise TypeError("cores must be contiguous float64 CUDA tensors")
+
+
+def empty(shape) -> torch.Tensor:
+    return torch.empty(tuple(int(x) for x in shape), dtype=torch.float64, device=L.device())
+
+
+# ---------------------------------------------------------------------------
+# site contractions
+# ---------------------------------------------------------------------------
+
+def contract_mpo_mps(W: Cores, X: Cores) -> Cores:
+    """Raw per-site ``W @ X`` (matrix_product_operator.py:183-191)."""
+    _check(W)
+    _check(X)
+    out = []
+    st = L.stream_ptr()
+    for w, x in zip(W, X):
+        a, p, a2 = x.shape
+        b, i, o, b2 = w.shape
+        if p != i:
+            raise ValueError("physical leg mismatch: state %d vs operator input %d" % (p, i))
+        P = empty((a * b, o, a2 * b2))
+        L.call("sgt_site_contract_mpo_mps", L.ptr(x), a, p, a2, L.ptr(w), b, o, b2, L.ptr(P), st)
+        out.append(P)
+    return out
+
+
+def contract_mpo_mpo(A: Cores, B: Cores) -> Cores:
+    """Raw per-site ``A @ B`` (matrix_product_operator.py:279-288), output leg
+    of size ``B.out``."""
+    _check(A)
+    _check(B)
+    out = []
+    st = L.stream_ptr()
+    for a_, b_ in zip(A, B):
+        b, i, m, b2 = a_.shape
+        c, m2, o, c2 = b_.shape
+        if m != m2:
+            raise ValueError("contracted leg mismatch: %d vs %d" % (m, m2))
+        P = empty((b * c, i, o, b2 * c2))
+        L.call("sgt_site_contract_mpo_mpo", L.ptr(a_), b, i, m, b2, L.ptr(b_), c, o, c2, L.ptr(P), st)
+        out.append(P)
+    return out
+
+
+# ---------------------------------------------------------------------------
+# direct sum
+# ---------------------------------------------------------------------------
+
+def concat(A: Cores, B: Cores) -> Cores:
+    """Bond concatenation of two chains in one launch
+    (matrix_product_state.py:75-100, matrix_product_operator.py:84-108)."""
+    _check(A)
+    _check(B)
+    n = len(A)
+    outs = []
+    for k, (a, b) in enumerate(zip(A, B)):
+        if tuple(a.shape[1:-1]) != tuple(b.shape[1:-1]):
+            raise ValueError("physical legs differ at site %d" % k)
+        la, ra, lb, rb = a.shape[0], a.shape[-1], b.shape[0], b.shape[-1]
+        if n == 1:
+            ol, orr = la, ra
+        elif k == 0:
+            ol, orr = la, ra + rb
+        elif k == n - 1:
+            ol, orr = la + lb, ra
+        else:
+            ol, orr = la + lb, ra + rb
+        outs.append(empty((ol,) + tuple(a.shape[1:-1]) + (orr,)))
+    ap, _a = L.ptr_array(A)
+    bp, _b = L.ptr_array(B)
+    op, _o = L.ptr_array(outs)
+    ash, _as = L.shape_array([shape3(a) for a in A])
+    bsh, _bs = L.shape_array([shape3(b) for b in B])
+    L.call("sgt_bond_concat_chain", n, ap, ash, bp, bsh, op, None, 0, L.stream_ptr())
+    return outs
+
+
+# ---------------------------------------------------------------------------
+# overlap
+# ---------------------------------------------------------------------------
+
+def overlap_device(X: Cores, Y: Cores) -> torch.Tensor:
+    """Transfer sweep; returns a device tensor ``(mantissa, exponent2)`` with
+    ``<X|Y> = mantissa * 2**exponent2`` (no synchronisation)."""
+    _check(X)
+    _check(Y)
+    n = len(X)
+    if len(Y) != n:
+        raise ValueError("chains have different lengths")
+    xs, _x = L.shape_array([shape3(c) for c in X])
+    ys, _y = L.shape_array([shape3(c) for c in Y])
+    ws = L.workspace(L.query("sgt_overlap_workspace_size", n, xs, ys))
+    res = torch.empty(2, dtype=torch.float64, device=L.device())
+    xp, _xp = L.ptr_array(X)
+    yp, _yp = L.ptr_array(Y)
+    L.call("sgt_overlap_sweep", n, xp, xs, yp, ys, L.ptr(res), L.ptr(ws), ws.numel(), L.stream_ptr())
+    return res
+
+
+def decode_overlap(res) -> float:
+    m, e = (float(v) for v in res)
+    try:
+        return math.ldexp(m, int(e))
+    except OverflowError:
+        return math.copysign(math.inf, m)
+
+
+def overlap(X: Cores, Y: Cores) -> float:
+    """``X | Y`` (matrix_product_state.py:116-127), as a Python float."""
+    return decode_overlap(overlap_device(X, Y).cpu().tolist())
+
+
+# ---------------------------------------------------------------------------
+# QR truncation (reference >>) and decompose
+# ---------------------------------------------------------------------------
+
+def qr_truncate(cores: Cores, dim: int) -> Cores:
+    """Left QR-column truncation to ``dim`` (matrix_product_state.py:432-468).
+    Raises ValueError where the reference's reshape fails (l*p < dim)."""
+    _check(cores)
+    n = len(cores)
+    shp = [shape3(c) for c in cores]
+    sh, _s = L.shape_array(shp)
+    outs = []
+    for k, c in enumerate(cores):
+        l = c.shape[0] if k == 0 else dim
+        r = c.shape[-1] if k == n - 1 else dim
+        outs.append(empty((l,) + tuple(c.shape[1:-1]) + (r,)))
+    nbytes = L.query("sgt_qr_truncate_workspace_size", n, sh, dim)
+    if nbytes == 0:
+        # size query fails exactly when the call would: surface its message
+        lib = L.load()
+        msg = lib.sgt_last_error().decode(errors="replace")
+        if "reshape" in msg:
+            raise ValueError(msg)
+        raise L.SyngularError("sgt_qr_truncate_workspace_size", 1, msg)
+    ws = L.workspace(nbytes)
+    cp, _c = L.ptr_array(cores)
+    op, _o = L.ptr_array(outs)
+    L.call("sgt_qr_truncate_sweep", n, cp, sh, dim, op, L.ptr(ws), ws.numel(), L.stream_ptr())
+    return outs
+
+
+def decompose(tensor: torch.Tensor, phys: Sequence[int], bonds: Sequence[int], core_shapes,
+              mode: int = 0) -> Cores:
+    """Dense tensor -> cores (matrix_product_state.py:296-350)."""
+    t = L.as_device(tensor)
+    n = len(phys)
+    ph, _p = L.i64_array(phys)
+    bd, _b = L.i64_array(list(bonds) if len(bonds) else [1])
+    nbytes = L.query("sgt_decompose_workspace_size", n, ph, bd, mode)
+    if nbytes == 0:
+        msg = L.load().sgt_last_error().decode(errors="replace")
+        if "reshape" in msg:
+            raise ValueError(msg)
+        raise L.SyngularError("sgt_decompose_workspace_size", 1, msg)
+    ws = L.workspace(nbytes)
+    outs = [empty(s) for s in core_shapes]
+    op, _o = L.ptr_array(outs)
+    L.call("sgt_decompose", L.ptr(t), n, ph, bd, mode, op, L.ptr(ws), ws.numel(), L.stream_ptr())
+    return outs
+
+
+# ---------------------------------------------------------------------------
+# orthonormalisation / orthogonality / normalisation
+# ---------------------------------------------------------------------------
+
+def _orth(cores: Cores, fn: str):
+    _check(cores)
+    n = len(cores)
+    sh, _s = L.shape_array([shape3(c) for c in cores])
+    ws = L.workspace(L.query("sgt_orthonormalize_workspace_size", n, sh))
+    cp, _c = L.ptr_array(cores)
+    L.call(fn, n, cp, sh, L.ptr(ws), ws.numel(), L.stream_ptr())
+
+
+def left_orthonormalize(cores: Cores):
+    """In place (matrix_product_state.py:554-566)."""
+    _orth(cores, "sgt_left_orthonormalize")
+
+
+def right_orthonormalize(cores: Cores):
+    """In place (matrix_product_state.py:568-580)."""
+    _orth(cores, "sgt_right_orthonormalize")
+
+
+def orthogonality(core: torch.Tensor, side: int) -> torch.Tensor:
+    """``L^T L`` (side 0) or ``R R^T`` (side 1) of one core, on the device."""
+    _check([core])
+    l, p, r = shape3(core)
+    d = r if side == 0 else l
+    out = empty((d, d))
+    L.call("sgt_orthogonality", L.ptr(core), l, p, r, side, L.ptr(out), L.stream_ptr())
+    return out
+
+
+def normalize_(core: torch.Tensor) -> torch.Tensor:
+    """Divide ``core`` by its Frobenius norm in place; returns the device norm."""
+    _check([core])
+    norm = torch.empty(1, dtype=torch.float64, device=L.device())
+    L.call("sgt_normalize", L.ptr(core), core.numel(), L.ptr(norm), L.stream_ptr())
+    return norm
+
+
+# ---------------------------------------------------------------------------
+# TT-SVD rounding
+# ---------------------------------------------------------------------------
+
+def svd_round_shapes(cores: Cores, chi: int):
+    n = len(cores)
+    sh, _s = L.shape_array([shape3(c) for c in cores])
+    out = (ctypes.c_int64 * (3 * n))()
+    cnt = (ctypes.c_int64 * max(1, n - 1))()
+    L.call("sgt_svd_round_shapes", n, sh, chi, ctypes.cast(out, L._PI64), ctypes.cast(cnt, L._PI64))
+    shapes = [(out[3 * k], out[3 * k + 1], out[3 * k + 2]) for k in range(n)]
+    return shapes, [cnt[k] for k in range(n - 1)]
+
+
+def svd_round(cores: Cores, chi: int, precision: int = L.PREC_F64):
+    """TT-SVD rounding to ``chi``.  Returns ``(cores, spectra, discarded,
+    status)``: device tensors; ``spectra`` concatenates every bond's singular
+    values (``counts`` gives the split), ``status`` the Jacobi verdict."""
+    _check(cores)
+    n = len(cores)
+    shapes3, counts = svd_round_shapes(cores, chi)
+    sh, _s = L.shape_array([shape3(c) for c in cores])
+    nbytes = L.query("sgt_svd_round_workspace_size", n, sh, chi, precision)
+    if nbytes == 0:
+        msg = L.load().sgt_last_error().decode(errors="replace")
+        raise L.SyngularError("sgt_svd_round_workspace_size", 1, msg)
+    ws = L.workspace(nbytes)
+    outs = []
+    for k, c in enumerate(cores):
+        l, p, r = shapes3[k]
+        outs.append(empty((l,) + tuple(c.shape[1:-1]) + (r,)))
+    dev = L.device()
+    spectra = torch.zeros(max(1, sum(counts)), dtype=torch.float64, device=dev)
+    disc = torch.zeros(max(1, n - 1), dtype=torch.float64, device=dev)
+    status = torch.zeros(1, dtype=torch.int32, device=dev)
+    cp, _c = L.ptr_array(cores)
+    op, _o = L.ptr_array(outs)
+    L.call("sgt_svd_round", n, cp, sh, chi, precision, op, L.ptr(spectra), L.ptr(disc), L.ptr(status),
+           L.ptr(ws), ws.numel(), L.stream_ptr())
+    return outs, spectra, counts, disc, status
+
+
+# ---------------------------------------------------------------------------
+# dense reconstruction / element retrieval (chains of GEMMs)
+# ---------------------------------------------------------------------------
+
+def _gemm(ta, tb, M, N, K, alpha, A, lda, B, ldb, beta, C, ldc, aoff=0, boff=0):
+    L.call("sgt_gemm_f64", int(ta), int(tb), M, N, K, alpha,
+           L._c_vp(A.data_ptr() + 8 * aoff), lda, 0, L._c_vp(B.data_ptr() + 8 * boff), ldb, 0,
+           beta, L.ptr(C), ldc, 0, 1, L.stream_ptr())
+
+
+def to_tensor_device(cores: Cores) -> torch.Tensor:
+    """Contract the whole chain: ``(prod phys)`` tensor (row-major over the
+    flattened physical legs), on the device."""
+    _check(cores)
+    l0, p0, r0 = shape3(cores[0])
+    T = cores[0].reshape(l0 * p0, r0)
+    rows = l0 * p0
+    for c in cores[1:]:
+        l, p, r = shape3(c)
+        out = empty((rows, p * r))
+        _gemm(False, False, rows, p * r, l, 1.0, T, l, c, p * r, 0.0, out, p * r)
+        rows = rows * p
+        T = out.reshape(rows, r)
+    return T.reshape(-1)
+
+
+def retrieve(cores: Cores, indices: Sequence[int]) -> float:
+    """One element (matrix_product_state.py:546-551): product of the slices
+    ``core_k[:, i_k, :]``."""
+    _check(cores)
+    v = torch.ones((1, 1), dtype=torch.float64, device=L.device())
+    for c, i in zip(cores, indices):
+        l, p, r = shape3(c)
+        nv = empty((1, r))
+        _gemm(False, False, 1, r, l, 1.0, v, l, c, p * r, 0.0, nv, r, boff=int(i) * r)
+        v = nv
+    return float(v.reshape(-1)[0].item())

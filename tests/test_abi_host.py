@@ -1,0 +1,93 @@
+"""CPU-side checks of the C-ABI library and the host logic (no GPU calls)."""
+import os
+import re
+
+import numpy as np
+import pytest
+
+from tests.conftest import ROOT
+
+
+@pytest.fixture(scope="module")
+def lib():
+    import __graft_entry__ as g
+
+    g.build()
+    from syngular_gb300 import _lib
+
+    return _lib.load()
+
+
+def header_symbols():
+    with open(os.path.join(ROOT, "include", "syngular_gb300.h")) as f:
+        text = f.read()
+    return sorted(set(re.findall(r"SGT_API\s+[\w\s\*]+?\b(sgt_\w+)\s*\(", text)))
+
+
+def test_header_lists_entry_points():
+    syms = header_symbols()
+    assert "sgt_svd_round" in syms and "sgt_overlap_sweep" in syms
+    assert len(syms) >= 20
+
+
+def test_library_exports_every_header_symbol(lib):
+    for name in header_symbols():
+        assert hasattr(lib, name), name
+
+
+def test_ctypes_signatures_cover_header(lib):
+    from syngular_gb300 import _lib
+
+    missing = [s for s in header_symbols() if s not in _lib.SIGNATURES]
+    assert not missing, missing
+
+
+def test_version_and_error_string(lib):
+    assert lib.sgt_version() >= 1
+    assert isinstance(lib.sgt_last_error(), bytes)
+
+
+def test_workspace_queries_and_shape_checks(lib):
+    """Size queries run on the host only; they validate shapes like the calls."""
+    from syngular_gb300 import _lib as L
+
+    sh, _k = L.shape_array([(1, 2, 4), (4, 2, 4), (4, 2, 1)])
+    assert L.query("sgt_overlap_workspace_size", 3, sh, sh) > 0
+    assert L.query("sgt_qr_truncate_workspace_size", 3, sh, 2) > 0
+    # l*p < dim at the first site: the reference's reshape fails, so does the query
+    assert L.query("sgt_qr_truncate_workspace_size", 3, sh, 4) == 0
+    assert b"reshape" in lib.sgt_last_error()
+    bad, _b = L.shape_array([(1, 2, 4), (3, 2, 1)])
+    assert L.query("sgt_overlap_workspace_size", 2, bad, bad) == 0
+    assert b"bond mismatch" in lib.sgt_last_error()
+
+
+def test_svd_round_shapes_match_oracle(lib):
+    from oracle import tt_fp64 as O
+    from syngular_gb300 import _lib as L
+    import ctypes
+
+    rng = np.random.default_rng(3)
+    for n, d, chi, D, cut in [(6, 2, 8, 3, 5), (5, 3, 4, 2, 7), (8, 2, 16, 4, 6)]:
+        X = O.random_mps_cores(rng, n, d, chi)
+        W = O.random_mpo_cores(rng, n, d, D)
+        P = O.mpo_mps_product(W, X)
+        Z, spec, _ = O.tt_svd_round(P, cut)
+        sh, _k = L.shape_array([c.shape for c in P])
+        out = (ctypes.c_int64 * (3 * n))()
+        cnt = (ctypes.c_int64 * (n - 1))()
+        assert lib.sgt_svd_round_shapes(n, sh, cut, ctypes.cast(out, L._PI64), ctypes.cast(cnt, L._PI64)) == 0
+        got = [(out[3 * k], out[3 * k + 1], out[3 * k + 2]) for k in range(n)]
+        assert got == [c.shape for c in Z]
+        assert [cnt[k] for k in range(n - 1)] == [len(s) for s in spec]
+
+
+def test_no_cpu_fallback_without_gpu():
+    import torch
+
+    if torch.cuda.is_available():
+        pytest.skip("a GPU is present")
+    from syngular_gb300.tensor import MatrixProductState
+
+    with pytest.raises(RuntimeError, match="CUDA"):
+        MatrixProductState.zeros((2, 2), (2,))
