@@ -197,6 +197,22 @@ SGT_API size_t sgt_jacobi_svd_workspace_size(int64_t m, int64_t n);
 SGT_API int sgt_jacobi_svd(double* A, int64_t m, int64_t n, double* V, double* s, int* status,
                    void* ws, size_t ws_bytes, void* stream);
 
+/* Tensor-core GEMM (tcgen05, kind::tf32, TMA-staged operands, TMEM accumulator):
+ * C (M x N, fp32) = alpha * A B^T + beta * C with A (M x K) and B (N x K)
+ * row-major fp32, leading dimensions multiples of 4, 16-byte aligned bases.
+ * passes = 1: TF32 inputs.  passes = 3: split precision, A_hi/B_hi the TF32
+ * parts and A_lo/B_lo the residuals (from sgt_split_tf32), accumulating
+ * A_hi B_hi + A_hi B_lo + A_lo B_hi in FP32.  `err` (device int, may be NULL)
+ * is set to 1 if a pipeline wait timed out.  GEMM-shaped work of the
+ * mixed-precision forms (product carries, trailing updates, transfer sweeps). */
+SGT_API int sgt_tc_gemm_f32(int passes, int64_t M, int64_t N, int64_t K, float alpha,
+                            const float* A_hi, const float* A_lo, int64_t lda,
+                            const float* B_hi, const float* B_lo, int64_t ldb, float beta,
+                            float* C, int64_t ldc, int* err, void* stream);
+
+/* hi = TF32 rounding of x (round to nearest, ties away), lo = x - hi (lo may be NULL). */
+SGT_API int sgt_split_tf32(const float* x, float* hi, float* lo, int64_t n, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -1,0 +1,54 @@
+"""tcgen05 TF32 / 3xTF32 GEMM against an FP64 reference of the same product.
+Tolerances: TF32 (10-bit mantissa) 5e-3 relative Frobenius error; 3xTF32 2e-6."""
+import numpy as np
+import pytest
+import torch
+
+from tests.conftest import rel
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module", autouse=True)
+def built():
+    import __graft_entry__ as g
+
+    g.build()
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+
+
+def run(M, N, K, passes, ldpad=0, beta=0.0, seed=0):
+    from syngular_gb300 import _lib as L
+
+    rng = np.random.default_rng(seed)
+    lda = ldb = K + ldpad
+    A = rng.standard_normal((M, lda)).astype(np.float32)
+    B = rng.standard_normal((N, ldb)).astype(np.float32)
+    C0 = rng.standard_normal((M, N)).astype(np.float32)
+    ref = 0.75 * A[:, :K].astype(np.float64) @ B[:, :K].astype(np.float64).T + beta * C0.astype(np.float64)
+    dev = torch.device("cuda")
+    Ad, Bd, Cd = (torch.from_numpy(x).to(dev) for x in (A, B, C0))
+    err = torch.zeros(1, dtype=torch.int32, device=dev)
+    if passes == 3:
+        Ah, Al, Bh, Bl = (torch.empty_like(t) for t in (Ad, Ad, Bd, Bd))
+        L.call("sgt_split_tf32", L.ptr(Ad), L.ptr(Ah), L.ptr(Al), Ad.numel(), L.stream_ptr())
+        L.call("sgt_split_tf32", L.ptr(Bd), L.ptr(Bh), L.ptr(Bl), Bd.numel(), L.stream_ptr())
+    else:
+        Ah, Al, Bh, Bl = Ad, None, Bd, None
+    L.call("sgt_tc_gemm_f32", passes, M, N, K, 0.75, L.ptr(Ah), L.ptr(Al) if Al is not None else None, lda,
+           L.ptr(Bh), L.ptr(Bl) if Bl is not None else None, ldb, beta, L.ptr(Cd), N, L.ptr(err), L.stream_ptr())
+    torch.cuda.synchronize()
+    assert int(err.item()) == 0
+    return rel(Cd.cpu().numpy(), ref)
+
+
+@pytest.mark.parametrize("M,N,K,pad", [(128, 128, 32, 0), (256, 384, 512, 0), (200, 300, 100, 0),
+                                       (1000, 136, 77, 3), (4096, 512, 4096, 0)])
+def test_tf32(M, N, K, pad):
+    assert run(M, N, K, 1, pad) < 5e-3
+
+
+@pytest.mark.parametrize("M,N,K", [(128, 128, 32), (300, 260, 1000), (2048, 1024, 2048)])
+def test_3xtf32(M, N, K):
+    assert run(M, N, K, 3, beta=0.5) < 2e-6
