@@ -52,9 +52,12 @@ extern "C" {
 #define SGT_PREC_TF32 1    /* GEMM-shaped work on tcgen05 kind::tf32, FP32 accumulate */
 #define SGT_PREC_BF16 2    /* GEMM-shaped work on tcgen05 kind::f16 with bf16 inputs */
 #define SGT_PREC_BF16X3 3  /* split bf16 (hi*hi + hi*lo + lo*hi) on tcgen05, FP32 accumulate */
+#define SGT_PREC_TF32X3 4  /* split tf32 (hi*hi + hi*lo + lo*hi) on tcgen05, FP32 accumulate */
 
 SGT_API int sgt_version(void);
 SGT_API const char* sgt_last_error(void);
+/* Number of kernels this library has launched in the process so far. */
+SGT_API unsigned long long sgt_launch_count(void);
 
 /* ----------------------------------------------------------------------
  * Site contractions (raw products, no rounding)
@@ -168,6 +171,26 @@ SGT_API size_t sgt_svd_round_workspace_size(int n, const int64_t* shape, int64_t
 SGT_API int sgt_svd_round(int n, const double* const* cores, const int64_t* shape, int64_t chi,
                   int precision, double* const* out, double* spectra, double* discarded,
                   int* status, void* ws, size_t ws_bytes, void* stream);
+
+/* ----------------------------------------------------------------------
+ * The metric operation: raw MPO x MPS product (W @ X without the reference's
+ * auto-round, mpo:183-191) followed by TT-SVD rounding to chi, in one call.
+ * wshape: 4n entries (b, in, out, b2) per operator core; xshape: 3n entries.
+ * Output cores (chi_k, out_k, chi_{k+1}) as given by sgt_svd_round_shapes on
+ * the product shapes (a*b, out, a2*b2); spectra / discarded / status as for
+ * sgt_svd_round (status -2: a tensor-core pipeline wait timed out).
+ * precision SGT_PREC_F64: plain FP64 (product + Householder QR sweep + Jacobi).
+ * SGT_PREC_TF32 / SGT_PREC_TF32X3: Gram form on tcgen05 -- product cores and
+ * left Gram matrices in FP32, every O(R^3) step a TF32 (one pass) or split
+ * 3xTF32 GEMM, eigen-solves by one-sided Jacobi (FP32 columns, FP64 angles).
+ * -------------------------------------------------------------------- */
+SGT_API size_t sgt_mpo_mps_round_workspace_size(int n, const int64_t* wshape, const int64_t* xshape,
+                                                int64_t chi, int precision);
+SGT_API int sgt_mpo_mps_round(int n, const double* const* W, const int64_t* wshape,
+                              const double* const* X, const int64_t* xshape, int64_t chi,
+                              int precision, double* const* out, double* spectra,
+                              double* discarded, int* status, void* ws, size_t ws_bytes,
+                              void* stream);
 
 /* ----------------------------------------------------------------------
  * Dense primitives (exported for composition and tests)

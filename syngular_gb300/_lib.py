@@ -28,6 +28,7 @@ PREC_F64 = 0
 PREC_TF32 = 1
 PREC_BF16 = 2
 PREC_BF16X3 = 3
+PREC_TF32X3 = 4
 
 _c_i64 = ctypes.c_int64
 _c_vp = ctypes.c_void_p
@@ -67,6 +68,9 @@ SIGNATURES = {
     "sgt_jacobi_svd": (_c_int, [_c_vp, _c_i64, _c_i64, _c_vp, _c_vp, _c_vp, _c_vp, _c_size, _c_vp]),
     "sgt_tc_gemm_f32": (_c_int, [_c_int, _c_i64, _c_i64, _c_i64, ctypes.c_float, _c_vp, _c_vp, _c_i64, _c_vp, _c_vp, _c_i64, ctypes.c_float, _c_vp, _c_i64, _c_vp, _c_vp]),
     "sgt_split_tf32": (_c_int, [_c_vp, _c_vp, _c_vp, _c_i64, _c_vp]),
+    "sgt_launch_count": (ctypes.c_ulonglong, []),
+    "sgt_mpo_mps_round_workspace_size": (_c_size, [_c_int, _PI64, _PI64, _c_i64, _c_int]),
+    "sgt_mpo_mps_round": (_c_int, [_c_int, _PP, _PI64, _PP, _PI64, _c_i64, _c_int, _PP, _c_vp, _c_vp, _c_vp, _c_vp, _c_size, _c_vp]),
 }
 
 _lib = None

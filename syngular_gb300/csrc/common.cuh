@@ -26,8 +26,13 @@ const char* get_error();
     }                                                                                      \
   } while (0)
 
+// Every kernel launch of the library bumps a process-wide counter
+// (sgt_launch_count), which benchmarks read around their timed region.
+void note_launch();
+
 #define SGT_LAUNCHED()                                                                     \
   do {                                                                                     \
+    ::sgt::note_launch();                                                                  \
     cudaError_t e_ = cudaGetLastError();                                                   \
     if (e_ != cudaSuccess) {                                                               \
       ::sgt::set_error("%s:%d: kernel launch: %s", __FILE__, __LINE__, cudaGetErrorString(e_)); \

@@ -232,6 +232,7 @@ int launch_panel(cudaStream_t st, double* A, int64_t m, int64_t lda, int64_t j0,
   cfg.attrs = attr;
   cfg.numAttrs = 1;
   SGT_CUDA(cudaLaunchKernelEx(&cfg, panel_kernel, A, m, lda, j0, jb, tau, Vbuf));
+  note_launch();
   return SGT_OK;
 }
 

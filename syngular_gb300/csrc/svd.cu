@@ -38,10 +38,20 @@ __device__ __forceinline__ int rr_index(int i, int s, int np) {
   return i == 0 ? 0 : ((i - 1 + s) % (np - 1)) + 1;
 }
 
-__global__ void __launch_bounds__(JAC_THREADS) jacobi_kernel(double* __restrict__ G, int64_t ldg,
-                                                             double* __restrict__ Vt, int64_t ldv,
+template <typename T>
+__device__ __forceinline__ T wsum_t(T v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
+
+// T = double: plain FP64.  T = float: the column data and dot products are
+// FP32 (warp-shuffle trees); the rotation angle is still formed in FP64.
+template <typename T>
+__global__ void __launch_bounds__(JAC_THREADS) jacobi_kernel(T* __restrict__ G, int64_t ldg,
+                                                             T* __restrict__ Vt, int64_t ldv,
                                                              int n, int64_t m, double tol,
-                                                             double* __restrict__ norms,
+                                                             T* __restrict__ norms,
                                                              int* __restrict__ status) {
   cg::cluster_group cluster = cg::this_cluster();
   const int cs = (int)cluster.num_blocks();
@@ -70,33 +80,34 @@ __global__ void __launch_bounds__(JAC_THREADS) jacobi_kernel(double* __restrict_
           p = q;
           q = t;
         }
-        double* gp = G + (int64_t)p * ldg;
-        double* gq = G + (int64_t)q * ldg;
-        double a = 0.0, b = 0.0, c = 0.0;
+        T* gp = G + (int64_t)p * ldg;
+        T* gq = G + (int64_t)q * ldg;
+        T a = 0, b = 0, c = 0;
         for (int64_t e = lane; e < m; e += 32) {
-          double x = gp[e], y = gq[e];
+          T x = gp[e], y = gq[e];
           a = fma(x, x, a);
           b = fma(y, y, b);
           c = fma(x, y, c);
         }
-        a = wsum(a);
-        b = wsum(b);
-        c = wsum(c);
-        if (c != 0.0 && fabs(c) > tol * sqrt(a) * sqrt(b)) {
+        a = wsum_t(a);
+        b = wsum_t(b);
+        c = wsum_t(c);
+        const double da = (double)a, db = (double)b, dc = (double)c;
+        if (dc != 0.0 && fabs(dc) > tol * sqrt(da) * sqrt(db)) {
           ++my_rot;
-          double zeta = (b - a) / (2.0 * c);
+          double zeta = (db - da) / (2.0 * dc);
           double t = copysign(1.0, zeta) / (fabs(zeta) + hypot(1.0, zeta));
-          double cs_ = 1.0 / sqrt(fma(t, t, 1.0));
-          double sn = cs_ * t;
+          double cd = 1.0 / sqrt(fma(t, t, 1.0));
+          const T cs_ = (T)cd, sn = (T)(cd * t);
           for (int64_t e = lane; e < m; e += 32) {
-            double x = gp[e], y = gq[e];
+            T x = gp[e], y = gq[e];
             gp[e] = cs_ * x - sn * y;
             gq[e] = sn * x + cs_ * y;
           }
-          double* vp = Vt + (int64_t)p * ldv;
-          double* vq = Vt + (int64_t)q * ldv;
+          T* vp = Vt + (int64_t)p * ldv;
+          T* vq = Vt + (int64_t)q * ldv;
           for (int e = lane; e < n; e += 32) {
-            double x = vp[e], y = vq[e];
+            T x = vp[e], y = vq[e];
             vp[e] = cs_ * x - sn * y;
             vq[e] = sn * x + cs_ * y;
           }
@@ -119,38 +130,41 @@ __global__ void __launch_bounds__(JAC_THREADS) jacobi_kernel(double* __restrict_
   }
   // row norms = singular values
   for (int j = gw; j < n; j += nw) {
-    const double* gj = G + (int64_t)j * ldg;
-    double a = 0.0;
+    const T* gj = G + (int64_t)j * ldg;
+    T a = 0;
     for (int64_t e = lane; e < m; e += 32) a = fma(gj[e], gj[e], a);
-    a = wsum(a);
+    a = wsum_t(a);
     if (lane == 0) norms[j] = sqrt(a);
   }
   if (rank == 0 && threadIdx.x == 0 && status) *status = converged ? sweeps : -1;
   cluster.sync();
 }
 
-__global__ void eye_rows_kernel(double* Vt, int64_t ldv, int n) {
+template <typename T>
+__global__ void eye_rows_kernel(T* Vt, int64_t ldv, int n) {
   for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < (int64_t)n * n;
        i += (int64_t)gridDim.x * blockDim.x) {
     int64_t r = i / n, c = i % n;
-    Vt[r * ldv + c] = (r == c) ? 1.0 : 0.0;
+    Vt[r * ldv + c] = (r == c) ? T(1) : T(0);
   }
 }
 
 // perm[j] = position of row j in descending order of norms (ties by index).
-__global__ void rank_kernel(const double* __restrict__ norms, int n, int* __restrict__ perm) {
+template <typename T>
+__global__ void rank_kernel(const T* __restrict__ norms, int n, int* __restrict__ perm) {
   for (int j = threadIdx.x; j < n; j += blockDim.x) {
-    double v = norms[j];
+    T v = norms[j];
     int r = 0;
     for (int i = 0; i < n; ++i) {
-      double w = norms[i];
+      T w = norms[i];
       r += (w > v) || (w == v && i < j);
     }
     perm[j] = r;
   }
 }
 
-__global__ void permute_rows_kernel(const double* __restrict__ src, int64_t lds, double* __restrict__ dst,
+template <typename T>
+__global__ void permute_rows_kernel(const T* __restrict__ src, int64_t lds, T* __restrict__ dst,
                                     int64_t ldd, int64_t cols, const int* __restrict__ perm, int n) {
   for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < (int64_t)n * cols;
        i += (int64_t)gridDim.x * blockDim.x) {
@@ -159,7 +173,8 @@ __global__ void permute_rows_kernel(const double* __restrict__ src, int64_t lds,
   }
 }
 
-__global__ void permute_vec_kernel(const double* __restrict__ src, double* __restrict__ dst,
+template <typename T>
+__global__ void permute_vec_kernel(const T* __restrict__ src, T* __restrict__ dst,
                                    const int* __restrict__ perm, int n) {
   for (int j = blockIdx.x * blockDim.x + threadIdx.x; j < n; j += gridDim.x * blockDim.x)
     dst[perm[j]] = src[j];
@@ -171,36 +186,49 @@ inline unsigned g1(int64_t n) {
 
 }  // namespace
 
-size_t jacobi_rows_ws_bytes(int64_t n, int64_t m) {
+template <typename T>
+size_t jacobi_rows_ws_bytes_t(int64_t n, int64_t m) {
   Arena a = Arena::measuring();
-  a.take<double>((size_t)n * m);
-  a.take<double>((size_t)n * n);
-  a.take<double>((size_t)n);
+  a.take<T>((size_t)n * m);
+  a.take<T>((size_t)n * n);
+  a.take<T>((size_t)n);
   a.take<int>((size_t)n);
   return a.used;
 }
 
+size_t jacobi_rows_ws_bytes(int64_t n, int64_t m) { return jacobi_rows_ws_bytes_t<double>(n, m); }
+size_t jacobi_rows_ws_bytes_f32(int64_t n, int64_t m) { return jacobi_rows_ws_bytes_t<float>(n, m); }
+
 // Orthogonalise the n rows (length m) of G; Vt (n x n) receives V^T, s the
 // descending singular values, rows of G and Vt sorted accordingly.
-int jacobi_rows(cudaStream_t st, double* G, int64_t ldg, int64_t n, int64_t m, double* Vt,
-                int64_t ldv, double* s, int* status, Arena& ar) {
+template <typename T>
+int jacobi_rows_t(cudaStream_t st, T* G, int64_t ldg, int64_t n, int64_t m, T* Vt, int64_t ldv, T* s,
+                  int* status, Arena& ar) {
   if (n <= 0) return SGT_OK;
   SGT_REQUIRE(n <= (1 << 20), SGT_ERR_INVALID, "jacobi: n too large");
-  double* Gtmp = ar.take<double>((size_t)n * m);
-  double* Vtmp = ar.take<double>((size_t)n * n);
-  double* norms = ar.take<double>((size_t)n);
+  T* Gtmp = ar.take<T>((size_t)n * m);
+  T* Vtmp = ar.take<T>((size_t)n * n);
+  T* norms = ar.take<T>((size_t)n);
   int* perm = ar.take<int>((size_t)n);
   SGT_REQUIRE(ar.ok(), SGT_ERR_WORKSPACE, "jacobi: workspace too small");
 
-  eye_rows_kernel<<<g1(n * n), 256, 0, st>>>(Vt, ldv, (int)n);
+  eye_rows_kernel<T><<<g1(n * n), 256, 0, st>>>(Vt, ldv, (int)n);
   SGT_LAUNCHED();
 
   int cs = 1;
   const int64_t pairs = (n + 1) / 2;
-  if (pairs >= 8 * JAC_WARPS) cs = 8;
+  if (pairs >= 16 * JAC_WARPS) cs = 16;
+  else if (pairs >= 8 * JAC_WARPS) cs = 8;
   else if (pairs >= 4 * JAC_WARPS) cs = 4;
   else if (pairs >= 2 * JAC_WARPS) cs = 2;
-  const double tol = DBL_EPSILON * sqrt((double)std::max<int64_t>(m, 1));
+  static bool nonportable = false;
+  if (!nonportable) {
+    SGT_CUDA(cudaFuncSetAttribute(jacobi_kernel<double>, cudaFuncAttributeNonPortableClusterSizeAllowed, 1));
+    SGT_CUDA(cudaFuncSetAttribute(jacobi_kernel<float>, cudaFuncAttributeNonPortableClusterSizeAllowed, 1));
+    nonportable = true;
+  }
+  const double eps = (sizeof(T) == 8) ? DBL_EPSILON : (double)FLT_EPSILON;
+  const double tol = eps * sqrt((double)std::max<int64_t>(m, 1));
   cudaLaunchConfig_t cfg = {};
   cfg.gridDim = dim3(cs, 1, 1);
   cfg.blockDim = dim3(JAC_THREADS, 1, 1);
@@ -212,19 +240,32 @@ int jacobi_rows(cudaStream_t st, double* G, int64_t ldg, int64_t n, int64_t m, d
   attr[0].val.clusterDim.z = 1;
   cfg.attrs = attr;
   cfg.numAttrs = 1;
-  SGT_CUDA(cudaLaunchKernelEx(&cfg, jacobi_kernel, G, ldg, Vt, ldv, (int)n, m, tol, norms, status));
+  SGT_CUDA(cudaLaunchKernelEx(&cfg, jacobi_kernel<T>, G, ldg, Vt, ldv, (int)n, m, tol, norms, status));
+  note_launch();
 
-  rank_kernel<<<1, 256, 0, st>>>(norms, (int)n, perm);
+  rank_kernel<T><<<1, 256, 0, st>>>(norms, (int)n, perm);
   SGT_LAUNCHED();
-  permute_rows_kernel<<<g1(n * m), 256, 0, st>>>(G, ldg, Gtmp, m, m, perm, (int)n);
+  permute_rows_kernel<T><<<g1(n * m), 256, 0, st>>>(G, ldg, Gtmp, m, m, perm, (int)n);
   SGT_LAUNCHED();
-  permute_rows_kernel<<<g1(n * n), 256, 0, st>>>(Vt, ldv, Vtmp, n, n, perm, (int)n);
+  permute_rows_kernel<T><<<g1(n * n), 256, 0, st>>>(Vt, ldv, Vtmp, n, n, perm, (int)n);
   SGT_LAUNCHED();
-  permute_vec_kernel<<<g1(n), 256, 0, st>>>(norms, s, perm, (int)n);
+  permute_vec_kernel<T><<<g1(n), 256, 0, st>>>(norms, s, perm, (int)n);
   SGT_LAUNCHED();
-  SGT_TRY(copy2d_f64(st, G, ldg, Gtmp, m, n, m));
-  SGT_TRY(copy2d_f64(st, Vt, ldv, Vtmp, n, n, n));
+  SGT_CUDA(cudaMemcpy2DAsync(G, ldg * sizeof(T), Gtmp, m * sizeof(T), m * sizeof(T), n,
+                             cudaMemcpyDeviceToDevice, st));
+  SGT_CUDA(cudaMemcpy2DAsync(Vt, ldv * sizeof(T), Vtmp, n * sizeof(T), n * sizeof(T), n,
+                             cudaMemcpyDeviceToDevice, st));
   return SGT_OK;
+}
+
+int jacobi_rows(cudaStream_t st, double* G, int64_t ldg, int64_t n, int64_t m, double* Vt,
+                int64_t ldv, double* s, int* status, Arena& ar) {
+  return jacobi_rows_t<double>(st, G, ldg, n, m, Vt, ldv, s, status, ar);
+}
+
+int jacobi_rows_f32(cudaStream_t st, float* G, int64_t ldg, int64_t n, int64_t m, float* Vt,
+                    int64_t ldv, float* s, int* status, Arena& ar) {
+  return jacobi_rows_t<float>(st, G, ldg, n, m, Vt, ldv, s, status, ar);
 }
 
 }  // namespace sgt

@@ -40,8 +40,11 @@ size_t jacobi_rows_ws_bytes(int64_t n, int64_t m);
 int jacobi_rows(cudaStream_t st, double* G, int64_t ldg, int64_t n, int64_t m, double* Vt,
                 int64_t ldv, double* s, int* status, Arena& ar);
 
-// ---- error state -----------------------------------------------------------
+// ---- error state and launch counter -----------------------------------------
 static thread_local char g_err[512] = "";
+static unsigned long long g_launches = 0;
+
+void note_launch() { __atomic_fetch_add(&g_launches, 1ull, __ATOMIC_RELAXED); }
 
 void set_error(const char* fmt, ...) {
   va_list ap;
@@ -652,6 +655,24 @@ static int svd_round_impl(cudaStream_t st, int n, const double* const* cores, co
   return SGT_OK;
 }
 
+size_t svd_round_ws(int n, const int64_t* shape, int64_t chi) {
+  Arena a = Arena::measuring();
+  if (svd_round_impl(nullptr, n, nullptr, shape, chi, SGT_PREC_F64, nullptr, nullptr, nullptr, nullptr, a) !=
+      SGT_OK)
+    return 0;
+  return a.used;
+}
+
+int svd_round_run(cudaStream_t st, int n, const double* const* cores, const int64_t* shape, int64_t chi,
+                  double* const* out, double* spectra, double* discarded, int* status, Arena& ar) {
+  return svd_round_impl(st, n, cores, shape, chi, SGT_PREC_F64, out, spectra, discarded, status, ar);
+}
+
+void svd_round_plan_public(int n, const int64_t* shape, int64_t chi, std::vector<int64_t>& b,
+                           std::vector<int64_t>& x, std::vector<int64_t>& cnt) {
+  svd_round_plan(n, shapes_of(n, shape), chi, b, x, cnt);
+}
+
 }  // namespace sgt
 
 // ============================================================================
@@ -662,6 +683,7 @@ using namespace sgt;
 extern "C" {
 
 int sgt_version(void) { return 1; }
+unsigned long long sgt_launch_count(void) { return __atomic_load_n(&g_launches, __ATOMIC_RELAXED); }
 const char* sgt_last_error(void) { return get_error(); }
 
 int sgt_site_contract_mpo_mps(const double* X, int64_t a, int64_t p, int64_t a2, const double* W,

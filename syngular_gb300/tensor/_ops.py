@@ -313,3 +313,39 @@ def retrieve(cores: Cores, indices: Sequence[int]) -> float:
         _gemm(False, False, 1, r, l, 1.0, v, l, c, p * r, 0.0, nv, r, boff=int(i) * r)
         v = nv
     return float(v.reshape(-1)[0].item())
+
+
+# ---------------------------------------------------------------------------
+# fused metric operation: raw W @ X then TT-SVD round
+# ---------------------------------------------------------------------------
+
+def mpo_mps_round(W: Cores, X: Cores, chi: int, precision: int = L.PREC_F64):
+    """Raw ``W @ X`` followed by TT-SVD rounding to ``chi`` in one library call.
+    Returns ``(cores, spectra, counts, discarded, status)`` (device tensors)."""
+    _check(W)
+    _check(X)
+    n = len(X)
+    wsh, _w = L.i64_array([int(v) for w in W for v in w.shape])
+    xsh, _x = L.shape_array([tuple(x.shape) for x in X])
+    pshapes = [(X[k].shape[0] * W[k].shape[0], W[k].shape[2], X[k].shape[2] * W[k].shape[3]) for k in range(n)]
+    psh, _p = L.shape_array(pshapes)
+    out_arr = (ctypes.c_int64 * (3 * n))()
+    cnt_arr = (ctypes.c_int64 * max(1, n - 1))()
+    L.call("sgt_svd_round_shapes", n, psh, chi, ctypes.cast(out_arr, L._PI64), ctypes.cast(cnt_arr, L._PI64))
+    counts = [cnt_arr[k] for k in range(n - 1)]
+    nbytes = L.query("sgt_mpo_mps_round_workspace_size", n, wsh, xsh, chi, precision)
+    if nbytes == 0:
+        msg = L.load().sgt_last_error().decode(errors="replace")
+        raise L.SyngularError("sgt_mpo_mps_round_workspace_size", 1, msg)
+    ws = L.workspace(nbytes)
+    outs = [empty((out_arr[3 * k], out_arr[3 * k + 1], out_arr[3 * k + 2])) for k in range(n)]
+    dev = L.device()
+    spectra = torch.zeros(max(1, sum(counts)), dtype=torch.float64, device=dev)
+    disc = torch.zeros(max(1, n - 1), dtype=torch.float64, device=dev)
+    status = torch.zeros(1, dtype=torch.int32, device=dev)
+    wp, _wp = L.ptr_array(W)
+    xp, _xp = L.ptr_array(X)
+    op, _o = L.ptr_array(outs)
+    L.call("sgt_mpo_mps_round", n, wp, wsh, xp, xsh, chi, precision, op, L.ptr(spectra), L.ptr(disc),
+           L.ptr(status), L.ptr(ws), ws.numel(), L.stream_ptr())
+    return outs, spectra, counts, disc, status

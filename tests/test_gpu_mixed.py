@@ -1,0 +1,62 @@
+"""Fused MPO x MPS + TT-SVD round in every precision against the FP64 oracle.
+
+FP64: 1e-12 relative on gauge-invariant quantities.  Mixed precision (Gram form
+on tcgen05): the overlap <X|Z> is a small fraction of |X||Z| for a random
+operator, so its relative error is reported together with the error
+normalised by |X||Z|; tolerances: 3xTF32 normalised 1e-6 and kept singular
+values 1e-4 relative to the largest; one-pass TF32 normalised 1e-3."""
+import numpy as np
+import pytest
+import torch
+
+from oracle import tt_fp64 as O
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module", autouse=True)
+def built():
+    import __graft_entry__ as g
+
+    g.build()
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+
+
+def dev(cores):
+    from syngular_gb300 import _lib
+
+    return [_lib.as_device(c) for c in cores]
+
+
+CASES = [(6, 2, 8, 3, 5), (10, 2, 32, 4, 24), (8, 3, 16, 4, 20), (12, 2, 64, 8, 64)]
+
+
+@pytest.mark.parametrize("n,d,chi,D,cut", CASES)
+@pytest.mark.parametrize("prec,tol_norm,tol_spec", [(0, 1e-13, 1e-11), (4, 1e-6, 1e-4), (1, 1e-3, 3e-2)])
+def test_mpo_mps_round(n, d, chi, D, cut, prec, tol_norm, tol_spec):
+    from syngular_gb300.tensor import _ops
+
+    rng = np.random.default_rng(1000 * n + chi)
+    X = O.random_mps_cores(rng, n, d, chi)
+    W = O.random_mpo_cores(rng, n, d, D)
+    Zr, spec_r, disc_r = O.tt_svd_round(O.mpo_mps_product(W, X), cut)
+    Z, spec, counts, disc, status = _ops.mpo_mps_round(dev(W), dev(X), cut, prec)
+    torch.cuda.synchronize()
+    assert int(status.item()) >= 0
+    assert [tuple(z.shape) for z in Z] == [z.shape for z in Zr]
+    Xd = dev(X)
+    ov, ovr = _ops.overlap(Xd, Z), O.overlap(X, Zr)
+    nx, nz = np.sqrt(O.overlap(X, X)), np.sqrt(O.overlap(Zr, Zr))
+    assert abs(ov - ovr) / (nx * nz) < tol_norm
+    zz = _ops.overlap(Z, Z)
+    assert abs(zz - nz * nz) / (nz * nz) < max(tol_norm, 1e-12) * 10
+    s = spec.cpu().numpy()
+    off = 0
+    for k in range(n - 1):
+        m = min(counts[k], len(spec_r[k]), cut)
+        np.testing.assert_allclose(s[off:off + m], spec_r[k][:m], rtol=0, atol=tol_spec * spec_r[k][0])
+        off += counts[k]
+    if prec == 0:
+        assert abs(ov - ovr) <= 1e-11 * abs(ovr)
+        np.testing.assert_allclose(disc.cpu().numpy(), disc_r, rtol=1e-9, atol=1e-15)

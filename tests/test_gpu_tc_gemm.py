@@ -1,5 +1,7 @@
 """tcgen05 TF32 / 3xTF32 GEMM against an FP64 reference of the same product.
-Tolerances: TF32 (10-bit mantissa) 5e-3 relative Frobenius error; 3xTF32 2e-6."""
+Tolerances: TF32 (10-bit mantissa) 5e-3 relative Frobenius error; 3xTF32 3e-5
+(the split products are exact to ~2^-22, the FP32 tensor-core accumulation
+adds about sqrt(K) * 2^-23)."""
 import numpy as np
 import pytest
 import torch
@@ -51,4 +53,4 @@ def test_tf32(M, N, K, pad):
 
 @pytest.mark.parametrize("M,N,K", [(128, 128, 32), (300, 260, 1000), (2048, 1024, 2048)])
 def test_3xtf32(M, N, K):
-    assert run(M, N, K, 3, beta=0.5) < 2e-6
+    assert run(M, N, K, 3, beta=0.5) < 3e-5
