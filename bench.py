@@ -1,0 +1,401 @@
+"""Benchmark: MPO.MPS + TT-SVD-round sweeps/s at chi=256 (config 2).
+
+Workload (one "step" = one sweep): a random MPS with N=64 sites, d=2, uniform
+bond chi=256 (entries N(0,1)/sqrt(chi*d)) and a random MPO with N=64, d=2x2,
+bond D=16 (entries N(0,1)/sqrt(D*d)), both seeded and synthetic.  A sweep is
+the raw product W @ X (bond chi*D = 4096), its TT-SVD rounding back to chi=256
+and the overlap <X|Z> of the rounded state with the input.
+
+  value       sweeps/s of the chosen form (default: 3xTF32 Gram form on tcgen05)
+              with the cores already resident in HBM
+  e2e         the same through the public call with the input cores copied
+              from pinned host memory every step and <X|Z> read back
+  plain_fp64  sweeps/s of the plain FP64 GPU form (Householder QR + FP64
+              Jacobi), the denominator of the metric
+  roofline    the dominant kernel (the tcgen05 GEMM) timed with CUDA events
+              over the timed region
+  cpu_baseline the numpy FP64 port of the same sweep on the host cores, on a
+              bounded sample (one full-size middle site), scaled by flops
+
+`--impl reference` times that CPU port alone (the reference itself is pure
+Python/numpy and has no GPU path; its own MPS/MPO code cannot run this
+workload, see the design notes).  Under torchrun every rank runs an
+independent replica (the single-chain sweep does not shard).
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+N_SITES, D_PHYS, CHI, D_MPO = 64, 2, 256, 16
+SEED = 2024
+METRIC = "MPO·MPS+SVD-round sweeps/s at χ=256 vs plain FP64 GPU; p50/p99 job latency"
+WORKLOAD = "config2: MPS N=64 d=2 chi=256 x MPO D=16 -> raw product (bond 4096) -> TT-SVD round to chi=256 -> <X|Z>"
+
+
+def make_inputs():
+    """Seeded config-2 cores (numpy float64)."""
+    import numpy as np
+
+    rng = np.random.default_rng(SEED)
+    dims = [1] + [CHI] * (N_SITES - 1) + [1]
+    X = [rng.standard_normal((dims[k], D_PHYS, dims[k + 1])) / math.sqrt(max(dims[k], dims[k + 1]) * D_PHYS)
+         for k in range(N_SITES)]
+    wd = [1] + [D_MPO] * (N_SITES - 1) + [1]
+    W = [rng.standard_normal((wd[k], D_PHYS, D_PHYS, wd[k + 1])) / math.sqrt(max(wd[k], wd[k + 1]) * D_PHYS)
+         for k in range(N_SITES)]
+    return X, W
+
+
+# ---------------------------------------------------------------------------
+# clocks sampling
+# ---------------------------------------------------------------------------
+
+class ClockSampler:
+    FIELDS = ("clocks.sm,clocks.max.sm,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+              "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+              "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index=0):
+        self.index = index
+        self.proc = None
+        self.lines = []
+        self.thread = None
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.index), "--query-gpu=" + self.FIELDS, "--format=csv,noheader,nounits",
+                 "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except (OSError, FileNotFoundError):
+            self.proc = None
+            return
+        self.thread = threading.Thread(target=self._read, daemon=True)
+        self.thread.start()
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        if self.thread:
+            self.thread.join(timeout=2)
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 7:
+                continue
+            try:
+                sm.append(float(parts[0]))
+                smax.append(float(parts[1]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, parts[3:7]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no samples"], "samples": 0}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(smax), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+# ---------------------------------------------------------------------------
+# CPU port (the oracle) on a bounded sample
+# ---------------------------------------------------------------------------
+
+def site_flops_model():
+    """Per-site flops of the TT-SVD sweep at config 2 (left QR step and right
+    SVD step), by site shape; returns (list, index of a middle site)."""
+    b = [1]
+    R = [1] + [CHI * D_MPO] * (N_SITES - 1) + [1]
+    for k in range(N_SITES - 1):
+        b.append(min(b[k] * D_PHYS, R[k + 1]))
+    x = [1] * (N_SITES + 1)
+    for k in range(N_SITES - 1, 0, -1):
+        x[k] = min(CHI, b[k], D_PHYS * x[k + 1])
+    fl = []
+    for k in range(N_SITES):
+        m, n = b[k] * D_PHYS, R[k + 1]
+        q = min(m, n)
+        left = 2 * m * n * q - 2 * q ** 3 / 3 + 2 * q * R[k + 1] * D_PHYS * R[min(k + 2, N_SITES)] if k < N_SITES - 1 else 0
+        c = D_PHYS * x[k + 1]
+        mm = b[k]
+        right = 2 * mm * c * min(mm, c) + 10 * min(mm, c) ** 3 + 2 * (b[k - 1] * D_PHYS if k else 1) * mm * x[k] if k else 0
+        fl.append(left + right)
+    mid = N_SITES // 2
+    return fl, mid
+
+
+def cpu_site_sample(rng_seed=7):
+    """One full-size middle site of the numpy FP64 sweep: left QR step
+    (reduced QR of the 8192 x 4096 carried core + the carry GEMM into the next
+    product core) and right SVD step (QR of 4096 x 512, SVD of 512 x 512,
+    push of U*S through Q).  Returns seconds."""
+    import numpy as np
+
+    from oracle import tt_fp64 as O
+
+    rng = np.random.default_rng(rng_seed)
+    R = CHI * D_MPO
+    x = O.random_mps_cores(rng, 3, D_PHYS, CHI)
+    w = O.random_mpo_cores(rng, 3, D_PHYS, D_MPO)
+    P = O.mpo_mps_product(w[1:2], x[1:2])[0]  # (4096, 2, 4096)
+    Pn = O.mpo_mps_product(w[1:2], x[1:2])[0]
+    t0 = time.perf_counter()
+    C = P.reshape(R * D_PHYS, R)
+    Q, Rf = np.linalg.qr(C)
+    Cn = Rf @ Pn.reshape(R, -1)
+    M = Cn.reshape(R, -1)[:, : D_PHYS * CHI]
+    Qm, Rm = np.linalg.qr(M)
+    U, s, Vt = np.linalg.svd(Rm)
+    US = (Qm @ U[:, :CHI]) * s[:CHI]
+    pushed = Q @ US
+    t1 = time.perf_counter()
+    del pushed
+    return t1 - t0
+
+
+def cpu_baseline_measure():
+    fl, mid = site_flops_model()
+    t_site = cpu_site_sample()
+    t_sweep = t_site * sum(fl) / fl[mid]
+    return {"value": 1.0 / t_sweep, "unit": "sweeps/s", "cores": os.cpu_count(), "kind": "port",
+            "sample": "one full-size middle site of the numpy FP64 sweep (%.2f s), scaled to 64 sites by "
+                      "per-site flops (x%.1f)" % (t_site, sum(fl) / fl[mid]),
+            "seconds_per_sweep": t_sweep}
+
+
+def run_reference(args, rank, world):
+    if rank != 0:
+        return 0
+    import numpy as np  # noqa: F401
+
+    fl, mid = site_flops_model()
+    scale = sum(fl) / fl[mid]
+    for _ in range(args.warmup):
+        cpu_site_sample()
+    ts = [cpu_site_sample() for _ in range(args.steps)]
+    t_sweep = statistics.mean(ts) * scale
+    v = 1.0 / t_sweep
+    line = {
+        "impl": "reference", "metric": METRIC, "value": v, "unit": "sweeps/s", "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": t_sweep * 1e3, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded, config-2 shapes)",
+        "config": {"workload": WORKLOAD, "cpu": "numpy FP64 port of the sweep (Householder QR + LAPACK SVD)"},
+        "cpu_baseline": {"value": v, "unit": "sweeps/s", "cores": os.cpu_count(), "kind": "port",
+                         "sample": "each step = one full-size middle site, scaled to 64 sites by flops (x%.1f)" % scale},
+        "e2e": {"value": v, "unit": "sweeps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line))
+    return 0
+
+
+# ---------------------------------------------------------------------------
+# GPU arm
+# ---------------------------------------------------------------------------
+
+def run_gpu(args, rank, world, local_rank):
+    import ctypes
+
+    import numpy as np
+    import torch
+    import torch.distributed as dist
+
+    import __graft_entry__ as g
+
+    g.build()
+    from syngular_gb300 import _lib as L
+    from syngular_gb300.tensor import _ops
+
+    torch.cuda.set_device(local_rank)
+    dev = torch.device("cuda", local_rank)
+    prec = {"tf32x3": L.PREC_TF32X3, "tf32": L.PREC_TF32, "f64": L.PREC_F64}[args.precision]
+
+    Xh, Wh = make_inputs()
+    Xd = [torch.from_numpy(c).to(dev) for c in Xh]
+    Wd = [torch.from_numpy(c).to(dev) for c in Wh]
+    Xp = [torch.from_numpy(c).pin_memory() for c in Xh]
+    Wp = [torch.from_numpy(c).pin_memory() for c in Wh]
+    h2d = sum(c.numel() * 8 for c in Xh) + sum(c.numel() * 8 for c in Wh)
+
+    def step(X, W):
+        Z, spec, counts, disc, status = _ops.mpo_mps_round(W, X, CHI, prec)
+        res = _ops.overlap_device(X, Z)
+        return Z, res, status
+
+    def barrier():
+        if world > 1:
+            dist.barrier()
+
+    def max_over_ranks(v):
+        if world > 1:
+            t = torch.tensor([v], dtype=torch.float64, device=dev)
+            dist.all_reduce(t, op=dist.ReduceOp.MAX)
+            return float(t.item())
+        return v
+
+    # warm-up
+    for _ in range(max(args.warmup, 3)):
+        Z, res, status = step(Xd, Wd)
+    torch.cuda.synchronize()
+    st = int(status.item())
+    if st < 0:
+        raise RuntimeError("round did not converge (status %d)" % st)
+
+    # ---- timed region: device-resident inputs ----
+    clocks = ClockSampler(local_rank)
+    clocks.start()
+    time.sleep(0.3)
+    L.call("sgt_tc_profile", 1, None, None, None)
+    launches0 = L.load().sgt_launch_count()
+    barrier()
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    for _ in range(args.steps):
+        Z, res, status = step(Xd, Wd)
+    e1.record()
+    torch.cuda.synchronize()
+    barrier()
+    launches = L.load().sgt_launch_count() - launches0
+    tc_ms, tc_flops, tc_n = ctypes.c_double(), ctypes.c_double(), ctypes.c_longlong()
+    L.call("sgt_tc_profile", 0, ctypes.byref(tc_ms), ctypes.byref(tc_flops), ctypes.byref(tc_n))
+    clk = clocks.stop()
+    ms_total = max_over_ranks(e0.elapsed_time(e1))
+    ms_step = ms_total / args.steps
+    value = world * args.steps / (ms_total / 1e3)
+    ov_fast = _ops.decode_overlap(res.cpu().tolist())
+
+    # ---- e2e: host buffers in, scalar out ----
+    torch.cuda.synchronize()
+    barrier()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        Xe = [c.to(dev, non_blocking=True) for c in Xp]
+        We = [c.to(dev, non_blocking=True) for c in Wp]
+        Z, res, status = step(Xe, We)
+        _ = res.cpu().tolist()
+    torch.cuda.synchronize()
+    barrier()
+    e2e_s = max_over_ranks(time.perf_counter() - t0)
+    e2e_value = world * args.steps / e2e_s
+
+    out = {
+        "metric": METRIC, "value": value, "unit": "sweeps/s", "n_gpus": world, "steps": args.steps,
+        "warmup": max(args.warmup, 3), "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": {"tf32x3": "tf32x3/f32", "tf32": "tf32/f32", "f64": "f64"}[args.precision],
+        "data": "synthetic (seeded N(0,1)/sqrt(chi*d) cores)",
+        "config": {"workload": WORKLOAD, "form": args.precision, "l2": "inputs larger than L2 (product cores 34 GB)",
+                   "parallelism": "replicas" if world > 1 else "single GPU"},
+        "e2e": {"value": e2e_value, "unit": "sweeps/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": 16},
+        "gpu_launches": int(launches),
+        "clocks": clk,
+        "overlap": ov_fast,
+    }
+    # roofline of the dominant kernel (tcgen05 GEMM), from the live events
+    peaks = {}
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            peaks = json.load(f)
+    except OSError:
+        pass
+    peak = peaks.get("bf16_tflops") or 1900.0
+    passes = 3 if args.precision == "tf32x3" else 1
+    if tc_n.value > 0:
+        per_launch_s = tc_ms.value / 1e3 / tc_n.value
+        alg_flops = tc_flops.value / tc_n.value
+        achieved = alg_flops * passes / per_launch_s / 1e12
+        traffic = None
+        tpath = os.path.join(ROOT, "profiles", "tc_gemm_tf32_traffic.json")
+        if os.path.exists(tpath):
+            with open(tpath) as f:
+                traffic = json.load(f).get("bytes_per_launch_4096cubed")
+        out["roofline"] = {
+            "bound": "tensor", "kernel": "tc_gemm_tf32_kernel", "achieved": achieved, "peak": peak,
+            "unit": "TFLOP/s", "frac": achieved / peak, "traffic": traffic,
+            "note": "tensor-pipe TF32 flops (%d pass(es) x 2MNK) per launch / mean CUDA-event launch time over "
+                    "the timed region; peak = measured dense bf16 (TF32 issues at half that rate)" % passes,
+            "share_of_step": tc_ms.value / (ms_total * 1.0) if ms_total > 0 else None,
+            "launches": tc_n.value,
+        }
+    # plain FP64 GPU form (denominator) and the error of the fast form against it
+    if not args.no_plain and prec != L.PREC_F64:
+        torch.cuda.synchronize()
+        # warm the FP64 kernels on a short chain with the same core shapes
+        Xs = [Xd[0], Xd[1], Xd[-1]]
+        Ws = [Wd[0], Wd[1], Wd[-1]]
+        _ops.mpo_mps_round(Ws, Xs, CHI, L.PREC_F64)
+        torch.cuda.synchronize()
+        p0, p1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        p0.record()
+        Zp, spec_p, counts_p, disc_p, status_p = _ops.mpo_mps_round(Wd, Xd, CHI, L.PREC_F64)
+        resp = _ops.overlap_device(Xd, Zp)
+        p1.record()
+        torch.cuda.synchronize()
+        plain_ms = max_over_ranks(p0.elapsed_time(p1))
+        ov_plain = _ops.decode_overlap(resp.cpu().tolist())
+        nx = math.sqrt(_ops.overlap(Xd, Xd))
+        nz = math.sqrt(abs(_ops.overlap(Zp, Zp)))
+        out["plain_fp64"] = {"sweeps_per_s": world * 1e3 / plain_ms, "ms_per_sweep": plain_ms, "steps": 1,
+                             "warmup": 1, "status": int(status_p.item())}
+        out["speedup_vs_plain_fp64"] = value / (world * 1e3 / plain_ms)
+        out["error_vs_fp64"] = {"overlap_rel": abs(ov_fast - ov_plain) / abs(ov_plain),
+                                "overlap_norm": abs(ov_fast - ov_plain) / (nx * nz),
+                                "overlap_fp64": ov_plain}
+    if rank == 0 and not args.no_cpu:
+        out["cpu_baseline"] = cpu_baseline_measure()
+    if rank == 0:
+        print(json.dumps(out))
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="syngular", choices=["syngular", "reference"])
+    ap.add_argument("--precision", default="tf32x3", choices=["tf32x3", "tf32", "f64"])
+    ap.add_argument("--no-plain", action="store_true")
+    ap.add_argument("--no-cpu", action="store_true")
+    args = ap.parse_args()
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local_rank = int(os.environ.get("LOCAL_RANK", "0"))
+    if args.impl == "reference":
+        return run_reference(args, rank, world)
+    if world > 1:
+        import torch
+        import torch.distributed as dist
+
+        torch.cuda.set_device(local_rank)
+        dist.init_process_group("nccl")
+    try:
+        return run_gpu(args, rank, world, local_rank)
+    finally:
+        if world > 1:
+            import torch.distributed as dist
+
+            dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -233,6 +233,12 @@ SGT_API int sgt_tc_gemm_f32(int passes, int64_t M, int64_t N, int64_t K, float a
                             const float* B_hi, const float* B_lo, int64_t ldb, float beta,
                             float* C, int64_t ldc, int* err, void* stream);
 
+/* Event timing of tensor-core GEMM launches: enable = 1 starts recording a
+ * CUDA event pair around every sgt tcgen05 GEMM launch (on its stream);
+ * enable = 0 stops, waits for the recorded events and returns the summed
+ * kernel milliseconds, algorithmic flops (2 M N K per launch) and launches. */
+SGT_API int sgt_tc_profile(int enable, double* ms, double* flops, long long* launches);
+
 /* hi = TF32 rounding of x (round to nearest, ties away), lo = x - hi (lo may be NULL). */
 SGT_API int sgt_split_tf32(const float* x, float* hi, float* lo, int64_t n, void* stream);
 

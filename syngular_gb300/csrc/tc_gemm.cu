@@ -16,6 +16,8 @@
 #include <cuda.h>
 #include <cudaTypedefs.h>
 
+#include <vector>
+
 #include "common.cuh"
 
 namespace sgt {
@@ -320,6 +322,15 @@ size_t tc_smem_bytes(int passes) {
   return 1024 + (size_t)TC_STAGES * tps * TILE_BYTES + 8 * (2 * TC_STAGES + 1) + 16;
 }
 
+// Optional event timing of the tensor-core GEMM launches (benchmarks): each
+// launch is bracketed by CUDA events recorded on its own stream.
+struct ProfRec {
+  cudaEvent_t a, b;
+  double flops;
+};
+bool g_prof_on = false;
+std::vector<ProfRec> g_prof;
+
 }  // namespace
 
 int tc_gemm_tf32(cudaStream_t st, int passes, int64_t M, int64_t N, int64_t K, float alpha,
@@ -350,8 +361,19 @@ int tc_gemm_tf32(cudaStream_t st, int passes, int64_t M, int64_t N, int64_t K, f
   TcArgs args{C, ldc, (int)M, (int)N, (int)K, alpha, beta, passes, err};
   dim3 grid((unsigned)cdiv(N, TC_BN), (unsigned)cdiv(M, TC_BM));
   SGT_REQUIRE(grid.y <= 65535, SGT_ERR_INVALID, "tc_gemm: M too large");
+  ProfRec rec{};
+  if (g_prof_on) {
+    SGT_CUDA(cudaEventCreate(&rec.a));
+    SGT_CUDA(cudaEventCreate(&rec.b));
+    SGT_CUDA(cudaEventRecord(rec.a, st));
+  }
   tc_gemm_tf32_kernel<<<grid, TC_THREADS, smem, st>>>(ma, mal, mb, mbl, args);
   SGT_LAUNCHED();
+  if (g_prof_on) {
+    SGT_CUDA(cudaEventRecord(rec.b, st));
+    rec.flops = 2.0 * (double)M * (double)N * (double)K;
+    g_prof.push_back(rec);
+  }
   return SGT_OK;
 }
 
@@ -380,6 +402,32 @@ extern "C" SGT_API int sgt_tc_gemm_f32(int passes, int64_t M, int64_t N, int64_t
                                        float* C, int64_t ldc, int* err, void* stream) {
   return sgt::tc_gemm_tf32(sgt::as_stream(stream), passes, M, N, K, alpha, A_hi, A_lo, lda, B_hi, B_lo,
                            ldb, beta, C, ldc, err);
+}
+
+extern "C" SGT_API int sgt_tc_profile(int enable, double* ms, double* flops, long long* launches) {
+  // enable = 1: start recording; 0: stop, synchronise on the recorded events,
+  // return the summed kernel time, algorithmic flops and launch count.
+  using namespace sgt;
+  if (enable) {
+    g_prof_on = true;
+    return SGT_OK;
+  }
+  g_prof_on = false;
+  double tot = 0.0, fl = 0.0;
+  for (auto& r : g_prof) {
+    SGT_CUDA(cudaEventSynchronize(r.b));
+    float t = 0.f;
+    SGT_CUDA(cudaEventElapsedTime(&t, r.a, r.b));
+    tot += t;
+    fl += r.flops;
+    cudaEventDestroy(r.a);
+    cudaEventDestroy(r.b);
+  }
+  if (ms) *ms = tot;
+  if (flops) *flops = fl;
+  if (launches) *launches = (long long)g_prof.size();
+  g_prof.clear();
+  return SGT_OK;
 }
 
 extern "C" SGT_API int sgt_split_tf32(const float* x, float* hi, float* lo, int64_t n, void* stream) {
