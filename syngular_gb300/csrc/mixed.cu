@@ -15,7 +15,8 @@
 // QR-then-SVD sweep decomposes, so the kept singular vectors / values are the
 // same.  GEMMs: tcgen05 kind::tf32 (one pass, or three passes on split
 // hi/lo operands); product cores and Gram matrices are held in FP32; the
-// eigen-solves are one-sided Jacobi on Z_k with FP32 columns and FP64 angles.
+// eigen-solves are one-sided Jacobi on Z_k with FP32 columns and FP64 angles,
+// after which the kept eigenvectors are re-orthonormalised in FP64.
 #include <float.h>
 
 #include <algorithm>
@@ -36,6 +37,8 @@ int tc_gemm_tf32(cudaStream_t st, int passes, int64_t M, int64_t N, int64_t K, f
                  const float* Ahi, const float* Alo, int64_t lda, const float* Bhi, const float* Blo,
                  int64_t ldb, float beta, float* C, int64_t ldc, int* err);
 int split_tf32(cudaStream_t st, const float* x, float* hi, float* lo, int64_t n);
+int split_f64(cudaStream_t st, const double* x, int64_t ldx, float* hi, float* lo, int64_t rows,
+              int64_t cols);
 size_t jacobi_rows_ws_bytes_f32(int64_t n, int64_t m);
 int jacobi_rows_f32(cudaStream_t st, float* G, int64_t ldg, int64_t n, int64_t m, float* Vt,
                     int64_t ldv, float* s, int* status, Arena& ar);
@@ -281,6 +284,8 @@ static int mixed_round_impl(cudaStream_t st, int n, const double* const* W, cons
   float* Vh = ar.take<float>(cmax * cmax);
   float* Vl = ar.take<float>(cmax * cmax);
   float* lam = ar.take<float>(cmax);
+  double* Vd = ar.take<double>(chi * cmax);
+  double* Sd = ar.take<double>(chi * chi);
   int* stat = ar.take<int>(n + 1);
   int* tc_err = ar.take<int>(1);
   char* jscratch = ar.take<char>(jacobi_rows_ws_bytes_f32(cmax, cmax));
@@ -344,9 +349,13 @@ static int mixed_round_impl(cudaStream_t st, int n, const double* const* W, cons
     SGT_TRY(gemm_nt(st, passes, c, c, r, 1.f, Yth, Ytl, r, GYh, GYl, r, 0.f, Z, c, tc_err));
     Arena ja(jscratch, jbytes);
     SGT_TRY(jacobi_rows_f32(st, Z, c, c, c, Vt, c, lam, stat + k, ja));
-    // core_k = Vt[:keep]
-    f32_to_f64_kernel<<<gs(keep * c), 256, 0, st>>>(Vt, c, out[k], c, keep, c);
+    // core_k = Vt[:keep], re-orthonormalised in FP64 by one Newton-Schulz step
+    // V <- 1.5 V - 0.5 (V V^T) V (the FP32 rotations leave |V V^T - I| ~ 1e-6)
+    f32_to_f64_kernel<<<gs(keep * c), 256, 0, st>>>(Vt, c, Vd, c, keep, c);
     SGT_LAUNCHED();
+    SGT_TRY(gemm_f64(st, false, true, keep, keep, c, 1.0, Vd, c, 0, Vd, c, 0, 0.0, Sd, keep, 0, 1));
+    SGT_TRY(copy2d_f64(st, out[k], c, Vd, c, keep, c));
+    SGT_TRY(gemm_f64(st, false, false, keep, c, keep, -0.5, Sd, keep, 0, Vd, c, 0, 1.5, out[k], c, 0, 1));
     double* spec_k = nullptr;
     if (spectra) {
       int64_t off = 0;
@@ -359,7 +368,7 @@ static int mixed_round_impl(cudaStream_t st, int n, const double* const* W, cons
     // Ft_k (keep x r) = Vt[:keep] Y^T with Y = Yt^T (r x c)
     SGT_TRY(transpose_f32(st, Y, c, 0, Yt, r, 0, c, r, 1));
     SGT_TRY(split_tf32(st, Y, Yh, Yl, r * c));
-    SGT_TRY(split_tf32(st, Vt, Vh, Vl, keep * c));
+    SGT_TRY(split_f64(st, out[k], c, Vh, Vl, keep, c));
     SGT_TRY(gemm_nt(st, passes, keep, r, c, 1.f, Vh, Vl, c, Yh, Yl, c, 0.f, Ftn, r, tc_err));
     SGT_TRY(split_tf32(st, Ftn, Fth, Ftl, keep * r));
   }
