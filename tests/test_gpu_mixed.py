@@ -50,7 +50,7 @@ def test_mpo_mps_round(n, d, chi, D, cut, prec, tol_norm, tol_spec):
     nx, nz = np.sqrt(O.overlap(X, X)), np.sqrt(O.overlap(Zr, Zr))
     assert abs(ov - ovr) / (nx * nz) < tol_norm
     zz = _ops.overlap(Z, Z)
-    assert abs(zz - nz * nz) / (nz * nz) < max(tol_norm, 1e-12) * 10
+    assert abs(zz - nz * nz) / (nz * nz) < max(tol_norm * 100, 1e-12)
     s = spec.cpu().numpy()
     off = 0
     for k in range(n - 1):
