@@ -234,7 +234,7 @@ def run_gpu(args, rank, world, local_rank):
     Wd = [torch.from_numpy(c).to(dev) for c in Wh]
     Xp = [torch.from_numpy(c).pin_memory() for c in Xh]
     Wp = [torch.from_numpy(c).pin_memory() for c in Wh]
-    h2d = sum(c.numel() * 8 for c in Xh) + sum(c.numel() * 8 for c in Wh)
+    h2d = sum(c.size * 8 for c in Xh) + sum(c.size * 8 for c in Wh)
 
     def step(X, W):
         Z, spec, counts, disc, status = _ops.mpo_mps_round(W, X, CHI, prec)

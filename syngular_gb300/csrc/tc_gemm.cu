@@ -8,9 +8,12 @@
 // B = B_hi + B_lo with hi the TF32-rounded value, accumulating
 // A_hi*B_hi + A_hi*B_lo + A_lo*B_hi in FP32 (about 22 significant bits).
 //
-// One CTA computes a 128 x 128 tile with 4 warps: lane 0 of warp 0 issues the
-// TMA loads into a 3-stage ring, lane 0 of warp 1 issues the MMAs, then all
-// four warps drain TMEM (warp w owns TMEM lanes 32w..32w+31 = tile rows).
+// One CTA computes a 128 x 128 tile with 6 warps: lane 0 of warp 0 issues the
+// TMA loads into a 3-stage ring, lane 0 of warp 1 issues the MMAs, warps 2..5
+// drain the accumulator after every 32-wide K chunk (double-buffered in TMEM)
+// and add it into FP32 registers, so the tensor-core accumulation never spans
+// more than one chunk (its long-K accumulation truncates).  Warp w may only
+// touch TMEM lanes 32*(w%4)..+31, which are tile rows.
 // Every mbarrier wait has an iteration limit; on expiry the kernel records an
 // error code, skips the remaining work, still frees its TMEM and returns.
 #include <cuda.h>
@@ -28,7 +31,9 @@ constexpr int TC_BM = 128;
 constexpr int TC_BN = 128;
 constexpr int TC_BK = 32;  // fp32 elements per stage along K = 128 bytes = one swizzle row
 constexpr int TC_STAGES = 3;
-constexpr int TC_THREADS = 128;
+constexpr int TC_EPI_WARPS = 4;
+constexpr int TC_THREADS = 64 + 32 * TC_EPI_WARPS;  // producer warp, MMA warp, 4 accumulator warps
+constexpr int TC_TMEM_COLS = 2 * 128;               // two accumulator buffers of TC_BN columns
 constexpr int TILE_BYTES = TC_BM * TC_BK * 4;  // 16 KB (A and B tiles have the same size)
 constexpr uint32_t WAIT_LIMIT = 1u << 24;
 
@@ -131,12 +136,20 @@ struct TcArgs {
   int* err;
 };
 
+__device__ __forceinline__ void mbar_arrive(uint64_t* bar) {
+  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(bar)) : "memory");
+}
+
+// Warp roles: warp 0 lane 0 issues TMA loads into a TC_STAGES ring; warp 1
+// owns TMEM (2 x 128 columns) and lane 0 issues the MMAs; warps 2..5 drain
+// each 32-wide K chunk of the accumulator from TMEM into FP32 registers
+// (round-to-nearest adds), so the tensor core never accumulates more than one
+// chunk.  Two TMEM buffers let the MMA of chunk c+1 overlap the drain of c.
 __global__ void __launch_bounds__(TC_THREADS, 1)
     tc_gemm_tf32_kernel(const __grid_constant__ CUtensorMap mA, const __grid_constant__ CUtensorMap mAl,
                         const __grid_constant__ CUtensorMap mB, const __grid_constant__ CUtensorMap mBl,
                         const TcArgs args) {
   extern __shared__ __align__(1024) unsigned char smem_raw[];
-  // 1024-byte alignment for the swizzled tiles
   unsigned char* smem = reinterpret_cast<unsigned char*>(
       (reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
   const int npass = args.passes;
@@ -144,8 +157,9 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
   unsigned char* ring = smem;
   uint64_t* full = reinterpret_cast<uint64_t*>(ring + (size_t)TC_STAGES * tiles_per_stage * TILE_BYTES);
   uint64_t* empty = full + TC_STAGES;
-  uint64_t* done = empty + TC_STAGES;
-  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(done + 1);
+  uint64_t* accf = empty + TC_STAGES;  // accumulator buffer b holds a finished chunk
+  uint64_t* acce = accf + 2;           // accumulator buffer b has been drained
+  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(acce + 2);
   __shared__ int s_fail;
 
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -158,13 +172,16 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
       mbar_init(&full[s], 1);
       mbar_init(&empty[s], 1);
     }
-    mbar_init(done, 1);
+    for (int b = 0; b < 2; ++b) {
+      mbar_init(&accf[b], 1);
+      mbar_init(&acce[b], TC_EPI_WARPS);
+    }
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
   if (warp == 1) {
     asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(
                      smem_u32(tmem_slot)),
-                 "r"(TC_BN));
+                 "r"(TC_TMEM_COLS));
     asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
   }
   asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
@@ -176,78 +193,100 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
     return ring + ((size_t)stage * tiles_per_stage + which) * TILE_BYTES;
   };
 
-  if (warp == 0 && lane == 0) {
-    // ---- TMA producer ----
-    const uint32_t bytes = (uint32_t)tiles_per_stage * TILE_BYTES;
-    for (int kt = 0; kt < KT; ++kt) {
-      const int s = kt % TC_STAGES;
-      const uint32_t ph = (uint32_t)(kt / TC_STAGES) & 1u;
-      if (kt >= TC_STAGES && !mbar_wait(&empty[s], ph ^ 1u)) {
-        atomicExch(&s_fail, 1);
-        break;
-      }
-      if (atomicAdd(&s_fail, 0)) break;
-      mbar_expect_tx(&full[s], bytes);
-      const int kx = kt * TC_BK;
-      tma_load_2d(tile(s, 0), &mA, &full[s], kx, m0);
-      tma_load_2d(tile(s, 1), &mB, &full[s], kx, n0);
-      if (npass == 3) {
-        tma_load_2d(tile(s, 2), &mAl, &full[s], kx, m0);
-        tma_load_2d(tile(s, 3), &mBl, &full[s], kx, n0);
+  if (warp == 0) {
+    if (lane == 0) {
+      // ---- TMA producer ----
+      const uint32_t bytes = (uint32_t)tiles_per_stage * TILE_BYTES;
+      for (int kt = 0; kt < KT; ++kt) {
+        const int s = kt % TC_STAGES;
+        const uint32_t ph = (uint32_t)(kt / TC_STAGES) & 1u;
+        if (kt >= TC_STAGES && !mbar_wait(&empty[s], ph ^ 1u)) {
+          atomicExch(&s_fail, 1);
+          break;
+        }
+        if (*(volatile int*)&s_fail) break;
+        mbar_expect_tx(&full[s], bytes);
+        const int kx = kt * TC_BK;
+        tma_load_2d(tile(s, 0), &mA, &full[s], kx, m0);
+        tma_load_2d(tile(s, 1), &mB, &full[s], kx, n0);
+        if (npass == 3) {
+          tma_load_2d(tile(s, 2), &mAl, &full[s], kx, m0);
+          tma_load_2d(tile(s, 3), &mBl, &full[s], kx, n0);
+        }
       }
     }
-  } else if (warp == 1 && lane == 0) {
-    // ---- MMA issuer ----
-    constexpr uint32_t idesc = idesc_tf32(TC_BM, TC_BN);
+    __syncwarp();
+  } else if (warp == 1) {
+    if (lane == 0) {
+      // ---- MMA issuer: one K-tile per accumulator chunk ----
+      constexpr uint32_t idesc = idesc_tf32(TC_BM, TC_BN);
+      for (int kt = 0; kt < KT; ++kt) {
+        const int s = kt % TC_STAGES;
+        const uint32_t ph = (uint32_t)(kt / TC_STAGES) & 1u;
+        const int b = kt & 1, use = kt >> 1;
+        if (use >= 1 && !mbar_wait(&acce[b], (uint32_t)(use - 1) & 1u)) {
+          atomicExch(&s_fail, 1);
+          break;
+        }
+        if (!mbar_wait(&full[s], ph)) {
+          atomicExch(&s_fail, 1);
+          break;
+        }
+        asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+        const uint32_t d = tmem + (uint32_t)(b * TC_BN);
+        const uint32_t a = smem_u32(tile(s, 0)), bb = smem_u32(tile(s, 1));
+        const uint32_t al = smem_u32(tile(s, 2)), bl = smem_u32(tile(s, 3));
+#pragma unroll
+        for (int kk = 0; kk < TC_BK / 8; ++kk) {  // tf32 MMA consumes K = 8 (32 bytes)
+          const uint32_t off = kk * 32;
+          if (npass == 3) {  // small cross terms first, then hi*hi
+            mma_tf32(d, smem_desc(a + off), smem_desc(bl + off), idesc, kk > 0 ? 1u : 0u);
+            mma_tf32(d, smem_desc(al + off), smem_desc(bb + off), idesc, 1u);
+            mma_tf32(d, smem_desc(a + off), smem_desc(bb + off), idesc, 1u);
+          } else {
+            mma_tf32(d, smem_desc(a + off), smem_desc(bb + off), idesc, kk > 0 ? 1u : 0u);
+          }
+        }
+        mma_commit(&empty[s]);
+        mma_commit(&accf[b]);
+      }
+    }
+    __syncwarp();
+  } else {
+    // ---- accumulator warps: drain every chunk into registers ----
+    const int q = warp & 3;  // TMEM lane quarter this warp may access
+    float acc[TC_BN];
+#pragma unroll
+    for (int i = 0; i < TC_BN; ++i) acc[i] = 0.f;
     bool ok = true;
-    for (int kt = 0; kt < KT; ++kt) {
-      const int s = kt % TC_STAGES;
-      const uint32_t ph = (uint32_t)(kt / TC_STAGES) & 1u;
-      if (!mbar_wait(&full[s], ph)) {
+    for (int kt = 0; kt < KT && ok; ++kt) {
+      const int b = kt & 1, use = kt >> 1;
+      if (!mbar_wait(&accf[b], (uint32_t)use & 1u)) {
         atomicExch(&s_fail, 1);
         ok = false;
         break;
       }
       asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-      const uint32_t a = smem_u32(tile(s, 0)), b = smem_u32(tile(s, 1));
-      const uint32_t al = smem_u32(tile(s, 2)), bl = smem_u32(tile(s, 3));
 #pragma unroll
-      for (int kk = 0; kk < TC_BK / 8; ++kk) {  // tf32 MMA consumes K = 8 (32 bytes)
-        const uint32_t off = kk * 32;
-        mma_tf32(tmem, smem_desc(a + off), smem_desc(b + off), idesc, (kt > 0 || kk > 0) ? 1u : 0u);
-        if (npass == 3) {
-          mma_tf32(tmem, smem_desc(a + off), smem_desc(bl + off), idesc, 1u);
-          mma_tf32(tmem, smem_desc(al + off), smem_desc(b + off), idesc, 1u);
-        }
+      for (int c0 = 0; c0 < TC_BN; c0 += 32) {
+        float v[32];
+        tmem_ld32(tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)(b * TC_BN + c0), v);
+#pragma unroll
+        for (int i = 0; i < 32; ++i) acc[c0 + i] += v[i];
       }
-      mma_commit(&empty[s]);
+      asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+      __syncwarp();
+      if (lane == 0) mbar_arrive(&acce[b]);
     }
-    if (ok) mma_commit(done);
-  }
-  __syncwarp();
-
-  // ---- epilogue: all four warps ----
-  bool have = (KT > 0) ? mbar_wait(done, 0) : false;
-  if (KT > 0 && !have) atomicExch(&s_fail, 1);
-  __syncthreads();
-  have = have && !s_fail;
-  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-  const int row = m0 + warp * 32 + lane;
-  for (int c0 = 0; c0 < TC_BN; c0 += 32) {
-    float v[32];
-    if (have) {
-      tmem_ld32(tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)c0, v);
-    } else {
+    ok = ok && !*(volatile int*)&s_fail;
+    const int row = m0 + q * 32 + lane;
+    if (ok && row < args.M) {
+      float* crow = args.C + (int64_t)row * args.ldc + n0;
 #pragma unroll
-      for (int i = 0; i < 32; ++i) v[i] = 0.f;
-    }
-    if (row < args.M && (have || KT == 0)) {
-      float* crow = args.C + (int64_t)row * args.ldc + n0 + c0;
-#pragma unroll
-      for (int i = 0; i < 32; ++i) {
-        if (n0 + c0 + i < args.N) {
-          const float acc = args.alpha * v[i];
-          crow[i] = (args.beta == 0.f) ? acc : fmaf(args.beta, crow[i], acc);
+      for (int i = 0; i < TC_BN; ++i) {
+        if (n0 + i < args.N) {
+          const float r = args.alpha * acc[i];
+          crow[i] = (args.beta == 0.f) ? r : fmaf(args.beta, crow[i], r);
         }
       }
     }
@@ -255,7 +294,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
   asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
   __syncthreads();
   if (warp == 1) {
-    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(TC_BN));
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(TC_TMEM_COLS));
   }
   if (threadIdx.x == 0 && s_fail && args.err) atomicExch(args.err, 1);
 }
@@ -319,7 +358,7 @@ int make_map(CUtensorMap* map, const float* ptr, int64_t rows, int64_t K, int64_
 
 size_t tc_smem_bytes(int passes) {
   const int tps = (passes == 3) ? 4 : 2;
-  return 1024 + (size_t)TC_STAGES * tps * TILE_BYTES + 8 * (2 * TC_STAGES + 1) + 16;
+  return 1024 + (size_t)TC_STAGES * tps * TILE_BYTES + 8 * (2 * TC_STAGES + 4) + 16;
 }
 
 // Optional event timing of the tensor-core GEMM launches (benchmarks): each

@@ -1,7 +1,8 @@
 """tcgen05 TF32 / 3xTF32 GEMM against an FP64 reference of the same product.
-Tolerances: TF32 (10-bit mantissa) 5e-3 relative Frobenius error; 3xTF32 3e-5
-(the split products are exact to ~2^-22, the FP32 tensor-core accumulation
-adds about sqrt(K) * 2^-23)."""
+Tolerances: TF32 (10-bit mantissa) 5e-3 relative Frobenius error; 3xTF32 1e-6
+(split products exact to ~2^-22; the kernel drains the tensor-core accumulator
+every 32 of K into round-to-nearest FP32 registers, so long K does not
+accumulate the tensor core's truncation)."""
 import numpy as np
 import pytest
 import torch
@@ -51,6 +52,6 @@ def test_tf32(M, N, K, pad):
     assert run(M, N, K, 1, pad) < 5e-3
 
 
-@pytest.mark.parametrize("M,N,K", [(128, 128, 32), (300, 260, 1000), (2048, 1024, 2048)])
+@pytest.mark.parametrize("M,N,K", [(128, 128, 32), (300, 260, 1000), (2048, 1024, 2048), (512, 512, 8192)])
 def test_3xtf32(M, N, K):
-    assert run(M, N, K, 3, beta=0.5) < 3e-5
+    assert run(M, N, K, 3, beta=0.5) < 1e-6
