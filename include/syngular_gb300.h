@@ -106,6 +106,22 @@ SGT_API int sgt_overlap_sweep(int n, const double* const* X, const int64_t* xsha
                       const double* const* Y, const int64_t* yshape,
                       double* result, void* ws, size_t ws_bytes, void* stream);
 
+/* Overlap <X|Y> that allocates nothing and takes no workspace.  It has no
+ * counterpart in the reference.  It serves callers that cannot give the
+ * library scratch memory -- e.g. a C/ctypes binding whose process leaves all
+ * device memory to another framework's pool, or a loop that must not
+ * allocate.  Its scratch is a fixed ~9.4 MB device array inside the library
+ * (held on every GPU that loads it until exit), so every bond must be <= 256
+ * and every physical leg <= 16; larger chains are rejected with
+ * SGT_ERR_INVALID (use sgt_overlap_sweep).  The first call on a device looks
+ * up that array's device address (make it before any stream capture).  All
+ * calls share the array: calls that overlap on the GPU (other streams or host
+ * threads) race and must be serialised by the caller.  Result as for
+ * sgt_overlap_sweep. */
+SGT_API int sgt_overlap_sweep_noalloc(int n, const double* const* X, const int64_t* xshape,
+                                      const double* const* Y, const int64_t* yshape,
+                                      double* result, void* stream);
+
 /* ----------------------------------------------------------------------
  * Reference rounding `>> dim` = compress(dim, strict=True), left mode
  * (mps:432-468, mpo:544-580): for k = 0..n-2, complete Householder QR of the

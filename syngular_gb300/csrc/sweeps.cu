@@ -655,6 +655,18 @@ static int svd_round_impl(cudaStream_t st, int n, const double* const* cores, co
   return SGT_OK;
 }
 
+size_t overlap_ws_size(int n, const int64_t* xs, const int64_t* ys) {
+  Arena a = Arena::measuring();
+  if (overlap_impl(nullptr, n, nullptr, xs, nullptr, ys, nullptr, a) != SGT_OK) return 0;
+  return a.used;
+}
+
+int overlap_ws_run(cudaStream_t st, int n, const double* const* X, const int64_t* xs,
+                   const double* const* Y, const int64_t* ys, double* result, void* ws, size_t ws_bytes) {
+  Arena a(ws, ws_bytes);
+  return overlap_impl(st, n, X, xs, Y, ys, result, a);
+}
+
 size_t svd_round_ws(int n, const int64_t* shape, int64_t chi) {
   Arena a = Arena::measuring();
   if (svd_round_impl(nullptr, n, nullptr, shape, chi, SGT_PREC_F64, nullptr, nullptr, nullptr, nullptr, a) !=
