@@ -87,7 +87,7 @@ def test_householder_qr(m, n, keep):
     np.testing.assert_allclose(Qh.T @ Qh, np.eye(keep), atol=1e-13)
 
 
-@pytest.mark.parametrize("m,n", [(24, 24), (100, 60), (300, 300), (520, 513)])
+@pytest.mark.parametrize("m,n", [(24, 24), (100, 60), (300, 300), (520, 513), (512, 512), (2000, 128)])
 def test_jacobi_svd(m, n):
     from syngular_gb300 import _lib as L
 
