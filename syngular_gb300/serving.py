@@ -1,0 +1,207 @@
+"""Continuous-batching request loop for contract / round / overlap jobs.
+
+Jobs arrive on a queue; a scheduler thread admits them while the device
+memory they need (workspace + outputs, from the library's size queries) fits
+an HBM budget and a stream slot is free, launches them on their own CUDA
+stream, and retires them as their completion events fire -- so requests that
+arrive while others run join as soon as memory and slots free up, and their
+kernels overlap on the device.  Session cores stay resident on the device
+between jobs (a job references them by session id).  A job whose own
+footprint exceeds the whole budget is rejected at submission.
+
+Job kinds (the three of the serving workload):
+  * "round"   : raw W @ X followed by TT-SVD rounding to chi (sgt_mpo_mps_round)
+  * "add_round": X + Y (bond concatenation) followed by TT-SVD rounding to chi
+  * "overlap" : <X|Y>
+Every job's result is the same whether it runs alone or in the mix: each job
+has its own workspace and stream, and the kernels read only its own data.
+"""
+from __future__ import annotations
+
+import queue
+import threading
+import time
+from dataclasses import dataclass, field
+from typing import Dict, List, Optional
+
+import torch
+
+from . import _lib as L
+from .tensor import _ops
+
+
+@dataclass
+class Job:
+    kind: str
+    session: str
+    chi: int = 0
+    precision: int = L.PREC_TF32X3
+    other: Optional[str] = None          # second operand's session (add_round / overlap)
+    arrival: float = 0.0                 # seconds (time.perf_counter clock)
+    job_id: int = 0
+    # filled in by the server
+    start: float = 0.0
+    end: float = 0.0
+    result: object = None
+    error: Optional[str] = None
+    done: threading.Event = field(default_factory=threading.Event)
+
+    @property
+    def latency(self) -> float:
+        return self.end - self.arrival
+
+
+class RoundServer:
+    """Admission by HBM budget, one CUDA stream per in-flight job."""
+
+    def __init__(self, budget_bytes: int = 120 << 30, slots: int = 8):
+        self.budget = int(budget_bytes)
+        self.slots = int(slots)
+        self.sessions: Dict[str, dict] = {}
+        self.inbox: "queue.Queue[Job]" = queue.Queue()
+        self.streams = [torch.cuda.Stream() for _ in range(self.slots)]
+        self.free_streams = list(range(self.slots))
+        self.used = 0
+        self.inflight: List[tuple] = []
+        self.pending: List[Job] = []
+        self.completed: List[Job] = []
+        self.rejected: List[Job] = []
+        self._stop = threading.Event()
+        self._thread = threading.Thread(target=self._loop, daemon=True)
+
+    # ---------------------------------------------------------------- sessions
+    def add_session(self, name: str, mps=None, mpo=None):
+        """Keep cores resident on the device: mps = list of (l, p, r), mpo =
+        list of (l, in, out, r) float64 tensors (host or device)."""
+        self.sessions[name] = {
+            "mps": [L.as_device(c) for c in mps] if mps is not None else None,
+            "mpo": [L.as_device(c) for c in mpo] if mpo is not None else None,
+        }
+
+    # ----------------------------------------------------------------- control
+    def start(self):
+        self._thread.start()
+        return self
+
+    def stop(self):
+        self._stop.set()
+        self._thread.join()
+
+    def submit(self, job: Job) -> Job:
+        if not job.arrival:
+            job.arrival = time.perf_counter()
+        self.inbox.put(job)
+        return job
+
+    # ------------------------------------------------------------- accounting
+    def footprint(self, job: Job) -> int:
+        s = self.sessions[job.session]
+        if job.kind == "round":
+            W, X = s["mpo"], s["mps"]
+            n = len(X)
+            wsh, _a = L.i64_array([int(v) for w in W for v in w.shape])
+            xsh, _b = L.shape_array([tuple(x.shape) for x in X])
+            ws = L.query("sgt_mpo_mps_round_workspace_size", n, wsh, xsh, job.chi, job.precision)
+            out = sum(x.shape[1] * job.chi * job.chi * 8 for x in X)
+            return ws + out if ws else -1
+        if job.kind == "add_round":
+            X, Y = s["mps"], self.sessions[job.other]["mps"]
+            cat = sum(8 * (x.shape[0] + y.shape[0]) * x.shape[1] * (x.shape[2] + y.shape[2]) for x, y in zip(X, Y))
+            shp = [(x.shape[0] + (y.shape[0] if k else 0), x.shape[1],
+                    x.shape[2] + (y.shape[2] if k < len(X) - 1 else 0)) for k, (x, y) in enumerate(zip(X, Y))]
+            shp[0] = (1, shp[0][1], shp[0][2])
+            sh, _c = L.shape_array(shp)
+            ws = L.query("sgt_svd_round_workspace_size", len(X), sh, job.chi, L.PREC_F64)
+            return cat + ws if ws else -1
+        X, Y = s["mps"], self.sessions[job.other]["mps"]
+        xs, _d = L.shape_array([tuple(x.shape) for x in X])
+        ys, _e = L.shape_array([tuple(y.shape) for y in Y])
+        return L.query("sgt_overlap_workspace_size", len(X), xs, ys) + 16
+
+    # -------------------------------------------------------------- execution
+    def _launch(self, job: Job, stream_idx: int):
+        s = self.sessions[job.session]
+        st = self.streams[stream_idx]
+        st.wait_stream(torch.cuda.current_stream())
+        with torch.cuda.stream(st):
+            if job.kind == "round":
+                res = _ops.mpo_mps_round(s["mpo"], s["mps"], job.chi, job.precision)
+                out = (res[0], res[1], res[2], res[3], res[4])
+            elif job.kind == "add_round":
+                S = _ops.concat(s["mps"], self.sessions[job.other]["mps"])
+                out = _ops.svd_round(S, job.chi)
+            else:
+                out = _ops.overlap_device(s["mps"], self.sessions[job.other]["mps"])
+            ev = torch.cuda.Event()
+            ev.record(st)
+        return out, ev
+
+    def _loop(self):
+        while not self._stop.is_set() or self.pending or self.inflight or not self.inbox.empty():
+            # take arrivals
+            try:
+                while True:
+                    j = self.inbox.get_nowait()
+                    need = self.footprint(j)
+                    if need < 0 or need > self.budget:
+                        j.error = "rejected: footprint %d bytes exceeds the HBM budget" % need
+                        j.end = time.perf_counter()
+                        self.rejected.append(j)
+                        j.done.set()
+                        continue
+                    j._need = need
+                    self.pending.append(j)
+            except queue.Empty:
+                pass
+            # retire finished jobs
+            still = []
+            for job, ev, out, sidx in self.inflight:
+                if ev.query():
+                    job.end = time.perf_counter()
+                    job.result = out
+                    self.used -= job._need
+                    self.free_streams.append(sidx)
+                    self.completed.append(job)
+                    job.done.set()
+                else:
+                    still.append((job, ev, out, sidx))
+            self.inflight = still
+            # admit in arrival order while memory and slots allow
+            admitted = []
+            for j in self.pending:
+                if not self.free_streams:
+                    break
+                if self.used + j._need > self.budget:
+                    break
+                sidx = self.free_streams.pop()
+                self.used += j._need
+                j.start = time.perf_counter()
+                try:
+                    out, ev = self._launch(j, sidx)
+                    self.inflight.append((j, ev, out, sidx))
+                except Exception as e:  # surface the error on the job, keep serving
+                    j.error = str(e)
+                    j.end = time.perf_counter()
+                    self.used -= j._need
+                    self.free_streams.append(sidx)
+                    self.rejected.append(j)
+                    j.done.set()
+                admitted.append(j)
+            if admitted:
+                self.pending = [j for j in self.pending if j not in admitted]
+            if not admitted and not self.inflight:
+                time.sleep(0.0002)
+            else:
+                time.sleep(0)
+
+
+def latency_stats(jobs: List[Job]):
+    lat = sorted(j.latency for j in jobs)
+    if not lat:
+        return {"p50_ms": None, "p99_ms": None, "count": 0}
+
+    def pct(p):
+        k = min(len(lat) - 1, max(0, int(round(p / 100.0 * (len(lat) - 1)))))
+        return lat[k] * 1e3
+
+    return {"p50_ms": pct(50), "p99_ms": pct(99), "count": len(lat), "mean_ms": 1e3 * sum(lat) / len(lat)}
