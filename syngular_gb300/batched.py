@@ -1,0 +1,203 @@
+"""Many independent MPO x MPS + TT-SVD round + overlap problems of uneven size.
+
+Instances (their own N, d, chi, D) are dealt to S CUDA streams, longest first;
+each stream runs its instances one after another inside one reusable
+workspace, so device memory is S x (largest workspace of a stream) plus the
+outputs.  Everything is enqueued through the C ABI with preallocated buffers
+(no allocation, no host synchronisation), so the whole batch can be captured
+once into a CUDA graph and replayed.
+
+The autotuner times the candidate stream counts (by graph replay) for a shape
+class (bucketed largest fused bond, mean length, count) and caches the choice
+in a JSON file.
+"""
+from __future__ import annotations
+
+import ctypes
+import json
+import math
+import os
+from typing import Dict, List, Optional, Sequence
+
+import torch
+
+from . import _lib as L
+
+TUNE_FILE = os.path.join(os.path.dirname(os.path.abspath(__file__)), "tuning.json")
+
+
+class Instance:
+    def __init__(self, W: Sequence[torch.Tensor], X: Sequence[torch.Tensor], chi: int):
+        self.W = [L.as_device(w) for w in W]
+        self.X = [L.as_device(x) for x in X]
+        self.chi = int(chi)
+        self.n = len(self.X)
+        self.wsh = [int(v) for w in self.W for v in w.shape]
+        self.xsh = [int(v) for x in self.X for v in x.shape]
+        self.pshapes = [(x.shape[0] * w.shape[0], w.shape[2], x.shape[2] * w.shape[3])
+                        for w, x in zip(self.W, self.X)]
+        self.rmax = max(max(p[0], p[2]) for p in self.pshapes)
+
+
+class BatchedRound:
+    def __init__(self, instances: List[Instance], precision: int = L.PREC_TF32X3, streams: int = 4,
+                 budget_bytes: int = 160 << 30):
+        self.instances = instances
+        self.precision = precision
+        dev = L.device()
+        # output shapes, spectra counts, workspace sizes
+        self.ws_need = []
+        for inst in instances:
+            n = inst.n
+            psh, _p = L.shape_array(inst.pshapes)
+            out = (ctypes.c_int64 * (3 * n))()
+            cnt = (ctypes.c_int64 * max(1, n - 1))()
+            L.call("sgt_svd_round_shapes", n, psh, inst.chi, ctypes.cast(out, L._PI64), ctypes.cast(cnt, L._PI64))
+            inst.out = [torch.empty((out[3 * k], out[3 * k + 1], out[3 * k + 2]), dtype=torch.float64, device=dev)
+                        for k in range(n)]
+            inst.counts = [cnt[k] for k in range(n - 1)]
+            inst.spectra = torch.zeros(max(1, sum(inst.counts)), dtype=torch.float64, device=dev)
+            inst.disc = torch.zeros(max(1, n - 1), dtype=torch.float64, device=dev)
+            inst.status = torch.zeros(1, dtype=torch.int32, device=dev)
+            inst.ovl = torch.zeros(2, dtype=torch.float64, device=dev)
+            wsh, _w = L.i64_array(inst.wsh)
+            xsh, _x = L.i64_array(inst.xsh)
+            need = L.query("sgt_mpo_mps_round_workspace_size", n, wsh, xsh, inst.chi, precision)
+            if need == 0:
+                raise L.SyngularError("sgt_mpo_mps_round_workspace_size", 1,
+                                      L.load().sgt_last_error().decode(errors="replace"))
+            outsh, _o = L.shape_array([tuple(o.shape) for o in inst.out])
+            ovl_need = L.query("sgt_overlap_workspace_size", n, xsh, outsh)
+            inst.ws_need = max(need, ovl_need)
+        # deal instances to streams, largest first, onto the least loaded stream
+        S = max(1, int(streams))
+        order = sorted(range(len(instances)), key=lambda i: -instances[i].ws_need)
+        self.lanes: List[List[int]] = [[] for _ in range(S)]
+        load = [0.0] * S
+        for i in order:
+            s = min(range(S), key=lambda j: load[j])
+            self.lanes[s].append(i)
+            load[s] += instances[i].ws_need
+        self.lanes = [lane for lane in self.lanes if lane]
+        lane_ws = [max(instances[i].ws_need for i in lane) for lane in self.lanes]
+        if sum(lane_ws) > budget_bytes:
+            raise MemoryError("batched workspaces need %d bytes > budget %d; use fewer streams"
+                              % (sum(lane_ws), budget_bytes))
+        self.ws = [torch.empty(b, dtype=torch.uint8, device=dev) for b in lane_ws]
+        self.streams = [torch.cuda.Stream() for _ in self.lanes]
+        self.graph: Optional[torch.cuda.CUDAGraph] = None
+        # keep the ctypes argument arrays alive for graph replays
+        self._keep = []
+        self._args = [self._build_args(inst) for inst in instances]
+
+    def _build_args(self, inst: Instance):
+        n = inst.n
+        wp, a1 = L.ptr_array(inst.W)
+        xp, a2 = L.ptr_array(inst.X)
+        op, a3 = L.ptr_array(inst.out)
+        wsh, a4 = L.i64_array(inst.wsh)
+        xsh, a5 = L.i64_array(inst.xsh)
+        osh, a6 = L.shape_array([tuple(o.shape) for o in inst.out])
+        self._keep += [a1, a2, a3, a4, a5, a6]
+        return (n, wp, wsh, xp, xsh, op, osh)
+
+    def launch(self):
+        """Enqueue every instance on its stream (no synchronisation)."""
+        cur = torch.cuda.current_stream()
+        for lane, ws, st in zip(self.lanes, self.ws, self.streams):
+            st.wait_stream(cur)
+            sp = L._c_vp(st.cuda_stream)
+            for i in lane:
+                inst = self.instances[i]
+                n, wp, wsh, xp, xsh, op, osh = self._args[i]
+                L.call("sgt_mpo_mps_round", n, wp, wsh, xp, xsh, inst.chi, self.precision, op,
+                       L.ptr(inst.spectra), L.ptr(inst.disc), L.ptr(inst.status), L.ptr(ws), ws.numel(), sp)
+                L.call("sgt_overlap_sweep", n, xp, xsh, op, osh, L.ptr(inst.ovl), L.ptr(ws), ws.numel(), sp)
+        for st in self.streams:
+            cur.wait_stream(st)
+
+    def capture(self):
+        """Capture launch() once into a CUDA graph (run launch() eagerly first
+        so every one-time set-up inside the library has happened)."""
+        self.launch()
+        torch.cuda.synchronize()
+        g = torch.cuda.CUDAGraph()
+        side = torch.cuda.Stream()
+        side.wait_stream(torch.cuda.current_stream())
+        with torch.cuda.stream(side):
+            with torch.cuda.graph(g, stream=side):
+                self.launch()
+        torch.cuda.current_stream().wait_stream(side)
+        self.graph = g
+        return g
+
+    def replay(self):
+        if self.graph is None:
+            self.capture()
+        self.graph.replay()
+
+    def overlaps(self) -> List[float]:
+        from .tensor._ops import decode_overlap
+
+        return [decode_overlap(inst.ovl.cpu().tolist()) for inst in self.instances]
+
+    def statuses(self) -> List[int]:
+        return [int(inst.status.item()) for inst in self.instances]
+
+
+def shape_class(instances: List[Instance]) -> str:
+    r = max(i.rmax for i in instances)
+    nb = int(round(sum(i.n for i in instances) / max(1, len(instances))))
+    return "r%d_n%d_c%d" % (2 ** math.ceil(math.log2(max(r, 1))), 8 * ((nb + 7) // 8), len(instances))
+
+
+def autotune(instances: List[Instance], precision: int = L.PREC_TF32X3,
+             candidates: Sequence[int] = (2, 4, 8, 16), budget_bytes: int = 160 << 30,
+             reps: int = 2) -> Dict:
+    """Pick the stream count with the fastest graph replay for this shape class;
+    the result is cached in TUNE_FILE."""
+    key = "%s_p%d" % (shape_class(instances), precision)
+    cache = {}
+    if os.path.exists(TUNE_FILE):
+        try:
+            with open(TUNE_FILE) as f:
+                cache = json.load(f)
+        except (OSError, ValueError):
+            cache = {}
+    if key in cache:
+        return cache[key]
+    best = None
+    trials = {}
+    for s in candidates:
+        try:
+            b = BatchedRound(instances, precision, streams=s, budget_bytes=budget_bytes)
+        except MemoryError:
+            continue
+        b.capture()
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        for _ in range(reps):
+            b.replay()
+        e1.record()
+        torch.cuda.synchronize()
+        ms = e0.elapsed_time(e1) / reps
+        trials[str(s)] = ms
+        if best is None or ms < best[1]:
+            best = (s, ms)
+        del b
+        torch.cuda.empty_cache()
+    res = {"streams": best[0] if best else candidates[0], "ms": best[1] if best else None, "trials": trials}
+    cache[key] = res
+    try:
+        with open(TUNE_FILE, "w") as f:
+            json.dump(cache, f, indent=1, sort_keys=True)
+    except OSError:
+        pass
+    return res
+
+
+def shard(indices: Sequence[int], rank: int, world: int) -> List[int]:
+    """Instances of this rank when a batch is spread over `world` GPUs (no
+    data exchange: every instance is independent)."""
+    return [i for k, i in enumerate(indices) if k % world == rank]

@@ -15,8 +15,9 @@
 // QR-then-SVD sweep decomposes, so the kept singular vectors / values are the
 // same.  GEMMs: tcgen05 kind::tf32 (one pass, or three passes on split
 // hi/lo operands); product cores and Gram matrices are held in FP32; the
-// eigen-solves are one-sided Jacobi on Z_k with FP32 columns and FP64 angles,
-// after which the kept eigenvectors are re-orthonormalised in FP64.
+// eigen-solves are two-sided block Jacobi on Z_k in one thread-block cluster
+// (eig.cu; one-sided Jacobi on the rows of Z_k when Z_k is too large), after
+// which the kept eigenvectors are re-orthonormalised in FP64.
 #include <float.h>
 
 #include <algorithm>
@@ -42,6 +43,9 @@ int split_f64(cudaStream_t st, const double* x, int64_t ldx, float* hi, float* l
 size_t jacobi_rows_ws_bytes_f32(int64_t n, int64_t m);
 int jacobi_rows_f32(cudaStream_t st, float* G, int64_t ldg, int64_t n, int64_t m, float* Vt,
                     int64_t ldv, float* s, int* status, Arena& ar);
+size_t sym_eig_ws_bytes(int64_t n);
+int sym_eig_f32(cudaStream_t st, const float* Z, int64_t ldz, int64_t n, float* Vt, int64_t ldt, float* lam,
+                int* status, Arena& ar, bool* done);
 
 namespace {
 
@@ -288,8 +292,8 @@ static int mixed_round_impl(cudaStream_t st, int n, const double* const* W, cons
   double* Sd = ar.take<double>(chi * chi);
   int* stat = ar.take<int>(n + 1);
   int* tc_err = ar.take<int>(1);
-  char* jscratch = ar.take<char>(jacobi_rows_ws_bytes_f32(cmax, cmax));
-  const size_t jbytes = jacobi_rows_ws_bytes_f32(cmax, cmax);
+  const size_t jbytes = std::max(jacobi_rows_ws_bytes_f32(cmax, cmax), sym_eig_ws_bytes(cmax));
+  char* jscratch = ar.take<char>(jbytes);
   if (ar.measure) return SGT_OK;
   SGT_REQUIRE(ar.ok(), SGT_ERR_WORKSPACE, "mpo_mps_round: workspace too small");
   SGT_CUDA(cudaMemsetAsync(stat, 0, sizeof(int) * (n + 1), st));
@@ -347,8 +351,15 @@ static int mixed_round_impl(cudaStream_t st, int n, const double* const* W, cons
     SGT_TRY(gemm_nt(st, passes, c, r, r, 1.f, Yth, Ytl, r, Gh[k], Gl[k], r, 0.f, GY, r, tc_err));
     SGT_TRY(split_tf32(st, GY, GYh, GYl, c * r));
     SGT_TRY(gemm_nt(st, passes, c, c, r, 1.f, Yth, Ytl, r, GYh, GYl, r, 0.f, Z, c, tc_err));
+    // eigenpairs of the symmetric Z: two-sided block Jacobi in one cluster when
+    // it fits, else the one-sided Jacobi on the rows of Z
     Arena ja(jscratch, jbytes);
-    SGT_TRY(jacobi_rows_f32(st, Z, c, c, c, Vt, c, lam, stat + k, ja));
+    bool eig_done = false;
+    SGT_TRY(sym_eig_f32(st, Z, c, c, Vt, c, lam, stat + k, ja, &eig_done));
+    if (!eig_done) {
+      Arena jb(jscratch, jbytes);
+      SGT_TRY(jacobi_rows_f32(st, Z, c, c, c, Vt, c, lam, stat + k, jb));
+    }
     // core_k = Vt[:keep], re-orthonormalised in FP64 by one Newton-Schulz step
     // V <- 1.5 V - 0.5 (V V^T) V (the FP32 rotations leave |V V^T - I| ~ 1e-6)
     f32_to_f64_kernel<<<gs(keep * c), 256, 0, st>>>(Vt, c, Vd, c, keep, c);

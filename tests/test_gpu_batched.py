@@ -1,0 +1,69 @@
+"""Batched uneven instances (the batched workload at small scale): eager launch,
+CUDA-graph capture and replay; every instance against the FP64 oracle."""
+import numpy as np
+import pytest
+import torch
+
+from oracle import tt_fp64 as O
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module", autouse=True)
+def built():
+    import __graft_entry__ as g
+
+    g.build()
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+
+
+def make(rng, count):
+    from syngular_gb300.batched import Instance
+
+    insts, ref = [], []
+    for _ in range(count):
+        n = int(rng.integers(4, 10))
+        d = int(rng.choice([2, 3, 4]))
+        chi = int(rng.integers(4, 17))
+        D = int(rng.choice([2, 4]))
+        X = O.random_mps_cores(rng, n, d, chi)
+        W = O.random_mpo_cores(rng, n, d, D)
+        insts.append(Instance(W, X, chi))
+        Zr, spec, disc = O.tt_svd_round(O.mpo_mps_product(W, X), chi)
+        ref.append((O.overlap(X, Zr), np.sqrt(O.overlap(X, X) * O.overlap(Zr, Zr))))
+    return insts, ref
+
+
+@pytest.mark.parametrize("prec,tol", [(0, 1e-12), (4, 1e-6)])
+def test_batched_eager_and_graph(prec, tol):
+    from syngular_gb300.batched import BatchedRound
+
+    rng = np.random.default_rng(77)
+    insts, ref = make(rng, 12)
+    b = BatchedRound(insts, precision=prec, streams=4)
+    b.launch()
+    torch.cuda.synchronize()
+    eager = b.overlaps()
+    assert all(s >= 0 for s in b.statuses())
+    for v, (r, scale) in zip(eager, ref):
+        assert abs(v - r) <= tol * scale
+    b.capture()
+    for inst in insts:
+        inst.ovl.zero_()
+    b.replay()
+    torch.cuda.synchronize()
+    replayed = b.overlaps()
+    np.testing.assert_allclose(replayed, eager, rtol=1e-12, atol=0)
+
+
+def test_autotune_caches_choice(tmp_path, monkeypatch):
+    import syngular_gb300.batched as B
+
+    monkeypatch.setattr(B, "TUNE_FILE", str(tmp_path / "tune.json"))
+    rng = np.random.default_rng(5)
+    insts, _ = make(rng, 6)
+    r1 = B.autotune(insts, precision=0, candidates=(1, 2), reps=1)
+    assert r1["streams"] in (1, 2) and set(r1["trials"]) <= {"1", "2"}
+    r2 = B.autotune(insts, precision=0, candidates=(1, 2), reps=1)
+    assert r2 == r1

@@ -1,0 +1,96 @@
+"""Continuous-batching serving loop: admission by HBM budget, overlapping jobs on
+separate streams, each result equal alone and in the mix."""
+import time
+
+import numpy as np
+import pytest
+import torch
+
+from oracle import tt_fp64 as O
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module", autouse=True)
+def built():
+    import __graft_entry__ as g
+
+    g.build()
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+
+
+def server_with_sessions(rng, count, budget=8 << 30, slots=4):
+    from syngular_gb300.serving import RoundServer
+
+    srv = RoundServer(budget_bytes=budget, slots=slots)
+    for i in range(count):
+        n = int(rng.integers(4, 9))
+        d = int(rng.choice([2, 4]))
+        chi = int(rng.integers(4, 13))
+        D = int(rng.choice([2, 4]))
+        srv.add_session("s%d" % i, mps=O.random_mps_cores(rng, n, d, chi), mpo=O.random_mpo_cores(rng, n, d, D))
+    return srv
+
+
+def jobs_for(rng, count):
+    from syngular_gb300.serving import Job
+
+    jobs = []
+    for i in range(count):
+        kind = ["round", "add_round", "overlap"][i % 3]
+        s = "s%d" % i
+        jobs.append(Job(kind=kind, session=s, chi=int(rng.integers(3, 9)), precision=0, other=s, job_id=i))
+    return jobs
+
+
+def summary(job):
+    if job.kind == "overlap":
+        from syngular_gb300.tensor._ops import decode_overlap
+
+        return decode_overlap(job.result.cpu().tolist())
+    cores = job.result[0]
+    from syngular_gb300.tensor import _ops
+
+    return _ops.overlap(cores, cores)
+
+
+def test_mix_equals_alone():
+    rng = np.random.default_rng(3)
+    srv = server_with_sessions(rng, 12).start()
+    jobs = jobs_for(rng, 12)
+    for j in jobs:
+        srv.submit(j)
+    for j in jobs:
+        assert j.done.wait(120), "job did not finish"
+        assert j.error is None, j.error
+    mixed = [summary(j) for j in jobs]
+    srv.stop()
+    # alone: one slot, one job at a time
+    rng = np.random.default_rng(3)
+    solo = server_with_sessions(rng, 12, slots=1).start()
+    jobs2 = jobs_for(rng, 12)
+    alone = []
+    for j in jobs2:
+        solo.submit(j)
+        assert j.done.wait(120)
+        alone.append(summary(j))
+    solo.stop()
+    np.testing.assert_allclose(mixed, alone, rtol=1e-12, atol=0)
+
+
+def test_budget_admission_and_rejection():
+    from syngular_gb300.serving import Job, latency_stats
+
+    rng = np.random.default_rng(9)
+    srv = server_with_sessions(rng, 4, budget=1 << 20, slots=4).start()  # 1 MB budget
+    big = Job(kind="round", session="s0", chi=8, precision=0)
+    srv.submit(big)
+    assert big.done.wait(60)
+    ok = Job(kind="overlap", session="s1", other="s1")
+    srv.submit(ok)
+    assert ok.done.wait(60)
+    srv.stop()
+    assert ok.error is None and big.error is not None and "budget" in big.error
+    st = latency_stats([ok])
+    assert st["count"] == 1 and st["p50_ms"] >= 0
