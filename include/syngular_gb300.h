@@ -255,6 +255,14 @@ SGT_API int sgt_tc_gemm_f32(int passes, int64_t M, int64_t N, int64_t K, float a
  * kernel milliseconds, algorithmic flops (2 M N K per launch) and launches. */
 SGT_API int sgt_tc_profile(int enable, double* ms, double* flops, long long* launches);
 
+/* Symmetric PSD eigen-decomposition in FP32 (the Gram-form bond solve):
+ * Z (n x n, overwritten) -> Vt rows = eigenvectors, lam descending.
+ * method 0: two-sided block Jacobi in one thread-block cluster (used when it
+ * fits, else method 1); method 1: one-sided Jacobi on the rows of Z. */
+SGT_API size_t sgt_sym_eig_f32_workspace_size(int64_t n);
+SGT_API int sgt_sym_eig_f32(float* Z, int64_t n, float* Vt, float* lam, int* status, int method,
+                            void* ws, size_t ws_bytes, void* stream);
+
 /* hi = TF32 rounding of x (round to nearest, ties away), lo = x - hi (lo may be NULL). */
 SGT_API int sgt_split_tf32(const float* x, float* hi, float* lo, int64_t n, void* stream);
 

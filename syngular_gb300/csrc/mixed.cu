@@ -44,6 +44,11 @@ size_t jacobi_rows_ws_bytes_f32(int64_t n, int64_t m);
 int jacobi_rows_f32(cudaStream_t st, float* G, int64_t ldg, int64_t n, int64_t m, float* Vt,
                     int64_t ldv, float* s, int* status, Arena& ar);
 size_t sym_eig_ws_bytes(int64_t n);
+size_t gram_step_scratch_floats(int64_t chi, int64_t d, int64_t chi2, int64_t D, int64_t dout, int64_t D2);
+bool gram_step_supported(int64_t D, int64_t d, int64_t dout, int64_t D2);
+int gram_step_structured(cudaStream_t st, int passes, const float* Gh, const float* Gl, const double* X,
+                         int64_t chi, int64_t d, int64_t chi2, const double* W, int64_t D, int64_t dout,
+                         int64_t D2, float* Gout, float* scratch, int* err);
 int sym_eig_f32(cudaStream_t st, const float* Z, int64_t ldz, int64_t n, float* Vt, int64_t ldt, float* lam,
                 int* status, Arena& ar, bool* done);
 
@@ -210,9 +215,15 @@ int transpose_f32(cudaStream_t st, float* dst, int64_t ldd, int64_t db, const fl
   return SGT_OK;
 }
 
+struct Site4 {
+  int64_t b, i, o, b2;
+};
+
+}  // namespace
+
 // C = alpha A B^T + beta C (A: M x K, B: N x K, row-major fp32 hi/lo pairs).
 // tcgen05 when TMA can address the operands, CUDA cores otherwise.
-int gemm_nt(cudaStream_t st, int passes, int64_t M, int64_t N, int64_t K, float alpha, const float* Ah,
+int gemm_nt_dispatch(cudaStream_t st, int passes, int64_t M, int64_t N, int64_t K, float alpha, const float* Ah,
             const float* Al, int64_t lda, const float* Bh, const float* Bl, int64_t ldb, float beta,
             float* C, int64_t ldc, int* err) {
   if (M <= 0 || N <= 0) return SGT_OK;
@@ -226,12 +237,6 @@ int gemm_nt(cudaStream_t st, int passes, int64_t M, int64_t N, int64_t K, float 
   SGT_LAUNCHED();
   return SGT_OK;
 }
-
-struct Site4 {
-  int64_t b, i, o, b2;
-};
-
-}  // namespace
 
 // ---------------------------------------------------------------------------
 static int mixed_round_impl(cudaStream_t st, int n, const double* const* W, const int64_t* ws4,
@@ -252,14 +257,27 @@ static int mixed_round_impl(cudaStream_t st, int n, const double* const* W, cons
   std::vector<int64_t> bb, x, cnt;
   svd_round_plan_public(n, shp.data(), chi, bb, x, cnt);
 
+  // structured Gram recursion (gram.cu) unless a core's bonds are too large
+  // for its shared-memory contraction kernel; then dense GEMMs on the
+  // transposed product cores
+  bool structured = true;
+  int64_t gscratch = 1;
+  for (int k = 0; k + 1 < n; ++k) {
+    structured = structured && gram_step_supported(w[k].b, w[k].i, w[k].o, w[k].b2);
+    gscratch = std::max<int64_t>(gscratch, (int64_t)gram_step_scratch_floats(xs[3 * k], xs[3 * k + 1],
+                                                                              xs[3 * k + 2], w[k].b, w[k].o,
+                                                                              w[k].b2));
+  }
   std::vector<float*> Ph(n), Pl(n), Pth(n), Ptl(n), Gh(n), Gl(n);
   int64_t rmax = 1, cmax = 1, smax = 1;
   for (int k = 0; k < n; ++k) {
     const int64_t sz = R[k] * Pd[k] * R[k + 1];
     Ph[k] = ar.take<float>(sz);
     Pl[k] = ar.take<float>(sz);
-    Pth[k] = ar.take<float>(sz);
-    Ptl[k] = ar.take<float>(sz);
+    if (!structured) {
+      Pth[k] = ar.take<float>(sz);
+      Ptl[k] = ar.take<float>(sz);
+    }
     Gh[k] = ar.take<float>(R[k] * R[k]);
     Gl[k] = ar.take<float>(R[k] * R[k]);
     rmax = std::max(rmax, R[k + 1]);
@@ -268,9 +286,11 @@ static int mixed_round_impl(cudaStream_t st, int n, const double* const* W, cons
     smax = std::max(smax, sz);
   }
   float* Gacc = ar.take<float>(rmax * rmax);
-  float* Ht = ar.take<float>(rmax * rmax);
-  float* Hth = ar.take<float>(rmax * rmax);
-  float* Htl = ar.take<float>(rmax * rmax);
+  float* Ht = structured ? nullptr : ar.take<float>(rmax * rmax);
+  float* Hth = structured ? nullptr : ar.take<float>(rmax * rmax);
+  float* Htl = structured ? nullptr : ar.take<float>(rmax * rmax);
+  float* gsc = structured ? ar.take<float>(gscratch) : nullptr;
+  float* Ytp = structured ? ar.take<float>(cmax * rmax) : nullptr;
   float* Fth = ar.take<float>(chi * rmax);
   float* Ftl = ar.take<float>(chi * rmax);
   float* Ftn = ar.take<float>(chi * rmax);
@@ -306,6 +326,7 @@ static int mixed_round_impl(cudaStream_t st, int n, const double* const* W, cons
     product_split_kernel<<<gs(sz), 256, 0, st>>>(X[k], W[k], Ph[k], Pl[k], w[k].b, w[k].i, w[k].o, a2,
                                                   w[k].b2, sz);
     SGT_LAUNCHED();
+    if (structured) continue;
     // Pt[p] (R' x R) = (P[:, p, :])^T, P[:, p, :] is R x R' with row stride p*R'
     SGT_TRY(transpose_f32(st, Pth[k], R[k], R[k + 1] * R[k], Ph[k], Pd[k] * R[k + 1], R[k + 1], R[k],
                           R[k + 1], Pd[k]));
@@ -315,16 +336,22 @@ static int mixed_round_impl(cudaStream_t st, int n, const double* const* W, cons
   // ---- left Gram recursion ----
   set_one_kernel<<<1, 1, 0, st>>>(Gh[0], Gl[0]);
   SGT_LAUNCHED();
-  for (int k = 0; k + 1 < n; ++k) {
+  // structured: G_k is kept with its columns in (b, a) order (see gram.cu)
+  for (int k = 0; structured && k + 1 < n; ++k) {
+    SGT_TRY(gram_step_structured(st, passes, Gh[k], Gl[k], X[k], xs[3 * k], xs[3 * k + 1], xs[3 * k + 2], W[k],
+                                 w[k].b, w[k].o, w[k].b2, Gacc, gsc, tc_err));
+    SGT_TRY(split_tf32(st, Gacc, Gh[k + 1], Gl[k + 1], R[k + 1] * R[k + 1]));
+  }
+  for (int k = 0; !structured && k + 1 < n; ++k) {
     const int64_t r = R[k], r2 = R[k + 1];
     for (int64_t pi = 0; pi < Pd[k]; ++pi) {
       const float* Ah = Pth[k] + pi * r2 * r;
       const float* Al = Ptl[k] + pi * r2 * r;
       // Ht (r2 x r) = Pt[p] G_k^T
-      SGT_TRY(gemm_nt(st, passes, r2, r, r, 1.f, Ah, Al, r, Gh[k], Gl[k], r, 0.f, Ht, r, tc_err));
+      SGT_TRY(gemm_nt_dispatch(st, passes, r2, r, r, 1.f, Ah, Al, r, Gh[k], Gl[k], r, 0.f, Ht, r, tc_err));
       SGT_TRY(split_tf32(st, Ht, Hth, Htl, r2 * r));
       // G_{k+1} += Pt[p] Ht^T
-      SGT_TRY(gemm_nt(st, passes, r2, r2, r, 1.f, Ah, Al, r, Hth, Htl, r, pi == 0 ? 0.f : 1.f, Gacc, r2,
+      SGT_TRY(gemm_nt_dispatch(st, passes, r2, r2, r, 1.f, Ah, Al, r, Hth, Htl, r, pi == 0 ? 0.f : 1.f, Gacc, r2,
                       tc_err));
     }
     SGT_TRY(split_tf32(st, Gacc, Gh[k + 1], Gl[k + 1], r2 * r2));
@@ -336,7 +363,7 @@ static int mixed_round_impl(cudaStream_t st, int n, const double* const* W, cons
     const int64_t r = R[k], r2 = R[k + 1], p = Pd[k], xc = x[k + 1], c = p * xc;
     // Yt (c x r): rows p*xc..: Ft (xc x r2) * P[:, p, :]^T
     for (int64_t pi = 0; pi < p; ++pi) {
-      SGT_TRY(gemm_nt(st, passes, xc, r, r2, 1.f, Fth, Ftl, r2, Ph[k] + pi * r2, Pl[k] + pi * r2, p * r2,
+      SGT_TRY(gemm_nt_dispatch(st, passes, xc, r, r2, 1.f, Fth, Ftl, r2, Ph[k] + pi * r2, Pl[k] + pi * r2, p * r2,
                       0.f, Yt + pi * xc * r, r, tc_err));
     }
     if (k == 0) {
@@ -348,9 +375,17 @@ static int mixed_round_impl(cudaStream_t st, int n, const double* const* W, cons
     const int64_t keep = x[k];
     SGT_TRY(split_tf32(st, Yt, Yth, Ytl, c * r));
     // GY^T (c x r) = Yt G_k^T ;  Z (c x c) = Yt GY
-    SGT_TRY(gemm_nt(st, passes, c, r, r, 1.f, Yth, Ytl, r, Gh[k], Gl[k], r, 0.f, GY, r, tc_err));
+    if (structured) {
+      // G_k's columns are in (b, a) order: contract with Yt's columns permuted alike
+      const int64_t chik = xs[3 * k], Dk = w[k].b;
+      SGT_TRY(transpose_f32(st, Ytp, chik, r, Yt, Dk, r, chik, Dk, c));
+      SGT_TRY(split_tf32(st, Ytp, Y, Yl, c * r));  // Y / Yl reused as the split of Ytp
+      SGT_TRY(gemm_nt_dispatch(st, passes, c, r, r, 1.f, Y, Yl, r, Gh[k], Gl[k], r, 0.f, GY, r, tc_err));
+    } else {
+      SGT_TRY(gemm_nt_dispatch(st, passes, c, r, r, 1.f, Yth, Ytl, r, Gh[k], Gl[k], r, 0.f, GY, r, tc_err));
+    }
     SGT_TRY(split_tf32(st, GY, GYh, GYl, c * r));
-    SGT_TRY(gemm_nt(st, passes, c, c, r, 1.f, Yth, Ytl, r, GYh, GYl, r, 0.f, Z, c, tc_err));
+    SGT_TRY(gemm_nt_dispatch(st, passes, c, c, r, 1.f, Yth, Ytl, r, GYh, GYl, r, 0.f, Z, c, tc_err));
     // eigenpairs of the symmetric Z: two-sided block Jacobi in one cluster when
     // it fits, else the one-sided Jacobi on the rows of Z
     Arena ja(jscratch, jbytes);
@@ -380,7 +415,7 @@ static int mixed_round_impl(cudaStream_t st, int n, const double* const* W, cons
     SGT_TRY(transpose_f32(st, Y, c, 0, Yt, r, 0, c, r, 1));
     SGT_TRY(split_tf32(st, Y, Yh, Yl, r * c));
     SGT_TRY(split_f64(st, out[k], c, Vh, Vl, keep, c));
-    SGT_TRY(gemm_nt(st, passes, keep, r, c, 1.f, Vh, Vl, c, Yh, Yl, c, 0.f, Ftn, r, tc_err));
+    SGT_TRY(gemm_nt_dispatch(st, passes, keep, r, c, 1.f, Vh, Vl, c, Yh, Yl, c, 0.f, Ftn, r, tc_err));
     SGT_TRY(split_tf32(st, Ftn, Fth, Ftl, keep * r));
   }
   if (status) {
