@@ -152,7 +152,7 @@ __global__ void __launch_bounds__(SJ_THREADS) sjacobi_kernel(const float* __rest
           if (fabsf(apq) > fmaxf(tol * sqrtf(fabsf(app)) * sqrtf(fabsf(aqq)), abs_floor)) {
             const float tau = (aqq - app) / (2.f * apq);
             const float t = copysignf(1.f, tau) / (fabsf(tau) + sqrtf(fmaf(tau, tau, 1.f)));
-            c = rsqrtf(fmaf(t, t, 1.f));
+            c = 1.f / sqrtf(fmaf(t, t, 1.f));
             s = t * c;
             any = 1;
           }

@@ -156,6 +156,17 @@ __global__ void f32_to_f64_kernel(const float* __restrict__ src, int64_t lds, do
   }
 }
 
+// Z <- (Z + Z^T) / 2 (the GEMM-formed Gram projection is symmetric only up to rounding)
+__global__ void symmetrize_kernel(float* __restrict__ Z, int64_t n) {
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n * n; i += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t r = i / n, c = i % n;
+    if (c <= r) continue;
+    const float v = 0.5f * (Z[r * n + c] + Z[c * n + r]);
+    Z[r * n + c] = v;
+    Z[c * n + r] = v;
+  }
+}
+
 __global__ void set_one_kernel(float* hi, float* lo) {
   hi[0] = 1.f;
   lo[0] = 0.f;
@@ -386,6 +397,8 @@ static int mixed_round_impl(cudaStream_t st, int n, const double* const* W, cons
     }
     SGT_TRY(split_tf32(st, GY, GYh, GYl, c * r));
     SGT_TRY(gemm_nt_dispatch(st, passes, c, c, r, 1.f, Yth, Ytl, r, GYh, GYl, r, 0.f, Z, c, tc_err));
+    symmetrize_kernel<<<gs(c * c), 256, 0, st>>>(Z, c);
+    SGT_LAUNCHED();
     // eigenpairs of the symmetric Z: two-sided block Jacobi in one cluster when
     // it fits, else the one-sided Jacobi on the rows of Z
     Arena ja(jscratch, jbytes);

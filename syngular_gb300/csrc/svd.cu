@@ -58,7 +58,7 @@ __device__ __forceinline__ bool jacobi_rotation(T a, T b, T c, double tol, doubl
     if (!(fabsf(fc) > (float)tol * sqrtf(fa) * sqrtf(fb) && fabsf(fc) > (float)abs_floor)) return false;
     const float zeta = (fb - fa) / (2.f * fc);
     const float t = copysignf(1.f, zeta) / (fabsf(zeta) + sqrtf(fmaf(zeta, zeta, 1.f)));
-    const float cf = rsqrtf(fmaf(t, t, 1.f));
+    const float cf = 1.f / sqrtf(fmaf(t, t, 1.f));
     cs_ = (T)cf;
     sn = (T)(cf * t);
     return true;
@@ -71,7 +71,7 @@ __device__ __forceinline__ bool jacobi_rotation(T a, T b, T c, double tol, doubl
         rot = 1;
         const double zeta = (db - da) / (2.0 * dc);
         const double t = copysign(1.0, zeta) / (fabs(zeta) + sqrt(fma(zeta, zeta, 1.0)));
-        cd = rsqrt(fma(t, t, 1.0));
+        cd = 1.0 / sqrt(fma(t, t, 1.0));
         sd = cd * t;
       }
     }
