@@ -367,6 +367,145 @@ def run_gpu(args, rank, world, local_rank):
     return 0
 
 
+# ---------------------------------------------------------------------------
+# secondary workloads: batched uneven instances, serving stream
+# ---------------------------------------------------------------------------
+
+def config3_instances(count=512, seed=3):
+    """Batched workload: count independent pairs, N ~ U[8,64], d in {2,3,4},
+    chi ~ U[16,128], D in {4,8,16}, entries N(0,1)/sqrt(chi*d)."""
+    import numpy as np
+
+    rng = np.random.default_rng(seed)
+    out = []
+    for _ in range(count):
+        n = int(rng.integers(8, 65))
+        d = int(rng.choice([2, 3, 4]))
+        chi = int(rng.integers(16, 129))
+        D = int(rng.choice([4, 8, 16]))
+        dims = [1] + [chi] * (n - 1) + [1]
+        X = [rng.standard_normal((dims[k], d, dims[k + 1])) / math.sqrt(chi * d) for k in range(n)]
+        wd = [1] + [D] * (n - 1) + [1]
+        W = [rng.standard_normal((wd[k], d, d, wd[k + 1])) / math.sqrt(D * d) for k in range(n)]
+        out.append((W, X, chi))
+    return out
+
+
+def run_batched(args):
+    import torch
+
+    import __graft_entry__ as g
+
+    g.build()
+    from syngular_gb300 import _lib as L
+    from syngular_gb300.batched import BatchedRound, Instance, autotune
+
+    data = config3_instances(args.instances)
+    insts = [Instance(W, X, chi) for W, X, chi in data]
+    tune = autotune(insts, precision=L.PREC_TF32X3, candidates=(4, 8), reps=1)
+    b = BatchedRound(insts, precision=L.PREC_TF32X3, streams=tune["streams"])
+    b.capture()
+    for _ in range(max(args.warmup, 3)):
+        b.replay()
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    for _ in range(args.steps):
+        b.replay()
+    e1.record()
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1) / args.steps
+    st = b.statuses()
+    # plain FP64 per-instance form on a sample, scaled to the batch by instance count
+    sample = insts[: args.plain_sample]
+    bp = BatchedRound(sample, precision=L.PREC_F64, streams=1)
+    bp.launch()
+    torch.cuda.synchronize()
+    p0, p1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    p0.record()
+    bp.launch()
+    p1.record()
+    torch.cuda.synchronize()
+    plain_ms_per_inst = p0.elapsed_time(p1) / len(sample)
+    out = {
+        "metric": "batched MPO.MPS+TT-SVD-round+overlap instances/s", "value": len(insts) / (ms / 1e3),
+        "unit": "instances/s", "n_gpus": 1, "steps": args.steps, "warmup": max(args.warmup, 3),
+        "ms_per_step": ms, "higher_is_better": True, "dtype": "tf32x3/f32", "data": "synthetic (seeded)",
+        "config": {"workload": "config3: %d instances, N~U[8,64], d in {2,3,4}, chi~U[16,128], D in {4,8,16}"
+                   % len(insts), "streams": tune["streams"], "graph": "one captured CUDA graph per batch",
+                   "autotune": tune},
+        "converged": sum(1 for x in st if x >= 0), "plain_fp64_instances_per_s": 1e3 / plain_ms_per_inst,
+        "plain_fp64_sample": len(sample),
+    }
+    print(json.dumps(out))
+    return 0
+
+
+def run_serving(args):
+    import numpy as np
+    import torch
+
+    import __graft_entry__ as g
+
+    g.build()
+    from syngular_gb300 import _lib as L
+    from syngular_gb300.serving import Job, RoundServer, latency_stats
+
+    rng = np.random.default_rng(11)
+    srv = RoundServer(budget_bytes=120 << 30, slots=8)
+    nsess = args.sessions
+    for i in range(nsess):
+        n = int(rng.integers(8, 129))
+        d = int(rng.choice([2, 4]))
+        chi = int(round(math.exp(rng.uniform(math.log(8), math.log(512)))))
+        D = int(rng.choice([4, 16]))
+        dims = [1] + [chi] * (n - 1) + [1]
+        X = [rng.standard_normal((dims[k], d, dims[k + 1])) / math.sqrt(chi * d) for k in range(n)]
+        wd = [1] + [D] * (n - 1) + [1]
+        W = [rng.standard_normal((wd[k], d, d, wd[k + 1])) / math.sqrt(D * d) for k in range(n)]
+        srv.add_session("s%d" % i, mps=X, mpo=W)
+        srv.sessions["s%d" % i]["chi"] = chi
+    srv.start()
+    # seeded Poisson arrivals
+    t = 0.0
+    arrivals = []
+    while t < args.duration:
+        t += rng.exponential(1.0 / args.rate)
+        arrivals.append(t)
+    jobs = []
+    t0 = time.perf_counter()
+    for k, ta in enumerate(arrivals):
+        now = time.perf_counter() - t0
+        if ta > now:
+            time.sleep(ta - now)
+        sid = "s%d" % int(rng.integers(0, nsess))
+        kind = ["round", "add_round", "overlap"][int(rng.integers(0, 3))]
+        chi = srv.sessions[sid]["chi"]
+        j = Job(kind=kind, session=sid, chi=chi, precision=L.PREC_TF32X3, other=sid, job_id=k,
+                arrival=t0 + ta)
+        jobs.append(srv.submit(j))
+    deadline = time.perf_counter() + args.drain
+    for j in jobs:
+        j.done.wait(max(0.0, deadline - time.perf_counter()))
+    wall = time.perf_counter() - t0
+    srv.stop()
+    done = [j for j in jobs if j.done.is_set() and j.error is None]
+    rejected = [j for j in jobs if j.error is not None]
+    stats = latency_stats(done)
+    out = {
+        "metric": "serving jobs/s with p50/p99 latency", "value": len(done) / wall, "unit": "jobs/s",
+        "n_gpus": 1, "higher_is_better": True, "dtype": "tf32x3/f32 (round), f64 (add_round, overlap)",
+        "data": "synthetic seeded Poisson stream",
+        "config": {"workload": "config5 stream: %.0f jobs/s for %.1f s, %d resident sessions, N~U[8,128], "
+                               "d in {2,4}, chi log-uniform [8,512], D in {4,16}, HBM budget 120 GB"
+                               % (args.rate, args.duration, nsess), "slots": 8},
+        "submitted": len(jobs), "completed": len(done), "rejected_or_failed": len(rejected),
+        "unfinished": len(jobs) - len(done) - len(rejected), "latency": stats, "wall_s": wall,
+    }
+    print(json.dumps(out))
+    return 0
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -376,7 +515,18 @@ def main():
     ap.add_argument("--precision", default="tf32x3", choices=["tf32x3", "tf32", "f64"])
     ap.add_argument("--no-plain", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--workload", default="config2", choices=["config2", "batched", "serving"])
+    ap.add_argument("--instances", type=int, default=512)
+    ap.add_argument("--plain-sample", type=int, default=8)
+    ap.add_argument("--rate", type=float, default=2000.0)
+    ap.add_argument("--duration", type=float, default=2.0)
+    ap.add_argument("--sessions", type=int, default=64)
+    ap.add_argument("--drain", type=float, default=120.0)
     args = ap.parse_args()
+    if args.workload == "batched":
+        return run_batched(args)
+    if args.workload == "serving":
+        return run_serving(args)
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
     local_rank = int(os.environ.get("LOCAL_RANK", "0"))

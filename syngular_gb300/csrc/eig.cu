@@ -83,7 +83,7 @@ __global__ void __launch_bounds__(SJ_THREADS) sjacobi_kernel(const float* __rest
   __shared__ int s_blkI[32], s_blkJ[32];
   __shared__ int s_active[32];    // pair rotated this step (read remotely from solvers)
   __shared__ int s_rot[2];
-  __shared__ float s_rot_param[16][2];
+  __shared__ float s_rot_param[16][3];
 
   // ---- load own rows: Z (zero padded) and V = I ----
   for (int i = tid; i < w2 * ld; i += SJ_THREADS) {
@@ -148,16 +148,18 @@ __global__ void __launch_bounds__(SJ_THREADS) sjacobi_kernel(const float* __rest
           const int q0 = ((w2 - 1 - tid - 1 + sub) % (w2 - 1)) + 1;
           const int p = min(p0, q0), q = max(p0, q0);
           const float app = sm.S[p * 33 + p], aqq = sm.S[q * 33 + q], apq = sm.S[p * 33 + q];
-          float c = 1.f, s = 0.f;
+          float c = 1.f, s = 0.f, ta = 0.f;
           if (fabsf(apq) > fmaxf(tol * sqrtf(fabsf(app)) * sqrtf(fabsf(aqq)), abs_floor)) {
             const float tau = (aqq - app) / (2.f * apq);
             const float t = copysignf(1.f, tau) / (fabsf(tau) + sqrtf(fmaf(tau, tau, 1.f)));
             c = 1.f / sqrtf(fmaf(t, t, 1.f));
             s = t * c;
+            ta = s / (1.f + c);
             any = 1;
           }
           s_rot_param[tid][0] = c;
           s_rot_param[tid][1] = s;
+          s_rot_param[tid][2] = ta;
         }
         __syncthreads();
         // rows: S <- J^T S
@@ -166,11 +168,11 @@ __global__ void __launch_bounds__(SJ_THREADS) sjacobi_kernel(const float* __rest
           const int p0 = (k == 0) ? 0 : ((k - 1 + sub) % (w2 - 1)) + 1;
           const int q0 = ((w2 - 1 - k - 1 + sub) % (w2 - 1)) + 1;
           const int p = min(p0, q0), q = max(p0, q0);
-          const float c = s_rot_param[k][0], s = s_rot_param[k][1];
+          const float s = s_rot_param[k][1], ta = s_rot_param[k][2];
           if (s == 0.f) continue;
           const float x = sm.S[p * 33 + col], y = sm.S[q * 33 + col];
-          sm.S[p * 33 + col] = c * x - s * y;
-          sm.S[q * 33 + col] = s * x + c * y;
+          sm.S[p * 33 + col] = x - s * (y + ta * x);
+          sm.S[q * 33 + col] = y + s * (x - ta * y);
         }
         __syncthreads();
         // columns: S <- S J, Q <- Q J
@@ -181,12 +183,12 @@ __global__ void __launch_bounds__(SJ_THREADS) sjacobi_kernel(const float* __rest
           const int p0 = (k == 0) ? 0 : ((k - 1 + sub) % (w2 - 1)) + 1;
           const int q0 = ((w2 - 1 - k - 1 + sub) % (w2 - 1)) + 1;
           const int p = min(p0, q0), q = max(p0, q0);
-          const float c = s_rot_param[k][0], s = s_rot_param[k][1];
+          const float s = s_rot_param[k][1], ta = s_rot_param[k][2];
           if (s == 0.f) continue;
           float* M = which ? sm.Q : sm.S;
           const float x = M[row * 33 + p], y = M[row * 33 + q];
-          M[row * 33 + p] = c * x - s * y;
-          M[row * 33 + q] = s * x + c * y;
+          M[row * 33 + p] = x - s * (y + ta * x);
+          M[row * 33 + q] = y + s * (x - ta * y);
         }
         __syncthreads();
       }

@@ -47,12 +47,14 @@ __device__ __forceinline__ T wsum_t(T v) {
 
 // Rotation for the pair (p, q) with a = |g_p|^2, b = |g_q|^2, c = g_p.g_q
 // (identical on all lanes after the xor-shuffle reductions).  Returns whether
-// to rotate, and cs / sn.  T = float: computed in FP32 on every lane (cheap);
+// to rotate, cs / sn and tau = sn / (1 + cs): rotations are applied as
+// x' = x - sn (y + tau x), y' = y + sn (x - tau y) (Rutishauser), which keeps
+// the pair's norm to O(sn^4) even when 1 + t^2 rounds to 1.  T = float: computed in FP32 on every lane (cheap);
 // T = double: computed in FP64 on lane 0 and broadcast -- GB300 runs FP64 at a
 // small fraction of its FP32 rate, so 32 redundant lanes would dominate.
 template <typename T>
 __device__ __forceinline__ bool jacobi_rotation(T a, T b, T c, double tol, double abs_floor, int lane,
-                                                T& cs_, T& sn) {
+                                                T& cs_, T& sn, T& tau) {
   if (sizeof(T) == 4) {
     const float fa = (float)a, fb = (float)b, fc = (float)c;
     if (!(fabsf(fc) > (float)tol * sqrtf(fa) * sqrtf(fb) && fabsf(fc) > (float)abs_floor)) return false;
@@ -61,6 +63,7 @@ __device__ __forceinline__ bool jacobi_rotation(T a, T b, T c, double tol, doubl
     const float cf = 1.f / sqrtf(fmaf(t, t, 1.f));
     cs_ = (T)cf;
     sn = (T)(cf * t);
+    tau = (T)(sn / (1.f + cf));
     return true;
   } else {
     int rot = 0;
@@ -79,6 +82,7 @@ __device__ __forceinline__ bool jacobi_rotation(T a, T b, T c, double tol, doubl
     if (!rot) return false;
     cs_ = (T)__shfl_sync(0xffffffffu, cd, 0);
     sn = (T)__shfl_sync(0xffffffffu, sd, 0);
+    tau = (T)(sn / (T(1) + cs_));
     return true;
   }
 }
@@ -130,20 +134,20 @@ __global__ void __launch_bounds__(JAC_THREADS) jacobi_kernel(T* __restrict__ G, 
         a = wsum_t(a);
         b = wsum_t(b);
         c = wsum_t(c);
-        T cs_, sn;
-        if (jacobi_rotation<T>(a, b, c, tol, 0.0, lane, cs_, sn)) {
+        T cs_, sn, tau;
+        if (jacobi_rotation<T>(a, b, c, tol, 0.0, lane, cs_, sn, tau)) {
           ++my_rot;
           for (int64_t e = lane; e < m; e += 32) {
             T x = gp[e], y = gq[e];
-            gp[e] = cs_ * x - sn * y;
-            gq[e] = sn * x + cs_ * y;
+            gp[e] = x - sn * (y + tau * x);
+            gq[e] = y + sn * (x - tau * y);
           }
           T* vp = Vt + (int64_t)p * ldv;
           T* vq = Vt + (int64_t)q * ldv;
           for (int e = lane; e < n; e += 32) {
             T x = vp[e], y = vq[e];
-            vp[e] = cs_ * x - sn * y;
-            vq[e] = sn * x + cs_ * y;
+            vp[e] = x - sn * (y + tau * x);
+            vq[e] = y + sn * (x - tau * y);
           }
         }
       }
@@ -303,20 +307,20 @@ __global__ void __launch_bounds__(JAC_THREADS) bjacobi_kernel(T* __restrict__ G,
           a = wsum_t(a);
           b = wsum_t(b);
           c = wsum_t(c);
-          T cs_, sn;
-          if (jacobi_rotation<T>(a, b, c, tol, abs_floor, lane, cs_, sn)) {
+          T cs_, sn, tau;
+          if (jacobi_rotation<T>(a, b, c, tol, abs_floor, lane, cs_, sn, tau)) {
             ++my_rot;
             for (int e = lane; e < m; e += 32) {
               const T x = rp[e], y = rq[e];
-              rp[e] = cs_ * x - sn * y;
-              rq[e] = sn * x + cs_ * y;
+              rp[e] = x - sn * (y + tau * x);
+              rq[e] = y + sn * (x - tau * y);
             }
             T* vp = vt_smem ? rp + m : Vt + (int64_t)gp * ldv;
             T* vq = vt_smem ? rq + m : Vt + (int64_t)gq * ldv;
             for (int e = lane; e < n; e += 32) {
               const T x = vp[e], y = vq[e];
-              vp[e] = cs_ * x - sn * y;
-              vq[e] = sn * x + cs_ * y;
+              vp[e] = x - sn * (y + tau * x);
+              vq[e] = y + sn * (x - tau * y);
             }
           }
         }
