@@ -15,9 +15,9 @@
 // QR-then-SVD sweep decomposes, so the kept singular vectors / values are the
 // same.  GEMMs: tcgen05 kind::tf32 (one pass, or three passes on split
 // hi/lo operands); product cores and Gram matrices are held in FP32; the
-// eigen-solves are two-sided block Jacobi on Z_k in one thread-block cluster
-// (eig.cu; one-sided Jacobi on the rows of Z_k when Z_k is too large), after
-// which the kept eigenvectors are re-orthonormalised in FP64.
+// eigen-solves are one-sided block Jacobi on the rows of Z_k in one
+// thread-block cluster (svd.cu), after which the kept eigenvectors are
+// re-orthonormalised in FP64.
 #include <float.h>
 
 #include <algorithm>
@@ -399,15 +399,11 @@ static int mixed_round_impl(cudaStream_t st, int n, const double* const* W, cons
     SGT_TRY(gemm_nt_dispatch(st, passes, c, c, r, 1.f, Yth, Ytl, r, GYh, GYl, r, 0.f, Z, c, tc_err));
     symmetrize_kernel<<<gs(c * c), 256, 0, st>>>(Z, c);
     SGT_LAUNCHED();
-    // eigenpairs of the symmetric Z: two-sided block Jacobi in one cluster when
-    // it fits, else the one-sided Jacobi on the rows of Z
+    // eigenpairs of the symmetric Z: one-sided Jacobi on the rows of Z (block,
+    // cluster-resident).  The two-sided solver (eig.cu) converges in fewer
+    // sweeps but its FP32 stopping floor costs accuracy next to the cut.
     Arena ja(jscratch, jbytes);
-    bool eig_done = false;
-    SGT_TRY(sym_eig_f32(st, Z, c, c, Vt, c, lam, stat + k, ja, &eig_done));
-    if (!eig_done) {
-      Arena jb(jscratch, jbytes);
-      SGT_TRY(jacobi_rows_f32(st, Z, c, c, c, Vt, c, lam, stat + k, jb));
-    }
+    SGT_TRY(jacobi_rows_f32(st, Z, c, c, c, Vt, c, lam, stat + k, ja));
     // core_k = Vt[:keep], re-orthonormalised in FP64 by one Newton-Schulz step
     // V <- 1.5 V - 0.5 (V V^T) V (the FP32 rotations leave |V V^T - I| ~ 1e-6)
     f32_to_f64_kernel<<<gs(keep * c), 256, 0, st>>>(Vt, c, Vd, c, keep, c);

@@ -192,9 +192,11 @@ __global__ void __launch_bounds__(JAC_THREADS) jacobi_kernel(T* __restrict__ G, 
 // below m*(eps*|G|_F)^2 are skipped: such pairs are numerically zero columns
 // that FP rounding would otherwise keep re-rotating.
 constexpr int BJ_MAX_SLOT_BYTES = 64 * 1024;
+constexpr int BJ_THREADS = 512;  // 16 warps: one warp per pair of a sub-step (bs = 16)
+constexpr int BJ_WARPS = BJ_THREADS / 32;
 
 template <typename T>
-__global__ void __launch_bounds__(JAC_THREADS) bjacobi_kernel(T* __restrict__ G, int64_t ldg,
+__global__ void __launch_bounds__(BJ_THREADS) bjacobi_kernel(T* __restrict__ G, int64_t ldg,
                                                               T* __restrict__ Vt, int64_t ldv, int n,
                                                               int m, int bs, int vt_smem, double tol,
                                                               T* __restrict__ norms,
@@ -230,7 +232,7 @@ __global__ void __launch_bounds__(JAC_THREADS) bjacobi_kernel(T* __restrict__ G,
   for (int sl = 0; sl < 2; ++sl) {
     const int blk = slot_pos(rank, sl);
     if (tid == 0) s_blk[sl] = blk;
-    for (int64_t i = tid; i < slot_elems; i += JAC_THREADS) {
+    for (int64_t i = tid; i < slot_elems; i += BJ_THREADS) {
       const int r = (int)(i / row_len), e = (int)(i % row_len);
       const int gr = blk * bs + r;
       T v = T(0);
@@ -239,7 +241,7 @@ __global__ void __launch_bounds__(JAC_THREADS) bjacobi_kernel(T* __restrict__ G,
     }
   }
   if (!vt_smem) {
-    for (int64_t i = tid; i < (int64_t)n * n; i += JAC_THREADS) {
+    for (int64_t i = tid; i < (int64_t)n * n; i += BJ_THREADS) {
       // Vt = I in global memory; each CTA initialises its own rows
       const int r = (int)(i / n), c = (int)(i % n);
       const int b = r / bs;
@@ -250,7 +252,7 @@ __global__ void __launch_bounds__(JAC_THREADS) bjacobi_kernel(T* __restrict__ G,
   // |G|_F^2 over the cluster
   {
     double acc = 0.0;
-    for (int64_t i = tid; i < 2 * (int64_t)slot_elems; i += JAC_THREADS) {
+    for (int64_t i = tid; i < 2 * (int64_t)slot_elems; i += BJ_THREADS) {
       const int e = (int)(i % row_len);
       if (e < m) {
         const double v = (double)slots[i];
@@ -258,13 +260,13 @@ __global__ void __launch_bounds__(JAC_THREADS) bjacobi_kernel(T* __restrict__ G,
       }
     }
     for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
-    __shared__ double s_red[JAC_WARPS];
+    __shared__ double s_red[BJ_WARPS];
     if (lane == 0) s_red[warp] = acc;
     if (tid < 2) s_rot[tid] = 0;
     __syncthreads();
     if (tid == 0) {
       double t = 0.0;
-      for (int w = 0; w < JAC_WARPS; ++w) t += s_red[w];
+      for (int w = 0; w < BJ_WARPS; ++w) t += s_red[w];
       s_norm = t;
     }
     cluster.sync();
@@ -291,7 +293,7 @@ __global__ void __launch_bounds__(JAC_THREADS) bjacobi_kernel(T* __restrict__ G,
     for (int step = 0; step < nblk - 1; ++step) {
       // ---- all pairs of the 2*bs local rows ----
       for (int sub = 0; sub < W - 1; ++sub) {
-        for (int i = warp; i < bs; i += JAC_WARPS) {
+        for (int i = warp; i < bs; i += BJ_WARPS) {
           int p = rr_index(i, sub, W), q = rr_index(W - 1 - i, sub, W);
           const int gp = s_blk[p / bs] * bs + (p % bs), gq = s_blk[q / bs] * bs + (q % bs);
           if (gp >= n || gq >= n) continue;
@@ -344,10 +346,10 @@ __global__ void __launch_bounds__(JAC_THREADS) bjacobi_kernel(T* __restrict__ G,
       const uint4* s0 = reinterpret_cast<const uint4*>(r0);
       const uint4* s1 = reinterpret_cast<const uint4*>(r1);
       uint4* st4 = reinterpret_cast<uint4*>(stage);
-      uint4 regs[BJ_MAX_SLOT_BYTES / 16 / JAC_THREADS];
+      uint4 regs[BJ_MAX_SLOT_BYTES / 16 / BJ_THREADS];
 #pragma unroll
-      for (int j = 0; j < BJ_MAX_SLOT_BYTES / 16 / JAC_THREADS; ++j) {
-        const int idx = tid + j * JAC_THREADS;
+      for (int j = 0; j < BJ_MAX_SLOT_BYTES / 16 / BJ_THREADS; ++j) {
+        const int idx = tid + j * BJ_THREADS;
         if (idx < n4) {
           st4[idx] = s0[idx];
           regs[j] = s1[idx];
@@ -357,8 +359,8 @@ __global__ void __launch_bounds__(JAC_THREADS) bjacobi_kernel(T* __restrict__ G,
       uint4* d0 = reinterpret_cast<uint4*>(slots);
       uint4* d1 = reinterpret_cast<uint4*>(slots + slot_elems);
 #pragma unroll
-      for (int j = 0; j < BJ_MAX_SLOT_BYTES / 16 / JAC_THREADS; ++j) {
-        const int idx = tid + j * JAC_THREADS;
+      for (int j = 0; j < BJ_MAX_SLOT_BYTES / 16 / BJ_THREADS; ++j) {
+        const int idx = tid + j * BJ_THREADS;
         if (idx < n4) {
           d0[idx] = st4[idx];
           d1[idx] = regs[j];
@@ -384,7 +386,7 @@ __global__ void __launch_bounds__(JAC_THREADS) bjacobi_kernel(T* __restrict__ G,
   // sweeps, so use the recorded block ids) and row norms
   for (int sl = 0; sl < 2; ++sl) {
     const int blk = s_blk[sl];
-    for (int64_t i = tid; i < slot_elems; i += JAC_THREADS) {
+    for (int64_t i = tid; i < slot_elems; i += BJ_THREADS) {
       const int r = (int)(i / row_len), e = (int)(i % row_len);
       const int gr = blk * bs + r;
       if (gr >= n) continue;
@@ -392,7 +394,7 @@ __global__ void __launch_bounds__(JAC_THREADS) bjacobi_kernel(T* __restrict__ G,
       if (e < m) G[(int64_t)gr * ldg + e] = v;
       else Vt[(int64_t)gr * ldv + (e - m)] = v;
     }
-    for (int r = warp; r < bs; r += JAC_WARPS) {
+    for (int r = warp; r < bs; r += BJ_WARPS) {
       const int gr = blk * bs + r;
       if (gr >= n) continue;
       const T* row = slots + (int64_t)sl * slot_elems + (int64_t)r * row_len;
@@ -508,7 +510,7 @@ int jacobi_rows_t(cudaStream_t st, T* G, int64_t ldg, int64_t n, int64_t m, T* V
       const double tolb = jacobi_tol<T>(m);
       cudaLaunchConfig_t cfg = {};
       cfg.gridDim = dim3(csb, 1, 1);
-      cfg.blockDim = dim3(JAC_THREADS, 1, 1);
+      cfg.blockDim = dim3(BJ_THREADS, 1, 1);
       cfg.dynamicSmemBytes = (size_t)3 * slot_bytes;
       cfg.stream = st;
       cudaLaunchAttribute attr[1];

@@ -83,7 +83,7 @@ def test_budget_admission_and_rejection():
     from syngular_gb300.serving import Job, latency_stats
 
     rng = np.random.default_rng(9)
-    srv = server_with_sessions(rng, 4, budget=1 << 20, slots=4).start()  # 1 MB budget
+    srv = server_with_sessions(rng, 4, budget=16 << 10, slots=4).start()  # 16 KB budget
     big = Job(kind="round", session="s0", chi=8, precision=0)
     srv.submit(big)
     assert big.done.wait(60)
