@@ -40,7 +40,11 @@ sys.path.insert(0, ROOT)
 N_SITES, D_PHYS, CHI, D_MPO = 64, 2, 256, 16
 SEED = 2024
 METRIC = "MPO·MPS+SVD-round sweeps/s at χ=256 vs plain FP64 GPU; p50/p99 job latency"
-WORKLOAD = "config2: MPS N=64 d=2 chi=256 x MPO D=16 -> raw product (bond 4096) -> TT-SVD round to chi=256 -> <X|Z>"
+
+
+def workload_name():
+    return ("config2: MPS N=%d d=2 chi=256 x MPO D=16 -> raw product (bond 4096) -> TT-SVD round to chi=256 -> <X|Z>"
+            % N_SITES) + ("" if N_SITES == 64 else " (shortened chain for profiling, not the headline)")
 
 
 def make_inputs():
@@ -199,7 +203,7 @@ def run_reference(args, rank, world):
         "impl": "reference", "metric": METRIC, "value": v, "unit": "sweeps/s", "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": t_sweep * 1e3, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded, config-2 shapes)",
-        "config": {"workload": WORKLOAD, "cpu": "numpy FP64 port of the sweep (Householder QR + LAPACK SVD)"},
+        "config": {"workload": workload_name(), "cpu": "numpy FP64 port of the sweep (Householder QR + LAPACK SVD)"},
         "cpu_baseline": {"value": v, "unit": "sweeps/s", "cores": os.cpu_count(), "kind": "port",
                          "sample": "each step = one full-size middle site, scaled to 64 sites by flops (x%.1f)" % scale},
         "e2e": {"value": v, "unit": "sweeps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
@@ -303,12 +307,13 @@ def run_gpu(args, rank, world, local_rank):
         "warmup": max(args.warmup, 3), "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": {"tf32x3": "tf32x3/f32", "tf32": "tf32/f32", "f64": "f64"}[args.precision],
         "data": "synthetic (seeded N(0,1)/sqrt(chi*d) cores)",
-        "config": {"workload": WORKLOAD, "form": args.precision, "l2": "inputs larger than L2 (product cores 34 GB)",
+        "config": {"workload": workload_name(), "form": args.precision, "l2": "inputs larger than L2 (split product cores %.1f GB)" % (N_SITES * 4096 * 2 * 4096 * 8 / 1e9),
                    "parallelism": "replicas" if world > 1 else "single GPU"},
         "e2e": {"value": e2e_value, "unit": "sweeps/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": 16},
         "gpu_launches": int(launches),
         "clocks": clk,
         "overlap": ov_fast,
+        "jacobi_sweeps_max": int(status.item()),
     }
     # roofline of the dominant kernel (tcgen05 GEMM), from the live events
     peaks = {}
@@ -400,14 +405,23 @@ def run_batched(args):
     from syngular_gb300 import _lib as L
     from syngular_gb300.batched import BatchedRound, Instance, autotune
 
+    t_start = time.perf_counter()
+
+    def log(msg):
+        print("[batched %7.1f s] %s" % (time.perf_counter() - t_start, msg), file=sys.stderr, flush=True)
+
     data = config3_instances(args.instances)
     insts = [Instance(W, X, chi) for W, X, chi in data]
+    log("%d instances resident" % len(insts))
     tune = autotune(insts, precision=L.PREC_TF32X3, candidates=(4, 8), reps=1)
+    log("autotune: %s" % json.dumps(tune))
     b = BatchedRound(insts, precision=L.PREC_TF32X3, streams=tune["streams"])
     b.capture()
+    log("graph captured")
     for _ in range(max(args.warmup, 3)):
         b.replay()
     torch.cuda.synchronize()
+    log("warm-up replays done")
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     e0.record()
     for _ in range(args.steps):
@@ -416,6 +430,7 @@ def run_batched(args):
     torch.cuda.synchronize()
     ms = e0.elapsed_time(e1) / args.steps
     st = b.statuses()
+    log("timed replays: %.1f ms per batch" % ms)
     # plain FP64 per-instance form on a sample, scaled to the batch by instance count
     sample = insts[: args.plain_sample]
     bp = BatchedRound(sample, precision=L.PREC_F64, streams=1)
@@ -427,6 +442,7 @@ def run_batched(args):
     p1.record()
     torch.cuda.synchronize()
     plain_ms_per_inst = p0.elapsed_time(p1) / len(sample)
+    log("plain FP64 sample: %.1f ms per instance" % plain_ms_per_inst)
     out = {
         "metric": "batched MPO.MPS+TT-SVD-round+overlap instances/s", "value": len(insts) / (ms / 1e3),
         "unit": "instances/s", "n_gpus": 1, "steps": args.steps, "warmup": max(args.warmup, 3),
@@ -522,7 +538,11 @@ def main():
     ap.add_argument("--duration", type=float, default=2.0)
     ap.add_argument("--sessions", type=int, default=64)
     ap.add_argument("--drain", type=float, default=120.0)
+    ap.add_argument("--sites", type=int, default=64, help="chain length (64 = the headline workload; shorter "
+                    "chains only for profiling captures)")
     args = ap.parse_args()
+    global N_SITES
+    N_SITES = max(3, int(args.sites))
     if args.workload == "batched":
         return run_batched(args)
     if args.workload == "serving":
