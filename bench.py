@@ -362,9 +362,14 @@ def run_gpu(args, rank, world, local_rank):
         out["plain_fp64"] = {"sweeps_per_s": world * 1e3 / plain_ms, "ms_per_sweep": plain_ms, "steps": 1,
                              "warmup": 1, "status": int(status_p.item())}
         out["speedup_vs_plain_fp64"] = value / (world * 1e3 / plain_ms)
+        # 1 - |<Z|Z_fp64>| / (|Z| |Z_fp64|): how far the rounded state of the
+        # fast form is from the FP64 one (gauge-invariant)
+        nzf = math.sqrt(abs(_ops.overlap(Z, Z)))
+        fid = abs(_ops.overlap(Z, Zp)) / (nzf * nz)
         out["error_vs_fp64"] = {"overlap_rel": abs(ov_fast - ov_plain) / abs(ov_plain),
                                 "overlap_norm": abs(ov_fast - ov_plain) / (nx * nz),
-                                "overlap_fp64": ov_plain}
+                                "overlap_fp64": ov_plain, "state_infidelity": 1.0 - fid,
+                                "norm_rel": abs(nzf - nz) / nz}
     if rank == 0 and not args.no_cpu:
         out["cpu_baseline"] = cpu_baseline_measure()
     if rank == 0:

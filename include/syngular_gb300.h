@@ -258,10 +258,20 @@ SGT_API int sgt_tc_profile(int enable, double* ms, double* flops, long long* lau
 /* Symmetric PSD eigen-decomposition in FP32 (the Gram-form bond solve):
  * Z (n x n, overwritten) -> Vt rows = eigenvectors, lam descending.
  * method 0: two-sided block Jacobi in one thread-block cluster (used when it
- * fits, else method 1); method 1: one-sided Jacobi on the rows of Z. */
+ * fits, else method 1); method 1: one-sided Jacobi on the rows of Z;
+ * method 2: one-sided Jacobi on the rows of the Cholesky factor of Z taken in
+ * decreasing-diagonal order (about half the sweeps; vectors by normalisation);
+ * method 3: method 2 followed by accumulated Jacobi on the rows of V^T Z.
+ * status: sweeps performed (method 3: both phases), -1 at the sweep cap. */
 SGT_API size_t sgt_sym_eig_f32_workspace_size(int64_t n);
 SGT_API int sgt_sym_eig_f32(float* Z, int64_t n, float* Vt, float* lam, int* status, int method,
                             void* ws, size_t ws_bytes, void* stream);
+
+/* Eigensolver used for the bond problems of the Gram form (sgt_mpo_mps_round
+ * with TF32 / TF32X3): the sgt_sym_eig_f32 method 1, 2 or 3 (other values leave
+ * it unchanged).  Returns the previous choice.  The initial choice is 1, or the
+ * value of the environment variable SGT_EIG_METHOD.  Process-wide. */
+SGT_API int sgt_eig_method(int method);
 
 /* hi = TF32 rounding of x (round to nearest, ties away), lo = x - hi (lo may be NULL). */
 SGT_API int sgt_split_tf32(const float* x, float* hi, float* lo, int64_t n, void* stream);

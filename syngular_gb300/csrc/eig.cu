@@ -396,29 +396,34 @@ int sym_eig_f32(cudaStream_t st, const float* Z, int64_t ldz, int64_t n, float* 
 
 namespace sgt {
 size_t jacobi_rows_ws_bytes_f32(int64_t n, int64_t m);
-int jacobi_rows_f32(cudaStream_t st, float* G, int64_t ldg, int64_t n, int64_t m, float* Vt, int64_t ldv,
-                    float* s, int* status, Arena& ar);
+size_t sym_eig_rows_ws_bytes(int64_t n);
+int sym_eig_rows_f32(cudaStream_t st, float* Z, int64_t n, float* Vt, float* lam, int* status, Arena& ar,
+                     int method);
 }  // namespace sgt
 
 extern "C" SGT_API size_t sgt_sym_eig_f32_workspace_size(int64_t n) {
-  return sgt::sym_eig_ws_bytes(n) + sgt::jacobi_rows_ws_bytes_f32(n, n) + 256 * 4 + sizeof(float) * n * n;
+  return std::max(sgt::sym_eig_ws_bytes(n) + sgt::jacobi_rows_ws_bytes_f32(n, n) + 256 * 4 + sizeof(float) * n * n,
+                  sgt::sym_eig_rows_ws_bytes(n));
 }
 
 // Eigen-decomposition of a symmetric positive semi-definite FP32 matrix Z
 // (n x n, row-major; Z is overwritten): Vt rows = eigenvectors, lam descending.
 // method 0: two-sided block Jacobi in one cluster (falls back to 1 when n does
-// not fit); method 1: one-sided Jacobi on the rows of Z.
+// not fit); method 1: one-sided Jacobi on the rows of Z; method 2: Jacobi on
+// the rows of Z's diagonal-ordered Cholesky factor (vectors by normalisation);
+// method 3: method 2 refined by accumulated Jacobi on the rows of V^T Z.
 extern "C" SGT_API int sgt_sym_eig_f32(float* Z, int64_t n, float* Vt, float* lam, int* status, int method,
                                        void* ws, size_t ws_bytes, void* stream) {
   using namespace sgt;
   SGT_REQUIRE(Z && Vt && lam && n > 0, SGT_ERR_INVALID, "sym_eig: bad argument");
+  SGT_REQUIRE(method >= 0 && method <= 3, SGT_ERR_INVALID, "sym_eig: method must be 0..3");
   cudaStream_t st = as_stream(stream);
   Arena ar(ws, ws_bytes);
   bool done = false;
   if (method == 0) SGT_TRY(sym_eig_f32(st, Z, n, n, Vt, n, lam, status, ar, &done));
   if (!done) {
     Arena a2(ws, ws_bytes);
-    SGT_TRY(jacobi_rows_f32(st, Z, n, n, n, Vt, n, lam, status, a2));
+    SGT_TRY(sym_eig_rows_f32(st, Z, n, Vt, lam, status, a2, method));
   }
   return SGT_OK;
 }

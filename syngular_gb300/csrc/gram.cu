@@ -116,6 +116,139 @@ __global__ void transpose_split_f64_kernel(const double* __restrict__ src, int64
   }
 }
 
+// Register-tiled form of steps B and C for middle sites (D2 = D, dout = d,
+// D a multiple of 8), compile-time sizes.  Both steps are small GEMMs with
+// K = 32-ish and a fixed W operand in shared memory:
+//   B: rows (a, b, c') x K (e, j)  -> cols (o, e')   [U = T1 W]
+//   C: rows (a, e', c') x K (b, o) -> cols (i, b')   [T3 = U W']
+// A thread owns 8 rows (the 8 values of c' of the tile, contiguous in shared
+// memory: two 16-byte loads per K step) x 8 columns (one 16-byte pair of W),
+// so every 4 shared loads feed 64 FMAs.  U is laid out [a][e'][b][o][c'] for
+// step C's row access; step C's tile is staged [c'][e'][b'][a][i] in the T1
+// buffer and stored as 32-byte runs (a, i) with the TF32 hi/lo split.
+constexpr int GT_TA = 4, GT_TC = 8, GT_THREADS = 256;
+
+template <int D, int d>
+__global__ void __launch_bounds__(GT_THREADS) gram_mid_tiled_kernel(const float* __restrict__ T1,
+                                                                    const double* __restrict__ W,
+                                                                    float* __restrict__ T3h, float* __restrict__ T3l,
+                                                                    int chi, int chi2) {
+  constexpr int K = D * d;               // (e, j) and (b, o) extents
+  constexpr int NB = d * D;              // (o, e') and (i, b') extents
+  constexpr int TROWS = GT_TA * D * K;   // T1 tile rows of 8 c' values: [a][b][e][j]
+  extern __shared__ __align__(16) float gt_smem[];
+  float* sWB = gt_smem;                  // [(e, j)][(o, e')] = W[e][j][o][e']
+  float* sWC = sWB + K * NB;             // [(b, o)][(i, b')] = W[b][i][o][b']
+  float* sT = sWC + K * NB;              // [a][b][e][j][c'], later the output stage
+  float* sU = sT + TROWS * GT_TC;        // [a][e'][b][o][c']
+  const int a0 = blockIdx.x * GT_TA, c0 = blockIdx.y * GT_TC;
+  const int tid = threadIdx.x;
+  for (int idx = tid; idx < K * NB; idx += GT_THREADS) {
+    // idx = ((b * d + i) * d + o) * D + b2 in W's own order
+    const int b2 = idx % D, o = (idx / D) % d, i = (idx / (D * d)) % d, b = idx / (D * d * d);
+    const float w = (float)W[idx];
+    sWB[idx] = w;                                          // [(b, i)][(o, b2)]
+    sWC[(b * d + o) * NB + i * D + b2] = w;                // [(b, o)][(i, b2)]
+  }
+  const bool full_c = (c0 + GT_TC <= chi2) && (chi2 % 4 == 0);
+  for (int idx = tid; idx < TROWS * (GT_TC / 4); idx += GT_THREADS) {
+    const int r = idx / (GT_TC / 4), q = idx % (GT_TC / 4);
+    const int at = r / (D * K), a = a0 + at;
+    float4 v = make_float4(0.f, 0.f, 0.f, 0.f);
+    if (a < chi) {
+      const float* src = T1 + ((int64_t)a * (D * K) + (r % (D * K))) * chi2 + c0 + 4 * q;
+      if (full_c) {
+        v = *reinterpret_cast<const float4*>(src);
+      } else {
+        float t[4];
+        for (int u = 0; u < 4; ++u) t[u] = (c0 + 4 * q + u < chi2) ? src[u] : 0.f;
+        v = make_float4(t[0], t[1], t[2], t[3]);
+      }
+    }
+    reinterpret_cast<float4*>(sT)[idx] = v;
+  }
+  __syncthreads();
+  // ---- B: U[a][e'][b][o][c'] = sum_(e,j) T1[a][b][(e,j)][c'] W[(e,j)][(o,e')] ----
+  for (int task = tid; task < GT_TA * D * (NB / 8); task += GT_THREADS) {
+    const int cg = task % (NB / 8), rg = task / (NB / 8);  // rg = at * D + b
+    const int at = rg / D, b = rg % D;
+    const int n0 = cg * 8, o = n0 / D, e0 = n0 % D;
+    float acc[8][8];
+#pragma unroll
+    for (int t = 0; t < 8; ++t)
+#pragma unroll
+      for (int n = 0; n < 8; ++n) acc[t][n] = 0.f;
+    const float* arow = sT + (int64_t)rg * K * GT_TC;
+#pragma unroll 4
+    for (int k = 0; k < K; ++k) {
+      const float4 x0 = *reinterpret_cast<const float4*>(arow + k * GT_TC);
+      const float4 x1 = *reinterpret_cast<const float4*>(arow + k * GT_TC + 4);
+      const float4 w0 = *reinterpret_cast<const float4*>(sWB + k * NB + n0);
+      const float4 w1 = *reinterpret_cast<const float4*>(sWB + k * NB + n0 + 4);
+      const float xa[8] = {x0.x, x0.y, x0.z, x0.w, x1.x, x1.y, x1.z, x1.w};
+      const float wb[8] = {w0.x, w0.y, w0.z, w0.w, w1.x, w1.y, w1.z, w1.w};
+#pragma unroll
+      for (int t = 0; t < 8; ++t)
+#pragma unroll
+        for (int n = 0; n < 8; ++n) acc[t][n] = fmaf(xa[t], wb[n], acc[t][n]);
+    }
+#pragma unroll
+    for (int n = 0; n < 8; ++n) {
+      float* dst = sU + ((((int64_t)at * D + e0 + n) * D + b) * d + o) * GT_TC;
+      reinterpret_cast<float4*>(dst)[0] = make_float4(acc[0][n], acc[1][n], acc[2][n], acc[3][n]);
+      reinterpret_cast<float4*>(dst)[1] = make_float4(acc[4][n], acc[5][n], acc[6][n], acc[7][n]);
+    }
+  }
+  __syncthreads();
+  // ---- C: stage[c'][e'][b'][a][i] = sum_(b,o) U[a][e'][(b,o)][c'] W'[(b,o)][(i,b')] ----
+  float* stage = sT;
+  for (int task = tid; task < GT_TA * D * (NB / 8); task += GT_THREADS) {
+    const int cg = task % (NB / 8), rg = task / (NB / 8);  // rg = at * D + e'
+    const int at = rg / D, e2 = rg % D;
+    const int n0 = cg * 8, i = n0 / D, b20 = n0 % D;
+    float acc[8][8];
+#pragma unroll
+    for (int t = 0; t < 8; ++t)
+#pragma unroll
+      for (int n = 0; n < 8; ++n) acc[t][n] = 0.f;
+    const float* arow = sU + (int64_t)rg * K * GT_TC;
+#pragma unroll 4
+    for (int k = 0; k < K; ++k) {
+      const float4 x0 = *reinterpret_cast<const float4*>(arow + k * GT_TC);
+      const float4 x1 = *reinterpret_cast<const float4*>(arow + k * GT_TC + 4);
+      const float4 w0 = *reinterpret_cast<const float4*>(sWC + k * NB + n0);
+      const float4 w1 = *reinterpret_cast<const float4*>(sWC + k * NB + n0 + 4);
+      const float xa[8] = {x0.x, x0.y, x0.z, x0.w, x1.x, x1.y, x1.z, x1.w};
+      const float wb[8] = {w0.x, w0.y, w0.z, w0.w, w1.x, w1.y, w1.z, w1.w};
+#pragma unroll
+      for (int t = 0; t < 8; ++t)
+#pragma unroll
+        for (int n = 0; n < 8; ++n) acc[t][n] = fmaf(xa[t], wb[n], acc[t][n]);
+    }
+#pragma unroll
+    for (int t = 0; t < 8; ++t)
+#pragma unroll
+      for (int n = 0; n < 8; ++n)
+        stage[(((int64_t)(t * D + e2) * D + b20 + n) * GT_TA + at) * d + i] = acc[t][n];
+  }
+  __syncthreads();
+  // ---- store: runs of GT_TA * d values (a, i) per (c', e', b') ----
+  constexpr int RUN = GT_TA * d;
+  for (int idx = tid; idx < GT_TC * D * D * RUN; idx += GT_THREADS) {
+    const int ai = idx % RUN, rest = idx / RUN;  // rest = (t * D + e2) * D + b2
+    const int t = rest / (D * D);
+    const int at = ai / d, a = a0 + at, c = c0 + t;
+    if (a >= chi || c >= chi2) continue;
+    const int64_t g = ((int64_t)c * D * D + rest % (D * D)) * ((int64_t)chi * d) + (int64_t)a0 * d + ai;
+    split_store(stage[idx], T3h, T3l, g);
+  }
+}
+
+template <int D, int d>
+size_t tiled_smem_bytes() {
+  return sizeof(float) * (2 * (size_t)(D * d) * (d * D) + 2 * (size_t)GT_TA * D * (D * d) * GT_TC);
+}
+
 size_t mid_smem_bytes(int D, int d, int dout, int D2, int TC) {
   return sizeof(float) * ((size_t)D * d * dout * D2 + (size_t)GM_TA * D * D * d * TC +
                           (size_t)GM_TA * D * dout * D2 * TC);
@@ -160,6 +293,29 @@ int gram_step_structured(cudaStream_t st, int passes, const float* Gh, const flo
   SGT_TRY(gemm_nt_dispatch(st, passes, chi * D * D, d * chi2, chi, 1.f, Gh, Gl, chi, Xth, Xtl, chi, 0.f, T1,
                            d * chi2, err));
   // B + C
+  if (D2 == D && dout == d) {
+    bool done = false;
+    dim3 gt((unsigned)cdiv(chi, GT_TA), (unsigned)cdiv(chi2, GT_TC));
+    auto run = [&](auto kern, size_t smem) -> int {
+      if (smem > 200 * 1024) return SGT_OK;  // the generic kernel below takes it
+      SGT_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+      kern<<<gt, GT_THREADS, smem, st>>>(T1, W, T3h, T3l, (int)chi, (int)chi2);
+      SGT_LAUNCHED();
+      done = true;
+      return SGT_OK;
+    };
+    if (D == 16 && d == 2) SGT_TRY(run(gram_mid_tiled_kernel<16, 2>, tiled_smem_bytes<16, 2>()));
+    else if (D == 16 && d == 4) SGT_TRY(run(gram_mid_tiled_kernel<16, 4>, tiled_smem_bytes<16, 4>()));
+    else if (D == 8 && d == 2) SGT_TRY(run(gram_mid_tiled_kernel<8, 2>, tiled_smem_bytes<8, 2>()));
+    else if (D == 8 && d == 3) SGT_TRY(run(gram_mid_tiled_kernel<8, 3>, tiled_smem_bytes<8, 3>()));
+    else if (D == 8 && d == 4) SGT_TRY(run(gram_mid_tiled_kernel<8, 4>, tiled_smem_bytes<8, 4>()));
+    else if (D == 16 && d == 3) SGT_TRY(run(gram_mid_tiled_kernel<16, 3>, tiled_smem_bytes<16, 3>()));
+    if (done) {
+      SGT_TRY(gemm_nt_dispatch(st, passes, chi2 * D2 * D2, chi2, chi * d, 1.f, T3h, T3l, chi * d, X2h, X2l,
+                               chi * d, 0.f, Gout, chi2, err));
+      return SGT_OK;
+    }
+  }
   int TC = 8;
   while (TC > 1 && mid_smem_bytes((int)D, (int)d, (int)dout, (int)D2, TC) > 160 * 1024) TC /= 2;
   const size_t smem = mid_smem_bytes((int)D, (int)d, (int)dout, (int)D2, TC);

@@ -21,6 +21,8 @@
 #include <float.h>
 
 #include <algorithm>
+#include <atomic>
+#include <cstdlib>
 #include <vector>
 
 #include "common.cuh"
@@ -41,6 +43,9 @@ int split_tf32(cudaStream_t st, const float* x, float* hi, float* lo, int64_t n)
 int split_f64(cudaStream_t st, const double* x, int64_t ldx, float* hi, float* lo, int64_t rows,
               int64_t cols);
 size_t jacobi_rows_ws_bytes_f32(int64_t n, int64_t m);
+size_t sym_eig_rows_ws_bytes(int64_t n);
+int sym_eig_rows_f32(cudaStream_t st, float* Z, int64_t n, float* Vt, float* lam, int* status, Arena& ar,
+                     int method);
 int jacobi_rows_f32(cudaStream_t st, float* G, int64_t ldg, int64_t n, int64_t m, float* Vt,
                     int64_t ldv, float* s, int* status, Arena& ar);
 size_t sym_eig_ws_bytes(int64_t n);
@@ -212,6 +217,23 @@ __global__ void merge_status_kernel(const int* __restrict__ st, int n, int* __re
   *out = r;
 }
 
+// Eigensolver of the projected Gram matrices (sgt_sym_eig_f32 methods 1-3):
+// SGT_EIG_METHOD in the environment sets the initial choice, sgt_eig_method()
+// changes it.
+std::atomic<int> g_eig_method{0};
+
+int eig_method() {
+  int m = g_eig_method.load(std::memory_order_relaxed);
+  if (m == 0) {
+    const char* e = getenv("SGT_EIG_METHOD");
+    const int v = e ? atoi(e) : 1;
+    m = (v >= 1 && v <= 3) ? v : 1;
+    int expected = 0;
+    if (!g_eig_method.compare_exchange_strong(expected, m)) m = expected;
+  }
+  return m;
+}
+
 inline unsigned gs(int64_t n) {
   return (unsigned)std::max<int64_t>(1, std::min<int64_t>(cdiv(n, 256), 152 * 16));
 }
@@ -323,7 +345,8 @@ static int mixed_round_impl(cudaStream_t st, int n, const double* const* W, cons
   double* Sd = ar.take<double>(chi * chi);
   int* stat = ar.take<int>(n + 1);
   int* tc_err = ar.take<int>(1);
-  const size_t jbytes = std::max(jacobi_rows_ws_bytes_f32(cmax, cmax), sym_eig_ws_bytes(cmax));
+  const size_t jbytes = std::max(std::max(jacobi_rows_ws_bytes_f32(cmax, cmax), sym_eig_ws_bytes(cmax)),
+                                 sym_eig_rows_ws_bytes(cmax));
   char* jscratch = ar.take<char>(jbytes);
   if (ar.measure) return SGT_OK;
   SGT_REQUIRE(ar.ok(), SGT_ERR_WORKSPACE, "mpo_mps_round: workspace too small");
@@ -403,7 +426,7 @@ static int mixed_round_impl(cudaStream_t st, int n, const double* const* W, cons
     // cluster-resident).  The two-sided solver (eig.cu) converges in fewer
     // sweeps but its FP32 stopping floor costs accuracy next to the cut.
     Arena ja(jscratch, jbytes);
-    SGT_TRY(jacobi_rows_f32(st, Z, c, c, c, Vt, c, lam, stat + k, ja));
+    SGT_TRY(sym_eig_rows_f32(st, Z, c, Vt, lam, stat + k, ja, eig_method()));
     // core_k = Vt[:keep], re-orthonormalised in FP64 by one Newton-Schulz step
     // V <- 1.5 V - 0.5 (V V^T) V (the FP32 rotations leave |V V^T - I| ~ 1e-6)
     f32_to_f64_kernel<<<gs(keep * c), 256, 0, st>>>(Vt, c, Vd, c, keep, c);
@@ -497,3 +520,9 @@ SGT_API int sgt_mpo_mps_round(int n, const double* const* W, const int64_t* wsha
 }
 
 }  // extern "C"
+
+extern "C" SGT_API int sgt_eig_method(int method) {
+  const int prev = sgt::eig_method();
+  if (method >= 1 && method <= 3) sgt::g_eig_method.store(method, std::memory_order_relaxed);
+  return prev;
+}

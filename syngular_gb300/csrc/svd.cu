@@ -408,6 +408,481 @@ __global__ void __launch_bounds__(BJ_THREADS) bjacobi_kernel(T* __restrict__ G, 
   cluster.sync();
 }
 
+// ---------------------------------------------------------------------------
+// Gram-form block Jacobi (FP32).  Same cluster layout and circle of blocks as
+// bjacobi_kernel (Vt rows always in shared memory, bs <= 16), but an outer step
+// touches the 2*bs working rows [G | Vt] only twice instead of once per pair:
+//   1. C = G_w G_w^T, the Gram matrix of the working rows (W x W, W = 32 with
+//      zero padding): warp w owns an 8x8 tile, lanes stride the row length and
+//      a 5-step shuffle reduce-scatter leaves two sums per lane;
+//   2. one round-robin sweep of two-sided rotations C <- R C R^T on the small
+//      matrix (double-buffered, one barrier per sub-step; warp i holds pair i,
+//      lane j the 2x2 block (i, j); lanes 16..31 rotate rows of Q = prod R);
+//   3. [G | Vt]_w <- Q [G | Vt]_w, skipped when no pair rotated.
+// The angles are those of the row-pair form (same criterion, same Rutishauser
+// update) computed from the tracked Gram entries, so the sweep count and the
+// stopping floor are unchanged; shared-memory traffic per step drops from
+// O(W^2 (m + n)) to O(W (m + n)).
+//
+// MODE 0: rows of G, Vt = I.  MODE 1: rows of G, Vt rows loaded from Vt (a
+// refinement of approximate eigenvectors).  MODE 2 (G = a symmetric positive
+// semi-definite Z, m = n): the rows and columns of Z are gathered in the order
+// perm (decreasing diagonal), factored in place as Z_perm = R^T R by a blocked
+// row-oriented Cholesky across the cluster (the owner of block J factors its
+// rows, every CTA applies the rank-bs update of its later rows from a DSMEM
+// copy of R's block row) after a diagonal shift delta = 2 n eps max(diag)
+// that makes the FP32 factorisation stable for rank-deficient Z; then the
+// rows of R are orthogonalised without Vt (rows of J R = s_j u_j^T, u_j the
+// eigenvectors of Z_perm, s_j^2 = lam_j + delta).  On exit G rows are
+// lam_j u_j^T and Vt rows u_j^T, both in the original column order, and
+// norms = lam_j.  Jacobi on the pivoted Cholesky factor needs
+// about half the sweeps of Jacobi on Z (its rows are graded and nearly
+// orthogonal from the start); its vectors come from normalisation, so MODE 1
+// can follow to restore accumulated-rotation accuracy.
+constexpr int GJ_W = 32;
+
+template <int MODE>
+__global__ void __launch_bounds__(BJ_THREADS) gjacobi_kernel(float* __restrict__ G, int64_t ldg,
+                                                             float* __restrict__ Vt, int64_t ldv, int n, int m,
+                                                             int bs, double tol, float* __restrict__ norms,
+                                                             int* __restrict__ status,
+                                                             const int* __restrict__ perm) {
+  cg::cluster_group cluster = cg::this_cluster();
+  const int cs = (int)cluster.num_blocks();
+  const int rank = (int)cluster.block_rank();
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const int nblk = 2 * cs;
+  const int row_len = (MODE == 2) ? m : m + n;  // G part then Vt part
+  const int slot_elems = bs * row_len;
+  const int weff = 2 * bs;    // working rows (<= GJ_W)
+
+  extern __shared__ __align__(16) unsigned char gj_raw[];
+  float* slots = reinterpret_cast<float*>(gj_raw);  // [2][bs][row_len]
+  float* stage = slots + 2 * slot_elems;            // [bs][row_len]
+  __shared__ __align__(16) float sC[2][GJ_W][GJ_W];
+  __shared__ __align__(16) float sQ[GJ_W][GJ_W];
+  __shared__ int s_off[GJ_W];
+  __shared__ int s_blk[2];
+  __shared__ int s_rot[2];
+  __shared__ int s_any;
+  __shared__ double s_norm;
+  __shared__ double s_red[BJ_WARPS];
+
+  auto pos_owner = [&](int q, int& cta, int& slot) {
+    if (q < cs) {
+      cta = q;
+      slot = 0;
+    } else {
+      cta = nblk - 1 - q;
+      slot = 1;
+    }
+  };
+  auto slot_pos = [&](int c, int slot) { return slot == 0 ? c : nblk - 1 - c; };
+
+  if (tid < GJ_W) s_off[tid] = (tid < weff) ? (tid / bs) * slot_elems + (tid % bs) * row_len : -1;
+  for (int sl = 0; sl < 2; ++sl) {
+    const int blk = slot_pos(rank, sl);
+    if (tid == 0) s_blk[sl] = blk;
+    for (int64_t i = tid; i < slot_elems; i += BJ_THREADS) {
+      const int r = (int)(i / row_len), e = (int)(i % row_len);
+      const int gr = blk * bs + r;
+      float v = 0.f;
+      if (gr < n) {
+        if (MODE == 2) v = G[(int64_t)perm[gr] * ldg + perm[e]];
+        else if (e < m) v = G[(int64_t)gr * ldg + e];
+        else if (MODE == 1) v = Vt[(int64_t)gr * ldv + (e - m)];
+        else v = ((e - m) == gr) ? 1.f : 0.f;
+      }
+      slots[(int64_t)sl * slot_elems + i] = v;
+    }
+  }
+  float shift = 0.f;
+  if constexpr (MODE == 2) {
+    // ---- largest diagonal entry over the cluster -> shift and pivot floor ----
+    float mx = 0.f;
+    for (int sl = 0; sl < 2; ++sl)
+      for (int r = tid; r < bs; r += BJ_THREADS) {
+        const int gr = slot_pos(rank, sl) * bs + r;
+        if (gr < n) mx = fmaxf(mx, slots[(int64_t)sl * slot_elems + (int64_t)r * row_len + gr]);
+      }
+    for (int o = 16; o > 0; o >>= 1) mx = fmaxf(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+    if (lane == 0) s_red[warp] = (double)mx;
+    __syncthreads();
+    if (tid == 0) {
+      double t = 0.0;
+      for (int w = 0; w < BJ_WARPS; ++w) t = fmax(t, s_red[w]);
+      s_norm = t;
+    }
+    cluster.sync();
+    if (tid == 0) {
+      double t = 0.0;
+      for (int r = 0; r < cs; ++r) t = fmax(t, *cluster.map_shared_rank(&s_norm, r));
+      s_red[0] = t;
+    }
+    __syncthreads();
+    const float dfloor = fmaxf(FLT_EPSILON * (float)s_red[0], FLT_MIN);
+    // Z + delta I has the eigenvectors of Z and a condition number below
+    // 1 / (2 n eps), so its Cholesky factor is stable in FP32 even when Z is
+    // numerically rank deficient (static pivoting alone is not: a pivot that
+    // is rounding noise can carry off-diagonal entries of the size of the
+    // matrix).  delta is removed from the eigenvalues on exit.
+    shift = 2.f * (float)n * FLT_EPSILON * (float)s_red[0];
+    for (int sl = 0; sl < 2; ++sl)
+      for (int r = tid; r < bs; r += BJ_THREADS) {
+        const int gr = slot_pos(rank, sl) * bs + r;
+        if (gr < n) slots[(int64_t)sl * slot_elems + (int64_t)r * row_len + gr] += shift;
+      }
+    cluster.sync();  // s_norm / s_red are reused below
+    // ---- blocked row-oriented Cholesky, Z_perm = R^T R ----
+    float* coefT = &sQ[0][0];  // [2 bs][16]: R_J[i][K] for the CTA's own rows K
+    for (int J = 0; J < nblk; ++J) {
+      const int j0 = J * bs;
+      if (j0 >= n) break;
+      int ocs, osl;
+      pos_owner(J, ocs, osl);
+      const int jrows = min(bs, n - j0);
+      if (rank == ocs) {
+        float* blk = slots + (int64_t)osl * slot_elems;
+        for (int r = 0; r < jrows; ++r) {
+          const int gi = j0 + r;
+          float* row = blk + (int64_t)r * row_len;
+          __syncthreads();
+          float d = row[gi];
+          if (!(d > dfloor)) d = dfloor;
+          const float sd = sqrtf(d), inv = 1.f / sd;
+          __syncthreads();
+          for (int e = tid; e < n; e += BJ_THREADS) row[e] = (e < gi) ? 0.f : (e == gi ? sd : row[e] * inv);
+          __syncthreads();
+          const int rem = jrows - r - 1;
+          for (int idx = tid; idx < rem * n; idx += BJ_THREADS) {
+            const int r2 = r + 1 + idx / n, e = idx % n;
+            const int g2 = j0 + r2;
+            if (e >= g2) blk[(int64_t)r2 * row_len + e] -= row[g2] * row[e];
+          }
+        }
+      }
+      cluster.sync();
+      const int c0 = j0 + bs;
+      if (c0 < n) {
+        const float* src = cluster.map_shared_rank(slots, ocs) + (int64_t)osl * slot_elems;
+        const int w = n - c0;
+        for (int idx = tid; idx < bs * w; idx += BJ_THREADS) {
+          const int i = idx / w, e = c0 + idx % w;
+          stage[(int64_t)i * row_len + e] = (i < jrows) ? src[(int64_t)i * row_len + e] : 0.f;
+        }
+        __syncthreads();
+        for (int idx = tid; idx < 2 * bs * 16; idx += BJ_THREADS) {
+          const int lr = idx / 16, i = idx % 16;
+          const int sl = lr / bs, r = lr % bs;
+          const int B = slot_pos(rank, sl), K = B * bs + r;
+          coefT[idx] = (i < bs && B > J && K < n) ? stage[(int64_t)i * row_len + K] : 0.f;
+        }
+        __syncthreads();
+        for (int e = c0 + tid; e < n; e += BJ_THREADS) {
+          float x[16];
+#pragma unroll
+          for (int i = 0; i < 16; ++i) x[i] = (i < bs) ? stage[(int64_t)i * row_len + e] : 0.f;
+          for (int lr = 0; lr < 2 * bs; ++lr) {
+            const int sl = lr / bs, r = lr % bs;
+            if (slot_pos(rank, sl) <= J) continue;
+            const float4* c4 = reinterpret_cast<const float4*>(coefT + lr * 16);
+            float acc = 0.f;
+#pragma unroll
+            for (int q = 0; q < 4; ++q) {
+              const float4 c = c4[q];
+              acc = fmaf(c.x, x[4 * q], acc);
+              acc = fmaf(c.y, x[4 * q + 1], acc);
+              acc = fmaf(c.z, x[4 * q + 2], acc);
+              acc = fmaf(c.w, x[4 * q + 3], acc);
+            }
+            slots[(int64_t)sl * slot_elems + (int64_t)r * row_len + e] -= acc;
+          }
+        }
+        __syncthreads();
+      }
+    }
+    cluster.sync();
+  }
+  // |G|_F^2 over the cluster -> floor m (eps |G|_F)^2 on |g_p . g_q|
+  {
+    double acc = 0.0;
+    for (int64_t i = tid; i < 2 * (int64_t)slot_elems; i += BJ_THREADS) {
+      const int e = (int)(i % row_len);
+      if (e < m) {
+        const double v = (double)slots[i];
+        acc += v * v;
+      }
+    }
+    for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+    if (lane == 0) s_red[warp] = acc;
+    if (tid < 2) s_rot[tid] = 0;
+    __syncthreads();
+    if (tid == 0) {
+      double t = 0.0;
+      for (int w = 0; w < BJ_WARPS; ++w) t += s_red[w];
+      s_norm = t;
+    }
+    cluster.sync();
+    if (tid == 0) {
+      double t = 0.0;
+      for (int r = 0; r < cs; ++r) t += *cluster.map_shared_rank(&s_norm, r);
+      s_red[0] = t;
+    }
+    __syncthreads();
+    const double fl = 1.1920928955078125e-07 * sqrt(s_red[0]);
+    cluster.sync();
+    if (tid == 0) s_norm = (double)m * fl * fl;
+    __syncthreads();
+  }
+  const float abs_floor = (float)s_norm;
+  const float ftol = (float)tol;
+
+  // Gram tile of this warp and the rows it reads
+  const int ti = warp >> 2, tj = warp & 3;
+  int offi[8], offj[8];
+#pragma unroll
+  for (int a = 0; a < 8; ++a) {
+    offi[a] = s_off[8 * ti + a];
+    offj[a] = s_off[8 * tj + a];
+  }
+
+  int sweeps = 0;
+  bool converged = (n < 2);
+  int my_rot = 0;
+  while (!converged && sweeps < JAC_MAX_SWEEPS) {
+    const int par = sweeps & 1;
+    for (int step = 0; step < nblk - 1; ++step) {
+      // ---- 1. Gram matrix of the working rows ----
+      {
+        float v[64];
+#pragma unroll
+        for (int k = 0; k < 64; ++k) v[k] = 0.f;
+        for (int e = lane; e < m; e += 32) {
+          float xi[8], xj[8];
+#pragma unroll
+          for (int a = 0; a < 8; ++a) {
+            xi[a] = offi[a] >= 0 ? slots[offi[a] + e] : 0.f;
+            xj[a] = offj[a] >= 0 ? slots[offj[a] + e] : 0.f;
+          }
+#pragma unroll
+          for (int a = 0; a < 8; ++a)
+#pragma unroll
+            for (int b = 0; b < 8; ++b) v[a * 8 + b] = fmaf(xi[a], xj[b], v[a * 8 + b]);
+        }
+        // reduce-scatter over the 32 lanes: lane L ends with entries 2L, 2L+1
+#pragma unroll
+        for (int h = 32, o = 16; o > 0; h >>= 1, o >>= 1) {
+          const bool up = (lane & o) != 0;
+#pragma unroll
+          for (int k = 0; k < h; ++k) {
+            const float send = up ? v[k] : v[k + h];
+            const float keep = up ? v[k + h] : v[k];
+            v[k] = keep + __shfl_xor_sync(0xffffffffu, send, o);
+          }
+        }
+        const int a = lane >> 2, b = 2 * (lane & 3);
+        sC[0][8 * ti + a][8 * tj + b] = v[0];
+        sC[0][8 * ti + a][8 * tj + b + 1] = v[1];
+      }
+      for (int i = tid; i < GJ_W * GJ_W; i += BJ_THREADS) sQ[i / GJ_W][i % GJ_W] = (i / GJ_W == i % GJ_W) ? 1.f : 0.f;
+      if (tid == 0) s_any = 0;
+      __syncthreads();
+
+      // ---- 2. one sweep of two-sided rotations on C, accumulated in Q ----
+      int cur = 0;
+      for (int sub = 0; sub < weff - 1; ++sub) {
+        if (warp < bs) {
+          const int i = warp;
+          const int pi = rr_index(i, sub, weff), qi = rr_index(weff - 1 - i, sub, weff);
+          // lane j < bs: the rotation of pair j
+          float cj = 1.f, sj = 0.f, tj_ = 0.f, tanj = 0.f;
+          int rj = 0, pj = 0, qj = 0;
+          if (lane < bs) {
+            pj = rr_index(lane, sub, weff);
+            qj = rr_index(weff - 1 - lane, sub, weff);
+            const float a = fmaxf(sC[cur][pj][pj], 0.f), b = fmaxf(sC[cur][qj][qj], 0.f), c = sC[cur][pj][qj];
+            float c_, s_, t_;
+            if (jacobi_rotation<float>(a, b, c, (double)ftol, (double)abs_floor, lane, c_, s_, t_)) {
+              rj = 1;
+              cj = c_;
+              sj = s_;
+              tj_ = t_;
+              tanj = s_ / c_;
+            }
+          }
+          const int ri = __shfl_sync(0xffffffffu, rj, i);
+          const float ci = __shfl_sync(0xffffffffu, cj, i), si = __shfl_sync(0xffffffffu, sj, i);
+          const float taui = __shfl_sync(0xffffffffu, tj_, i), tani = __shfl_sync(0xffffffffu, tanj, i);
+          const int nxt = cur ^ 1;
+          if (lane < bs) {
+            float xpp = sC[cur][pi][pj], xpq = sC[cur][pi][qj], xqp = sC[cur][qi][pj], xqq = sC[cur][qi][qj];
+            if (lane == i) {
+              if (ri) {
+                ++my_rot;
+                s_any = 1;
+                const float c = xpq;
+                xpp = xpp - tani * c;
+                xqq = xqq + tani * c;
+                xpq = 0.f;
+                xqp = 0.f;
+              }
+            } else {
+              if (ri) {  // rows p_i, q_i
+                const float a0 = xpp - si * (xqp + taui * xpp), b0 = xqp + si * (xpp - taui * xqp);
+                const float a1 = xpq - si * (xqq + taui * xpq), b1 = xqq + si * (xpq - taui * xqq);
+                xpp = a0;
+                xqp = b0;
+                xpq = a1;
+                xqq = b1;
+              }
+              if (rj) {  // columns p_j, q_j
+                const float a0 = xpp - sj * (xpq + tj_ * xpp), b0 = xpq + sj * (xpp - tj_ * xpq);
+                const float a1 = xqp - sj * (xqq + tj_ * xqp), b1 = xqq + sj * (xqp - tj_ * xqq);
+                xpp = a0;
+                xpq = b0;
+                xqp = a1;
+                xqq = b1;
+              }
+            }
+            sC[nxt][pi][pj] = xpp;
+            sC[nxt][pi][qj] = xpq;
+            sC[nxt][qi][pj] = xqp;
+            sC[nxt][qi][qj] = xqq;
+          } else if (lane >= 16 && ri) {
+            // rows p_i, q_i of Q, columns u and u + 16
+#pragma unroll
+            for (int h = 0; h < 2; ++h) {
+              const int e = (lane - 16) + 16 * h;
+              if (e < weff) {
+                const float x = sQ[pi][e], y = sQ[qi][e];
+                sQ[pi][e] = x - si * (y + taui * x);
+                sQ[qi][e] = y + si * (x - taui * y);
+              }
+            }
+          }
+        }
+        __syncthreads();
+        cur ^= 1;
+      }
+
+      // ---- 3. apply Q to the working rows ----
+      if (s_any) {
+        for (int e = tid; e < row_len; e += BJ_THREADS) {
+          float x[GJ_W];
+#pragma unroll
+          for (int j = 0; j < GJ_W; ++j) x[j] = (j < weff) ? slots[s_off[j] + e] : 0.f;
+#pragma unroll 4
+          for (int r = 0; r < weff; ++r) {
+            const float4* q4 = reinterpret_cast<const float4*>(&sQ[r][0]);
+            float acc = 0.f;
+#pragma unroll
+            for (int j4 = 0; j4 < GJ_W / 4; ++j4) {
+              const float4 q = q4[j4];
+              acc = fmaf(q.x, x[4 * j4], acc);
+              acc = fmaf(q.y, x[4 * j4 + 1], acc);
+              acc = fmaf(q.z, x[4 * j4 + 2], acc);
+              acc = fmaf(q.w, x[4 * j4 + 3], acc);
+            }
+            slots[s_off[r] + e] = acc;
+          }
+        }
+      }
+
+      // ---- 4. move blocks one position along the circle ----
+      int src_cta[2], src_slot[2];
+      for (int sl = 0; sl < 2; ++sl) {
+        const int q = slot_pos(rank, sl);
+        const int qs = (q == 0) ? 0 : (q == 1 ? nblk - 1 : q - 1);
+        pos_owner(qs, src_cta[sl], src_slot[sl]);
+      }
+      cluster.sync();
+      const float* r0 = cluster.map_shared_rank(slots, src_cta[0]) + (int64_t)src_slot[0] * slot_elems;
+      const float* r1 = cluster.map_shared_rank(slots, src_cta[1]) + (int64_t)src_slot[1] * slot_elems;
+      const int nb0 = *cluster.map_shared_rank(&s_blk[src_slot[0]], src_cta[0]);
+      const int nb1 = *cluster.map_shared_rank(&s_blk[src_slot[1]], src_cta[1]);
+      const int n4 = slot_elems * (int)sizeof(float) / 16;
+      const uint4* s0 = reinterpret_cast<const uint4*>(r0);
+      const uint4* s1 = reinterpret_cast<const uint4*>(r1);
+      uint4* st4 = reinterpret_cast<uint4*>(stage);
+      uint4 regs[BJ_MAX_SLOT_BYTES / 16 / BJ_THREADS];
+#pragma unroll
+      for (int j = 0; j < BJ_MAX_SLOT_BYTES / 16 / BJ_THREADS; ++j) {
+        const int idx = tid + j * BJ_THREADS;
+        if (idx < n4) {
+          st4[idx] = s0[idx];
+          regs[j] = s1[idx];
+        }
+      }
+      cluster.sync();
+      uint4* d0 = reinterpret_cast<uint4*>(slots);
+      uint4* d1 = reinterpret_cast<uint4*>(slots + slot_elems);
+#pragma unroll
+      for (int j = 0; j < BJ_MAX_SLOT_BYTES / 16 / BJ_THREADS; ++j) {
+        const int idx = tid + j * BJ_THREADS;
+        if (idx < n4) {
+          d0[idx] = st4[idx];
+          d1[idx] = regs[j];
+        }
+      }
+      if (tid == 0) {
+        s_blk[0] = nb0;
+        s_blk[1] = nb1;
+      }
+      __syncthreads();
+    }
+    if (my_rot) atomicAdd(&s_rot[par], my_rot);
+    my_rot = 0;
+    __syncthreads();
+    cluster.sync();
+    int total = 0;
+    for (int r = 0; r < cs; ++r) total += *cluster.map_shared_rank(&s_rot[par], r);
+    ++sweeps;
+    converged = (total == 0);
+    cluster.sync();
+    if (tid == 0) s_rot[par] = 0;
+  }
+  for (int sl = 0; sl < 2; ++sl) {
+    const int blk = s_blk[sl];
+    if (MODE == 2) {
+      for (int r = warp; r < bs; r += BJ_WARPS) {
+        const int gr = blk * bs + r;
+        if (gr >= n) continue;
+        const float* row = slots + (int64_t)sl * slot_elems + (int64_t)r * row_len;
+        float acc = 0.f;
+        for (int e = lane; e < m; e += 32) acc = fmaf(row[e], row[e], acc);
+        acc = wsum_t(acc);
+        const float sg = sqrtf(acc), inv = sg > 0.f ? 1.f / sg : 0.f;
+        const float lam = fmaxf(acc - shift, 0.f);
+        for (int e = lane; e < m; e += 32) {
+          G[(int64_t)gr * ldg + perm[e]] = row[e] * (lam * inv);
+          Vt[(int64_t)gr * ldv + perm[e]] = row[e] * inv;
+        }
+        if (lane == 0) norms[gr] = lam;
+      }
+      continue;
+    }
+    for (int64_t i = tid; i < slot_elems; i += BJ_THREADS) {
+      const int r = (int)(i / row_len), e = (int)(i % row_len);
+      const int gr = blk * bs + r;
+      if (gr >= n) continue;
+      const float v = slots[(int64_t)sl * slot_elems + i];
+      if (e < m) G[(int64_t)gr * ldg + e] = v;
+      else Vt[(int64_t)gr * ldv + (e - m)] = v;
+    }
+    for (int r = warp; r < bs; r += BJ_WARPS) {
+      const int gr = blk * bs + r;
+      if (gr >= n) continue;
+      const float* row = slots + (int64_t)sl * slot_elems + (int64_t)r * row_len;
+      float acc = 0.f;
+      for (int e = lane; e < m; e += 32) acc = fmaf(row[e], row[e], acc);
+      acc = wsum_t(acc);
+      if (lane == 0) norms[gr] = sqrtf(acc);
+    }
+  }
+  if (rank == 0 && tid == 0 && status) *status = converged ? sweeps : -1;
+  cluster.sync();
+}
+
 template <typename T>
 __global__ void eye_rows_kernel(T* Vt, int64_t ldv, int n) {
   for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < (int64_t)n * n;
@@ -477,6 +952,69 @@ size_t jacobi_rows_ws_bytes_t(int64_t n, int64_t m) {
 size_t jacobi_rows_ws_bytes(int64_t n, int64_t m) { return jacobi_rows_ws_bytes_t<double>(n, m); }
 size_t jacobi_rows_ws_bytes_f32(int64_t n, int64_t m) { return jacobi_rows_ws_bytes_t<float>(n, m); }
 
+// Launch gjacobi_kernel<MODE> when its cluster layout fits (n in [64, 512],
+// blocks of <= 16 rows, slots within the shared-memory budget and a cluster
+// of that size schedulable); *launched reports whether it was.
+template <int MODE>
+static int launch_gjacobi(cudaStream_t st, float* G, int64_t ldg, float* Vt, int64_t ldv, int64_t n, int64_t m,
+                          float* norms, int* status, const int* perm, bool* launched) {
+  *launched = false;
+  if (n < 64 || n > 16 * GJ_W || (MODE == 2 && m != n)) return SGT_OK;
+  int csb = 2;
+  while (csb < 16 && cdiv(n, 2 * csb) > GJ_W / 2) csb *= 2;
+  const int64_t bsz = cdiv(n, 2 * csb);
+  const int64_t slot_bytes = bsz * (MODE == 2 ? m : m + n) * (int64_t)sizeof(float);
+  if (bsz > GJ_W / 2 || slot_bytes > BJ_MAX_SLOT_BYTES || slot_bytes % 16 != 0) return SGT_OK;
+  static bool attr_done = false;
+  auto kern = gjacobi_kernel<MODE>;
+  if (!attr_done) {
+    SGT_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeNonPortableClusterSizeAllowed, 1));
+    SGT_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, 3 * BJ_MAX_SLOT_BYTES));
+    attr_done = true;
+  }
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3(csb, 1, 1);
+  cfg.blockDim = dim3(BJ_THREADS, 1, 1);
+  cfg.dynamicSmemBytes = (size_t)3 * slot_bytes;
+  cfg.stream = st;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeClusterDimension;
+  attr[0].val.clusterDim.x = csb;
+  attr[0].val.clusterDim.y = 1;
+  attr[0].val.clusterDim.z = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  int clusters = 0;
+  if (cudaOccupancyMaxActiveClusters(&clusters, kern, &cfg) != cudaSuccess || clusters < 1) {
+    cudaGetLastError();
+    return SGT_OK;
+  }
+  SGT_CUDA(cudaLaunchKernelEx(&cfg, kern, G, ldg, Vt, ldv, (int)n, (int)m, (int)bsz, jacobi_tol<float>(m), norms,
+                              status, perm));
+  note_launch();
+  *launched = true;
+  return SGT_OK;
+}
+
+// Rows of G and Vt and the norms reordered by decreasing norm (ties by index).
+template <typename T>
+int sort_rows_t(cudaStream_t st, T* G, int64_t ldg, int64_t n, int64_t m, T* Vt, int64_t ldv, T* s,
+                const T* norms, int* perm, T* Gtmp, T* Vtmp) {
+  rank_kernel<T><<<1, 256, 0, st>>>(norms, (int)n, perm);
+  SGT_LAUNCHED();
+  permute_rows_kernel<T><<<g1(n * m), 256, 0, st>>>(G, ldg, Gtmp, m, m, perm, (int)n);
+  SGT_LAUNCHED();
+  permute_rows_kernel<T><<<g1(n * n), 256, 0, st>>>(Vt, ldv, Vtmp, n, n, perm, (int)n);
+  SGT_LAUNCHED();
+  permute_vec_kernel<T><<<g1(n), 256, 0, st>>>(norms, s, perm, (int)n);
+  SGT_LAUNCHED();
+  SGT_CUDA(cudaMemcpy2DAsync(G, ldg * sizeof(T), Gtmp, m * sizeof(T), m * sizeof(T), n,
+                             cudaMemcpyDeviceToDevice, st));
+  SGT_CUDA(cudaMemcpy2DAsync(Vt, ldv * sizeof(T), Vtmp, n * sizeof(T), n * sizeof(T), n,
+                             cudaMemcpyDeviceToDevice, st));
+  return SGT_OK;
+}
+
 // Orthogonalise the n rows (length m) of G; Vt (n x n) receives V^T, s the
 // descending singular values, rows of G and Vt sorted accordingly.
 template <typename T>
@@ -490,6 +1028,13 @@ int jacobi_rows_t(cudaStream_t st, T* G, int64_t ldg, int64_t n, int64_t m, T* V
   int* perm = ar.take<int>((size_t)n);
   SGT_REQUIRE(ar.ok(), SGT_ERR_WORKSPACE, "jacobi: workspace too small");
 
+  // FP32: Gram-form block Jacobi when the rows fit 2 blocks of <= 16 rows per
+  // CTA of a cluster of <= 16 CTAs, Vt included
+  if constexpr (sizeof(T) == 4) {
+    bool launched = false;
+    SGT_TRY(launch_gjacobi<0>(st, G, ldg, Vt, ldv, n, m, norms, status, nullptr, &launched));
+    if (launched) goto sort;
+  }
   // cluster-resident block Jacobi when a cluster of up to 16 CTAs can hold
   // the rows (G, and Vt too when it fits), else the L2-resident kernel below
   if (n >= 64 && m <= 4096) {
@@ -563,20 +1108,7 @@ int jacobi_rows_t(cudaStream_t st, T* G, int64_t ldg, int64_t n, int64_t m, T* V
   note_launch();
   }
 sort:
-
-  rank_kernel<T><<<1, 256, 0, st>>>(norms, (int)n, perm);
-  SGT_LAUNCHED();
-  permute_rows_kernel<T><<<g1(n * m), 256, 0, st>>>(G, ldg, Gtmp, m, m, perm, (int)n);
-  SGT_LAUNCHED();
-  permute_rows_kernel<T><<<g1(n * n), 256, 0, st>>>(Vt, ldv, Vtmp, n, n, perm, (int)n);
-  SGT_LAUNCHED();
-  permute_vec_kernel<T><<<g1(n), 256, 0, st>>>(norms, s, perm, (int)n);
-  SGT_LAUNCHED();
-  SGT_CUDA(cudaMemcpy2DAsync(G, ldg * sizeof(T), Gtmp, m * sizeof(T), m * sizeof(T), n,
-                             cudaMemcpyDeviceToDevice, st));
-  SGT_CUDA(cudaMemcpy2DAsync(Vt, ldv * sizeof(T), Vtmp, n * sizeof(T), n * sizeof(T), n,
-                             cudaMemcpyDeviceToDevice, st));
-  return SGT_OK;
+  return sort_rows_t<T>(st, G, ldg, n, m, Vt, ldv, s, norms, perm, Gtmp, Vtmp);
 }
 
 int jacobi_rows(cudaStream_t st, double* G, int64_t ldg, int64_t n, int64_t m, double* Vt,
@@ -587,6 +1119,115 @@ int jacobi_rows(cudaStream_t st, double* G, int64_t ldg, int64_t n, int64_t m, d
 int jacobi_rows_f32(cudaStream_t st, float* G, int64_t ldg, int64_t n, int64_t m, float* Vt,
                     int64_t ldv, float* s, int* status, Arena& ar) {
   return jacobi_rows_t<float>(st, G, ldg, n, m, Vt, ldv, s, status, ar);
+}
+
+// ---------------------------------------------------------------------------
+// Symmetric positive semi-definite eigenproblem Z = V diag(lam) V^T (FP32,
+// n x n, Z overwritten).  Vt rows: eigenvectors, lam: eigenvalues, decreasing.
+//   method 0: one-sided Jacobi on the rows of Z, rotations accumulated in Vt
+//             (rows of Z V are lam_j v_j^T)
+//   method 2: diagonal-ordered Cholesky + one-sided Jacobi on the rows of the
+//             factor, vectors by normalisation (gjacobi_kernel<2>)
+//   method 3: method 2, then accumulated Jacobi on the rows of V0^T Z starting
+//             from Vt = V0^T (gjacobi_kernel<1>): the first phase leaves the
+//             rows orthogonal to a few 1e-5, so this converges in 2-3 sweeps
+// status: sweeps (method 3: both phases' sum), -1 if a phase hit its cap.
+int split_tf32(cudaStream_t st, const float* x, float* hi, float* lo, int64_t n);
+int gemm_nt_dispatch(cudaStream_t st, int passes, int64_t M, int64_t N, int64_t K, float alpha, const float* Ah,
+                     const float* Al, int64_t lda, const float* Bh, const float* Bl, int64_t ldb, float beta,
+                     float* C, int64_t ldc, int* err);
+
+namespace {
+
+__global__ void diag_order_kernel(const float* __restrict__ Z, int64_t ldz, int n, int* __restrict__ order) {
+  for (int j = threadIdx.x; j < n; j += blockDim.x) {
+    const float v = Z[(int64_t)j * ldz + j];
+    int r = 0;
+    for (int i = 0; i < n; ++i) {
+      const float w = Z[(int64_t)i * ldz + i];
+      r += (w > v) || (w == v && i < j);
+    }
+    order[r] = j;
+  }
+}
+
+__global__ void transpose_sq_kernel(const float* __restrict__ src, float* __restrict__ dst, int n) {
+  __shared__ float tile[32][33];
+  const int bx = blockIdx.x * 32, by = blockIdx.y * 32;
+  for (int j = threadIdx.y; j < 32; j += blockDim.y) {
+    const int r = by + j, c = bx + threadIdx.x;
+    if (r < n && c < n) tile[j][threadIdx.x] = src[(int64_t)r * n + c];
+  }
+  __syncthreads();
+  for (int j = threadIdx.y; j < 32; j += blockDim.y) {
+    const int r = bx + j, c = by + threadIdx.x;
+    if (r < n && c < n) dst[(int64_t)r * n + c] = tile[threadIdx.x][j];
+  }
+}
+
+__global__ void add_status_kernel(int* __restrict__ a, const int* __restrict__ b) {
+  if (threadIdx.x == 0) *a = (*a < 0 || *b < 0) ? -1 : *a + *b;
+}
+
+}  // namespace
+
+size_t sym_eig_rows_ws_bytes(int64_t n) {
+  Arena a = Arena::measuring();
+  a.take<int>((size_t)n);            // diagonal order
+  a.take<int>(2);                    // refinement status, GEMM error word
+  for (int i = 0; i < 9; ++i) a.take<float>((size_t)n * n);  // Z copy, G1, V^T, 3 x (hi, lo)
+  return a.used + jacobi_rows_ws_bytes_t<float>(n, n);
+}
+
+int sym_eig_rows_f32(cudaStream_t st, float* Z, int64_t n, float* Vt, float* lam, int* status, Arena& ar,
+                     int method) {
+  if ((method != 2 && method != 3) || n < 64 || n > 16 * GJ_W)
+    return jacobi_rows_f32(st, Z, n, n, n, Vt, n, lam, status, ar);
+  Arena ar0 = ar;  // for the fallback below, which needs none of the buffers taken here
+  int* order = ar.take<int>((size_t)n);
+  int* st2 = ar.take<int>(2);
+  float* Zc = ar.take<float>((size_t)n * n);
+  float* G1 = ar.take<float>((size_t)n * n);
+  float* Ah = ar.take<float>((size_t)n * n);
+  float* Al = ar.take<float>((size_t)n * n);
+  float* Bh = ar.take<float>((size_t)n * n);
+  float* Bl = ar.take<float>((size_t)n * n);
+  float* VT = ar.take<float>((size_t)n * n);
+  float* Sh = ar.take<float>((size_t)n * n);
+  float* Sl = ar.take<float>((size_t)n * n);
+  float* Gtmp = ar.take<float>((size_t)n * n);
+  float* Vtmp = ar.take<float>((size_t)n * n);
+  float* norms = ar.take<float>((size_t)n);
+  int* perm = ar.take<int>((size_t)n);
+  SGT_REQUIRE(ar.ok(), SGT_ERR_WORKSPACE, "sym_eig: workspace too small");
+  if (method == 3) SGT_CUDA(cudaMemcpyAsync(Zc, Z, sizeof(float) * n * n, cudaMemcpyDeviceToDevice, st));
+  diag_order_kernel<<<1, 512, 0, st>>>(Z, n, (int)n, order);
+  SGT_LAUNCHED();
+  bool launched = false;
+  SGT_TRY(launch_gjacobi<2>(st, Z, n, Vt, n, n, n, norms, status, order, &launched));
+  if (!launched) return jacobi_rows_f32(st, Z, n, n, n, Vt, n, lam, status, ar0);
+  SGT_TRY(sort_rows_t<float>(st, Z, n, n, n, Vt, n, lam, norms, perm, Gtmp, Vtmp));
+  if (method == 2) return SGT_OK;
+  // V0's rows are orthogonal only to the Jacobi tolerance and rotations keep
+  // that error: one Newton-Schulz step V <- 1.5 V - 0.5 (V V^T) V first
+  SGT_CUDA(cudaMemsetAsync(st2, 0, 2 * sizeof(int), st));
+  transpose_sq_kernel<<<dim3((unsigned)cdiv(n, 32), (unsigned)cdiv(n, 32)), dim3(32, 8), 0, st>>>(Vt, VT, (int)n);
+  SGT_LAUNCHED();
+  SGT_TRY(split_tf32(st, Vt, Ah, Al, n * n));
+  SGT_TRY(split_tf32(st, VT, Bh, Bl, n * n));
+  SGT_TRY(gemm_nt_dispatch(st, 3, n, n, n, 1.f, Ah, Al, n, Ah, Al, n, 0.f, G1, n, st2 + 1));  // S = V V^T
+  SGT_TRY(split_tf32(st, G1, Sh, Sl, n * n));
+  SGT_TRY(gemm_nt_dispatch(st, 3, n, n, n, -0.5f, Sh, Sl, n, Bh, Bl, n, 1.5f, Vt, n, st2 + 1));  // S V
+  // G1 = V0^T Z (rows (Z v_j)^T; Z symmetric, so the NT product with Z itself)
+  SGT_TRY(split_tf32(st, Vt, Ah, Al, n * n));
+  SGT_TRY(split_tf32(st, Zc, Bh, Bl, n * n));
+  SGT_TRY(gemm_nt_dispatch(st, 3, n, n, n, 1.f, Ah, Al, n, Bh, Bl, n, 0.f, G1, n, st2 + 1));
+  SGT_TRY(launch_gjacobi<1>(st, G1, n, Vt, n, n, n, norms, st2, nullptr, &launched));
+  SGT_REQUIRE(launched, SGT_ERR_CUDA, "sym_eig: refinement kernel not schedulable");
+  SGT_TRY(sort_rows_t<float>(st, G1, n, n, n, Vt, n, lam, norms, perm, Gtmp, Vtmp));
+  add_status_kernel<<<1, 32, 0, st>>>(status, st2);
+  SGT_LAUNCHED();
+  return SGT_OK;
 }
 
 }  // namespace sgt

@@ -319,6 +319,13 @@ def retrieve(cores: Cores, indices: Sequence[int]) -> float:
 # fused metric operation: raw W @ X then TT-SVD round
 # ---------------------------------------------------------------------------
 
+def eig_method(method: int = 0) -> int:
+    """Select the bond eigensolver of the Gram form (1: one-sided Jacobi on Z,
+    2: on Z's Cholesky factor, 3: 2 + accumulated refinement); 0 only queries.
+    Returns the previous choice."""
+    return int(L.load().sgt_eig_method(int(method)))
+
+
 def mpo_mps_round(W: Cores, X: Cores, chi: int, precision: int = L.PREC_F64):
     """Raw ``W @ X`` followed by TT-SVD rounding to ``chi`` in one library call.
     Returns ``(cores, spectra, counts, discarded, status)`` (device tensors)."""

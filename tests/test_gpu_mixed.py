@@ -29,7 +29,8 @@ def dev(cores):
     return [_lib.as_device(c) for c in cores]
 
 
-CASES = [(6, 2, 8, 3, 5), (10, 2, 32, 4, 24), (8, 3, 16, 4, 20), (12, 2, 64, 8, 64)]
+CASES = [(6, 2, 8, 3, 5), (10, 2, 32, 4, 24), (8, 3, 16, 4, 20), (12, 2, 64, 8, 64), (8, 2, 32, 16, 48),
+         (7, 3, 16, 8, 30)]
 
 
 @pytest.mark.parametrize("n,d,chi,D,cut", CASES)
@@ -60,3 +61,27 @@ def test_mpo_mps_round(n, d, chi, D, cut, prec, tol_norm, tol_spec):
     if prec == 0:
         assert abs(ov - ovr) <= 1e-11 * abs(ovr)
         np.testing.assert_allclose(disc.cpu().numpy(), disc_r, rtol=1e-9, atol=1e-15)
+
+
+@pytest.mark.parametrize("method", [1, 2, 3])
+def test_mpo_mps_round_eig_methods(method):
+    """The three bond eigensolvers of the Gram form give the same rounded state
+    (3xTF32, a chain whose bond problems are 128 x 128)."""
+    from syngular_gb300.tensor import _ops
+
+    n, d, chi, D, cut = 10, 2, 32, 8, 64
+    rng = np.random.default_rng(77)
+    X = O.random_mps_cores(rng, n, d, chi)
+    W = O.random_mpo_cores(rng, n, d, D)
+    Zr, spec_r, _ = O.tt_svd_round(O.mpo_mps_product(W, X), cut)
+    prev = _ops.eig_method(method)
+    try:
+        Z, spec, counts, disc, status = _ops.mpo_mps_round(dev(W), dev(X), cut, 4)
+        torch.cuda.synchronize()
+    finally:
+        _ops.eig_method(prev)
+    assert int(status.item()) >= 0
+    Zd = [torch.from_numpy(z).cuda() for z in Zr]
+    nz = np.sqrt(O.overlap(Zr, Zr))
+    fid = abs(_ops.overlap(Z, Zd)) / (np.sqrt(abs(_ops.overlap(Z, Z))) * nz)
+    assert 1 - fid < 1e-8
