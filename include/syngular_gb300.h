@@ -259,10 +259,12 @@ SGT_API int sgt_tc_profile(int enable, double* ms, double* flops, long long* lau
  * Z (n x n, overwritten) -> Vt rows = eigenvectors, lam descending.
  * method 0: two-sided block Jacobi in one thread-block cluster (used when it
  * fits, else method 1); method 1: one-sided Jacobi on the rows of Z;
- * method 2: one-sided Jacobi on the rows of the Cholesky factor of Z taken in
- * decreasing-diagonal order (about half the sweeps; vectors by normalisation);
- * method 3: method 2 followed by accumulated Jacobi on the rows of V^T Z.
- * status: sweeps performed (method 3: both phases), -1 at the sweep cap. */
+ * method 2: one-sided Jacobi on the rows of the Cholesky factor of Z + delta I
+ * (delta = 2 n eps max diag) taken in decreasing-diagonal order: about two
+ * thirds of the sweeps, vectors by normalisation (less accurate near the cut);
+ * method 3: the same factor, one-sided Jacobi on its columns with the rotations
+ * accumulated (the eigenvectors are the rows of the accumulated rotation).
+ * status: sweeps performed, -1 at the sweep cap. */
 SGT_API size_t sgt_sym_eig_f32_workspace_size(int64_t n);
 SGT_API int sgt_sym_eig_f32(float* Z, int64_t n, float* Vt, float* lam, int* status, int method,
                             void* ws, size_t ws_bytes, void* stream);
@@ -270,7 +272,9 @@ SGT_API int sgt_sym_eig_f32(float* Z, int64_t n, float* Vt, float* lam, int* sta
 /* Eigensolver used for the bond problems of the Gram form (sgt_mpo_mps_round
  * with TF32 / TF32X3): the sgt_sym_eig_f32 method 1, 2 or 3 (other values leave
  * it unchanged).  Returns the previous choice.  The initial choice is 1, or the
- * value of the environment variable SGT_EIG_METHOD.  Process-wide. */
+ * value of the environment variable SGT_EIG_METHOD.  Process-wide.  The FP32
+ * Jacobi stopping threshold on |g_p.g_q| / (|g_p||g_q|) is k eps sqrt(m) with
+ * k = 8, or the value of SGT_EIG_TOL. */
 SGT_API int sgt_eig_method(int method);
 
 /* hi = TF32 rounding of x (round to nearest, ties away), lo = x - hi (lo may be NULL). */

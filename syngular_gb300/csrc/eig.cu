@@ -411,7 +411,7 @@ extern "C" SGT_API size_t sgt_sym_eig_f32_workspace_size(int64_t n) {
 // method 0: two-sided block Jacobi in one cluster (falls back to 1 when n does
 // not fit); method 1: one-sided Jacobi on the rows of Z; method 2: Jacobi on
 // the rows of Z's diagonal-ordered Cholesky factor (vectors by normalisation);
-// method 3: method 2 refined by accumulated Jacobi on the rows of V^T Z.
+// method 3: on the columns of that factor with the rotations accumulated.
 extern "C" SGT_API int sgt_sym_eig_f32(float* Z, int64_t n, float* Vt, float* lam, int* status, int method,
                                        void* ws, size_t ws_bytes, void* stream) {
   using namespace sgt;

@@ -217,7 +217,7 @@ __global__ void merge_status_kernel(const int* __restrict__ st, int n, int* __re
   *out = r;
 }
 
-// Eigensolver of the projected Gram matrices (sgt_sym_eig_f32 methods 1-3):
+// Eigensolver of the projected Gram matrices (sgt_sym_eig_f32 method 1, 2 or 3):
 // SGT_EIG_METHOD in the environment sets the initial choice, sgt_eig_method()
 // changes it.
 std::atomic<int> g_eig_method{0};

@@ -15,6 +15,8 @@
 #include <cooperative_groups.h>
 #include <float.h>
 
+#include <cstdlib>
+
 #include "common.cuh"
 
 namespace cg = cooperative_groups;
@@ -424,21 +426,20 @@ __global__ void __launch_bounds__(BJ_THREADS) bjacobi_kernel(T* __restrict__ G, 
 // stopping floor are unchanged; shared-memory traffic per step drops from
 // O(W^2 (m + n)) to O(W (m + n)).
 //
-// MODE 0: rows of G, Vt = I.  MODE 1: rows of G, Vt rows loaded from Vt (a
-// refinement of approximate eigenvectors).  MODE 2 (G = a symmetric positive
+// MODE 0: rows of G, Vt = I.  MODE 2 (G = a symmetric positive
 // semi-definite Z, m = n): the rows and columns of Z are gathered in the order
-// perm (decreasing diagonal), factored in place as Z_perm = R^T R by a blocked
-// row-oriented Cholesky across the cluster (the owner of block J factors its
-// rows, every CTA applies the rank-bs update of its later rows from a DSMEM
-// copy of R's block row) after a diagonal shift delta = 2 n eps max(diag)
-// that makes the FP32 factorisation stable for rank-deficient Z; then the
-// rows of R are orthogonalised without Vt (rows of J R = s_j u_j^T, u_j the
+// perm (decreasing diagonal), factored in place as Z_perm + delta I = R^T R by
+// a blocked row-oriented Cholesky across the cluster (the owner of block J
+// factors its rows, every CTA applies the rank-bs update of its later rows
+// from a DSMEM copy of R's block row); the shift delta = 2 n eps max(diag)
+// makes the FP32 factorisation stable for rank-deficient Z.  Then the rows of
+// R are orthogonalised without Vt (rows of J R = s_j u_j^T, u_j the
 // eigenvectors of Z_perm, s_j^2 = lam_j + delta).  On exit G rows are
 // lam_j u_j^T and Vt rows u_j^T, both in the original column order, and
-// norms = lam_j.  Jacobi on the pivoted Cholesky factor needs
-// about half the sweeps of Jacobi on Z (its rows are graded and nearly
-// orthogonal from the start); its vectors come from normalisation, so MODE 1
-// can follow to restore accumulated-rotation accuracy.
+// norms = lam_j.  Jacobi on the Cholesky factor needs about two thirds of the
+// sweeps of Jacobi on Z (its rows are graded and nearly orthogonal from the
+// start), but its vectors come from normalising rows that are orthogonal only
+// to the Jacobi tolerance.
 constexpr int GJ_W = 32;
 
 template <int MODE>
@@ -488,16 +489,15 @@ __global__ void __launch_bounds__(BJ_THREADS) gjacobi_kernel(float* __restrict__
       const int gr = blk * bs + r;
       float v = 0.f;
       if (gr < n) {
-        if (MODE == 2) v = G[(int64_t)perm[gr] * ldg + perm[e]];
+        if (MODE >= 2) v = (e < m) ? G[(int64_t)perm[gr] * ldg + perm[e]] : 0.f;
         else if (e < m) v = G[(int64_t)gr * ldg + e];
-        else if (MODE == 1) v = Vt[(int64_t)gr * ldv + (e - m)];
         else v = ((e - m) == gr) ? 1.f : 0.f;
       }
       slots[(int64_t)sl * slot_elems + i] = v;
     }
   }
   float shift = 0.f;
-  if constexpr (MODE == 2) {
+  if constexpr (MODE >= 2) {
     // ---- largest diagonal entry over the cluster -> shift and pivot floor ----
     float mx = 0.f;
     for (int sl = 0; sl < 2; ++sl)
@@ -602,6 +602,45 @@ __global__ void __launch_bounds__(BJ_THREADS) gjacobi_kernel(float* __restrict__
       }
     }
     cluster.sync();
+    if constexpr (MODE == 3) {
+      // rows of L = R^T: local row i (position) <- column i of R, gathered from
+      // the owners of R's rows; slot 0 through the stage buffer, slot 1
+      // through registers, one cluster barrier before the local writes; the
+      // Vt part starts as I
+      constexpr int REGS = BJ_MAX_SLOT_BYTES / 2 / 4 / BJ_THREADS;  // G part <= half a slot
+      float hold[REGS];
+      for (int sl = 0; sl < 2; ++sl) {
+        const int B = slot_pos(rank, sl);
+        int k = 0;
+        for (int idx = tid; idx < bs * m; idx += BJ_THREADS, ++k) {
+          const int r = idx / m, j = idx % m;
+          const int i = B * bs + r;
+          float v = 0.f;
+          if (i < n && j <= i) {
+            int ocs, osl;
+            pos_owner(j / bs, ocs, osl);
+            v = cluster.map_shared_rank(slots, ocs)[(int64_t)osl * slot_elems + (int64_t)(j % bs) * row_len + i];
+          }
+          if (sl == 0) stage[(int64_t)r * row_len + j] = v;
+          else if (k < REGS) hold[k] = v;
+        }
+      }
+      cluster.sync();
+      for (int sl = 0; sl < 2; ++sl) {
+        const int B = slot_pos(rank, sl);
+        int k = 0;
+        for (int idx = tid; idx < bs * m; idx += BJ_THREADS, ++k) {
+          const int r = idx / m, j = idx % m;
+          float* row = slots + (int64_t)sl * slot_elems + (int64_t)r * row_len;
+          row[j] = (sl == 0) ? stage[(int64_t)r * row_len + j] : (k < REGS ? hold[k] : 0.f);
+        }
+        for (int idx = tid; idx < bs * n; idx += BJ_THREADS) {
+          const int r = idx / n, c = idx % n;
+          slots[(int64_t)sl * slot_elems + (int64_t)r * row_len + m + c] = (B * bs + r == c) ? 1.f : 0.f;
+        }
+      }
+      __syncthreads();
+    }
   }
   // |G|_F^2 over the cluster -> floor m (eps |G|_F)^2 on |g_p . g_q|
   {
@@ -688,18 +727,30 @@ __global__ void __launch_bounds__(BJ_THREADS) gjacobi_kernel(float* __restrict__
       if (tid == 0) s_any = 0;
       __syncthreads();
 
-      // ---- 2. one sweep of two-sided rotations on C, accumulated in Q ----
+      // ---- 2. rotations on C, accumulated in Q.  The first step of a sweep
+      // takes every pair of the 2 bs working rows (round robin, 2 bs - 1
+      // sub-steps); all blocks sit in some working set then, so the later
+      // steps need only the pairs across the two blocks (sub-step u pairs
+      // local row i with row bs + (i + u) mod bs: bs sub-steps).  Every pair
+      // of rows is thus visited once per sweep.
       int cur = 0;
-      for (int sub = 0; sub < weff - 1; ++sub) {
+      const bool all_pairs = (step == 0);
+      const int nsub = all_pairs ? weff - 1 : bs;
+      auto pair_p = [&](int i, int u) { return all_pairs ? rr_index(i, u, weff) : i; };
+      auto pair_q = [&](int i, int u) {
+        if (!all_pairs) return bs + (i + u) % bs;
+        return rr_index(weff - 1 - i, u, weff);
+      };
+      for (int sub = 0; sub < nsub; ++sub) {
         if (warp < bs) {
           const int i = warp;
-          const int pi = rr_index(i, sub, weff), qi = rr_index(weff - 1 - i, sub, weff);
+          const int pi = pair_p(i, sub), qi = pair_q(i, sub);
           // lane j < bs: the rotation of pair j
           float cj = 1.f, sj = 0.f, tj_ = 0.f, tanj = 0.f;
           int rj = 0, pj = 0, qj = 0;
           if (lane < bs) {
-            pj = rr_index(lane, sub, weff);
-            qj = rr_index(weff - 1 - lane, sub, weff);
+            pj = pair_p(lane, sub);
+            qj = pair_q(lane, sub);
             const float a = fmaxf(sC[cur][pj][pj], 0.f), b = fmaxf(sC[cur][qj][qj], 0.f), c = sC[cur][pj][qj];
             float c_, s_, t_;
             if (jacobi_rotation<float>(a, b, c, (double)ftol, (double)abs_floor, lane, c_, s_, t_)) {
@@ -861,6 +912,24 @@ __global__ void __launch_bounds__(BJ_THREADS) gjacobi_kernel(float* __restrict__
       }
       continue;
     }
+    if (MODE == 3) {
+      for (int r = warp; r < bs; r += BJ_WARPS) {
+        const int gr = blk * bs + r;
+        if (gr >= n) continue;
+        const float* row = slots + (int64_t)sl * slot_elems + (int64_t)r * row_len;
+        float acc = 0.f;
+        for (int e = lane; e < m; e += 32) acc = fmaf(row[e], row[e], acc);
+        acc = wsum_t(acc);
+        const float lam = fmaxf(acc - shift, 0.f);
+        for (int e = lane; e < n; e += 32) {
+          const float v = row[m + e];
+          G[(int64_t)gr * ldg + perm[e]] = lam * v;
+          Vt[(int64_t)gr * ldv + perm[e]] = v;
+        }
+        if (lane == 0) norms[gr] = lam;
+      }
+      continue;
+    }
     for (int64_t i = tid; i < slot_elems; i += BJ_THREADS) {
       const int r = (int)(i / row_len), e = (int)(i % row_len);
       const int gr = blk * bs + r;
@@ -932,10 +1001,20 @@ inline unsigned g1(int64_t n) {
 // Convergence threshold on |g_p.g_q| / (|g_p| |g_q|): a few times the rounding
 // noise of an m-term dot product, so that noise alone does not keep pairs
 // rotating (FP64: 4 eps sqrt(m); FP32: 8 eps sqrt(m)).
+// FP32 multiplier: 8 unless SGT_EIG_TOL (a positive number) overrides it.
+static double f32_tol_scale() {
+  static const double v = [] {
+    const char* e = getenv("SGT_EIG_TOL");
+    const double x = e ? atof(e) : 0.0;
+    return (x > 0.0 && x < 1e6) ? x : 8.0;
+  }();
+  return v;
+}
+
 template <typename T>
 double jacobi_tol(int64_t m) {
   const double eps = (sizeof(T) == 8) ? DBL_EPSILON : (double)FLT_EPSILON;
-  const double k = (sizeof(T) == 8) ? 4.0 : 8.0;
+  const double k = (sizeof(T) == 8) ? 4.0 : f32_tol_scale();
   return k * eps * sqrt((double)std::max<int64_t>(m, 1));
 }
 
@@ -959,7 +1038,7 @@ template <int MODE>
 static int launch_gjacobi(cudaStream_t st, float* G, int64_t ldg, float* Vt, int64_t ldv, int64_t n, int64_t m,
                           float* norms, int* status, const int* perm, bool* launched) {
   *launched = false;
-  if (n < 64 || n > 16 * GJ_W || (MODE == 2 && m != n)) return SGT_OK;
+  if (n < 64 || n > 16 * GJ_W || (MODE >= 2 && m != n)) return SGT_OK;
   int csb = 2;
   while (csb < 16 && cdiv(n, 2 * csb) > GJ_W / 2) csb *= 2;
   const int64_t bsz = cdiv(n, 2 * csb);
@@ -1127,15 +1206,11 @@ int jacobi_rows_f32(cudaStream_t st, float* G, int64_t ldg, int64_t n, int64_t m
 //   method 0: one-sided Jacobi on the rows of Z, rotations accumulated in Vt
 //             (rows of Z V are lam_j v_j^T)
 //   method 2: diagonal-ordered Cholesky + one-sided Jacobi on the rows of the
-//             factor, vectors by normalisation (gjacobi_kernel<2>)
-//   method 3: method 2, then accumulated Jacobi on the rows of V0^T Z starting
-//             from Vt = V0^T (gjacobi_kernel<1>): the first phase leaves the
-//             rows orthogonal to a few 1e-5, so this converges in 2-3 sweeps
-// status: sweeps (method 3: both phases' sum), -1 if a phase hit its cap.
-int split_tf32(cudaStream_t st, const float* x, float* hi, float* lo, int64_t n);
-int gemm_nt_dispatch(cudaStream_t st, int passes, int64_t M, int64_t N, int64_t K, float alpha, const float* Ah,
-                     const float* Al, int64_t lda, const float* Bh, const float* Bl, int64_t ldb, float beta,
-                     float* C, int64_t ldc, int* err);
+//             factor R, vectors by normalisation (gjacobi_kernel<2>)
+//   method 3: the same factor, one-sided Jacobi on the rows of L = R^T with
+//             the rotations accumulated: the eigenvectors of Z are the rows of
+//             the accumulated rotation (R^T R = J^T S^2 J) (gjacobi_kernel<3>)
+// status: sweeps, -1 at the sweep cap.
 
 namespace {
 
@@ -1151,31 +1226,11 @@ __global__ void diag_order_kernel(const float* __restrict__ Z, int64_t ldz, int 
   }
 }
 
-__global__ void transpose_sq_kernel(const float* __restrict__ src, float* __restrict__ dst, int n) {
-  __shared__ float tile[32][33];
-  const int bx = blockIdx.x * 32, by = blockIdx.y * 32;
-  for (int j = threadIdx.y; j < 32; j += blockDim.y) {
-    const int r = by + j, c = bx + threadIdx.x;
-    if (r < n && c < n) tile[j][threadIdx.x] = src[(int64_t)r * n + c];
-  }
-  __syncthreads();
-  for (int j = threadIdx.y; j < 32; j += blockDim.y) {
-    const int r = bx + j, c = by + threadIdx.x;
-    if (r < n && c < n) dst[(int64_t)r * n + c] = tile[threadIdx.x][j];
-  }
-}
-
-__global__ void add_status_kernel(int* __restrict__ a, const int* __restrict__ b) {
-  if (threadIdx.x == 0) *a = (*a < 0 || *b < 0) ? -1 : *a + *b;
-}
-
 }  // namespace
 
 size_t sym_eig_rows_ws_bytes(int64_t n) {
   Arena a = Arena::measuring();
-  a.take<int>((size_t)n);            // diagonal order
-  a.take<int>(2);                    // refinement status, GEMM error word
-  for (int i = 0; i < 9; ++i) a.take<float>((size_t)n * n);  // Z copy, G1, V^T, 3 x (hi, lo)
+  a.take<int>((size_t)n);  // diagonal order
   return a.used + jacobi_rows_ws_bytes_t<float>(n, n);
 }
 
@@ -1185,48 +1240,18 @@ int sym_eig_rows_f32(cudaStream_t st, float* Z, int64_t n, float* Vt, float* lam
     return jacobi_rows_f32(st, Z, n, n, n, Vt, n, lam, status, ar);
   Arena ar0 = ar;  // for the fallback below, which needs none of the buffers taken here
   int* order = ar.take<int>((size_t)n);
-  int* st2 = ar.take<int>(2);
-  float* Zc = ar.take<float>((size_t)n * n);
-  float* G1 = ar.take<float>((size_t)n * n);
-  float* Ah = ar.take<float>((size_t)n * n);
-  float* Al = ar.take<float>((size_t)n * n);
-  float* Bh = ar.take<float>((size_t)n * n);
-  float* Bl = ar.take<float>((size_t)n * n);
-  float* VT = ar.take<float>((size_t)n * n);
-  float* Sh = ar.take<float>((size_t)n * n);
-  float* Sl = ar.take<float>((size_t)n * n);
   float* Gtmp = ar.take<float>((size_t)n * n);
   float* Vtmp = ar.take<float>((size_t)n * n);
   float* norms = ar.take<float>((size_t)n);
   int* perm = ar.take<int>((size_t)n);
   SGT_REQUIRE(ar.ok(), SGT_ERR_WORKSPACE, "sym_eig: workspace too small");
-  if (method == 3) SGT_CUDA(cudaMemcpyAsync(Zc, Z, sizeof(float) * n * n, cudaMemcpyDeviceToDevice, st));
   diag_order_kernel<<<1, 512, 0, st>>>(Z, n, (int)n, order);
   SGT_LAUNCHED();
   bool launched = false;
-  SGT_TRY(launch_gjacobi<2>(st, Z, n, Vt, n, n, n, norms, status, order, &launched));
+  if (method == 2) SGT_TRY(launch_gjacobi<2>(st, Z, n, Vt, n, n, n, norms, status, order, &launched));
+  else SGT_TRY(launch_gjacobi<3>(st, Z, n, Vt, n, n, n, norms, status, order, &launched));
   if (!launched) return jacobi_rows_f32(st, Z, n, n, n, Vt, n, lam, status, ar0);
   SGT_TRY(sort_rows_t<float>(st, Z, n, n, n, Vt, n, lam, norms, perm, Gtmp, Vtmp));
-  if (method == 2) return SGT_OK;
-  // V0's rows are orthogonal only to the Jacobi tolerance and rotations keep
-  // that error: one Newton-Schulz step V <- 1.5 V - 0.5 (V V^T) V first
-  SGT_CUDA(cudaMemsetAsync(st2, 0, 2 * sizeof(int), st));
-  transpose_sq_kernel<<<dim3((unsigned)cdiv(n, 32), (unsigned)cdiv(n, 32)), dim3(32, 8), 0, st>>>(Vt, VT, (int)n);
-  SGT_LAUNCHED();
-  SGT_TRY(split_tf32(st, Vt, Ah, Al, n * n));
-  SGT_TRY(split_tf32(st, VT, Bh, Bl, n * n));
-  SGT_TRY(gemm_nt_dispatch(st, 3, n, n, n, 1.f, Ah, Al, n, Ah, Al, n, 0.f, G1, n, st2 + 1));  // S = V V^T
-  SGT_TRY(split_tf32(st, G1, Sh, Sl, n * n));
-  SGT_TRY(gemm_nt_dispatch(st, 3, n, n, n, -0.5f, Sh, Sl, n, Bh, Bl, n, 1.5f, Vt, n, st2 + 1));  // S V
-  // G1 = V0^T Z (rows (Z v_j)^T; Z symmetric, so the NT product with Z itself)
-  SGT_TRY(split_tf32(st, Vt, Ah, Al, n * n));
-  SGT_TRY(split_tf32(st, Zc, Bh, Bl, n * n));
-  SGT_TRY(gemm_nt_dispatch(st, 3, n, n, n, 1.f, Ah, Al, n, Bh, Bl, n, 0.f, G1, n, st2 + 1));
-  SGT_TRY(launch_gjacobi<1>(st, G1, n, Vt, n, n, n, norms, st2, nullptr, &launched));
-  SGT_REQUIRE(launched, SGT_ERR_CUDA, "sym_eig: refinement kernel not schedulable");
-  SGT_TRY(sort_rows_t<float>(st, G1, n, n, n, Vt, n, lam, norms, perm, Gtmp, Vtmp));
-  add_status_kernel<<<1, 32, 0, st>>>(status, st2);
-  SGT_LAUNCHED();
   return SGT_OK;
 }
 

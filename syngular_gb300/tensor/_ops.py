@@ -321,7 +321,8 @@ def retrieve(cores: Cores, indices: Sequence[int]) -> float:
 
 def eig_method(method: int = 0) -> int:
     """Select the bond eigensolver of the Gram form (1: one-sided Jacobi on Z,
-    2: on Z's Cholesky factor, 3: 2 + accumulated refinement); 0 only queries.
+    2: on Z's Cholesky factor, vectors by normalisation, 3: on the factor's
+    columns with accumulated rotations); 0 only queries.
     Returns the previous choice."""
     return int(L.load().sgt_eig_method(int(method)))
 

@@ -36,7 +36,7 @@ def run(Z, method):
 
 # per method: (1 - min cos of the top-n/2 subspace angles, |Vt Vt^T - I| max).  Method 2
 # takes its vectors by normalising rows that are orthogonal to the Jacobi tolerance
-# (8 eps sqrt(n)), so both figures are looser; method 3 refines them back.
+# (8 eps sqrt(n)), so both figures are looser.
 TOL = {0: (1e-5, 5e-5), 1: (1e-5, 5e-5), 2: (3e-4, 3e-4), 3: (1e-5, 5e-5)}
 
 
