@@ -274,7 +274,7 @@ SGT_API int sgt_sym_eig_f32(float* Z, int64_t n, float* Vt, float* lam, int* sta
  * it unchanged).  Returns the previous choice.  The initial choice is 1, or the
  * value of the environment variable SGT_EIG_METHOD.  Process-wide.  The FP32
  * Jacobi stopping threshold on |g_p.g_q| / (|g_p||g_q|) is k eps sqrt(m) with
- * k = 8, or the value of SGT_EIG_TOL. */
+ * k = 1, or the value of SGT_EIG_TOL. */
 SGT_API int sgt_eig_method(int method);
 
 /* hi = TF32 rounding of x (round to nearest, ties away), lo = x - hi (lo may be NULL). */
