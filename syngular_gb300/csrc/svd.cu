@@ -445,6 +445,8 @@ __global__ void __launch_bounds__(BJ_THREADS) bjacobi_kernel(T* __restrict__ G, 
 // start), but its vectors come from normalising rows that are orthogonal only
 // to the Jacobi tolerance.
 constexpr int GJ_W = 32;
+constexpr int GJ_SLOT_CAP = BJ_MAX_SLOT_BYTES + 4 * (GJ_W / 2) * (GJ_W / 2);  // rows + tracked Gram
+constexpr int GJ_MOVE_REGS = (GJ_SLOT_CAP / 16 + BJ_THREADS - 1) / BJ_THREADS;
 
 template <int MODE>
 __global__ void __launch_bounds__(BJ_THREADS) gjacobi_kernel(float* __restrict__ G, int64_t ldg,
@@ -459,11 +461,15 @@ __global__ void __launch_bounds__(BJ_THREADS) gjacobi_kernel(float* __restrict__
   const int nblk = 2 * cs;
   const int row_len = (MODE == 2) ? m : m + n;  // G part then Vt part
   const int slot_elems = bs * row_len;
+  // each slot: bs rows, then the bs x bs Gram matrix of those rows as tracked
+  // through the rotations (it travels with the rows)
+  const int gstride = (bs * bs + 3) & ~3;
+  const int slot_tot = slot_elems + gstride;
   const int weff = 2 * bs;    // working rows (<= GJ_W)
 
   extern __shared__ __align__(16) unsigned char gj_raw[];
-  float* slots = reinterpret_cast<float*>(gj_raw);  // [2][bs][row_len]
-  float* stage = slots + 2 * slot_elems;            // [bs][row_len]
+  float* slots = reinterpret_cast<float*>(gj_raw);  // 2 x ([bs][row_len], [bs][bs])
+  float* stage = slots + 2 * slot_tot;              // one slot
   __shared__ __align__(16) float sC[2][GJ_W][GJ_W];
   __shared__ __align__(16) float sQ[GJ_W][GJ_W];
   __shared__ int s_off[GJ_W];
@@ -484,7 +490,7 @@ __global__ void __launch_bounds__(BJ_THREADS) gjacobi_kernel(float* __restrict__
   };
   auto slot_pos = [&](int c, int slot) { return slot == 0 ? c : nblk - 1 - c; };
 
-  if (tid < GJ_W) s_off[tid] = (tid < weff) ? (tid / bs) * slot_elems + (tid % bs) * row_len : -1;
+  if (tid < GJ_W) s_off[tid] = (tid < weff) ? (tid / bs) * slot_tot + (tid % bs) * row_len : -1;
   for (int sl = 0; sl < 2; ++sl) {
     const int blk = slot_pos(rank, sl);
     if (tid == 0) s_blk[sl] = blk;
@@ -497,7 +503,7 @@ __global__ void __launch_bounds__(BJ_THREADS) gjacobi_kernel(float* __restrict__
         else if (e < m) v = G[(int64_t)gr * ldg + e];
         else v = ((e - m) == gr) ? 1.f : 0.f;
       }
-      slots[(int64_t)sl * slot_elems + i] = v;
+      slots[(int64_t)sl * slot_tot + i] = v;
     }
   }
   float shift = 0.f;
@@ -507,7 +513,7 @@ __global__ void __launch_bounds__(BJ_THREADS) gjacobi_kernel(float* __restrict__
     for (int sl = 0; sl < 2; ++sl)
       for (int r = tid; r < bs; r += BJ_THREADS) {
         const int gr = slot_pos(rank, sl) * bs + r;
-        if (gr < n) mx = fmaxf(mx, slots[(int64_t)sl * slot_elems + (int64_t)r * row_len + gr]);
+        if (gr < n) mx = fmaxf(mx, slots[(int64_t)sl * slot_tot + (int64_t)r * row_len + gr]);
       }
     for (int o = 16; o > 0; o >>= 1) mx = fmaxf(mx, __shfl_xor_sync(0xffffffffu, mx, o));
     if (lane == 0) s_red[warp] = (double)mx;
@@ -534,7 +540,7 @@ __global__ void __launch_bounds__(BJ_THREADS) gjacobi_kernel(float* __restrict__
     for (int sl = 0; sl < 2; ++sl)
       for (int r = tid; r < bs; r += BJ_THREADS) {
         const int gr = slot_pos(rank, sl) * bs + r;
-        if (gr < n) slots[(int64_t)sl * slot_elems + (int64_t)r * row_len + gr] += shift;
+        if (gr < n) slots[(int64_t)sl * slot_tot + (int64_t)r * row_len + gr] += shift;
       }
     cluster.sync();  // s_norm / s_red are reused below
     // ---- blocked row-oriented Cholesky, Z_perm = R^T R ----
@@ -546,7 +552,7 @@ __global__ void __launch_bounds__(BJ_THREADS) gjacobi_kernel(float* __restrict__
       pos_owner(J, ocs, osl);
       const int jrows = min(bs, n - j0);
       if (rank == ocs) {
-        float* blk = slots + (int64_t)osl * slot_elems;
+        float* blk = slots + (int64_t)osl * slot_tot;
         for (int r = 0; r < jrows; ++r) {
           const int gi = j0 + r;
           float* row = blk + (int64_t)r * row_len;
@@ -568,7 +574,7 @@ __global__ void __launch_bounds__(BJ_THREADS) gjacobi_kernel(float* __restrict__
       cluster.sync();
       const int c0 = j0 + bs;
       if (c0 < n) {
-        const float* src = cluster.map_shared_rank(slots, ocs) + (int64_t)osl * slot_elems;
+        const float* src = cluster.map_shared_rank(slots, ocs) + (int64_t)osl * slot_tot;
         const int w = n - c0;
         for (int idx = tid; idx < bs * w; idx += BJ_THREADS) {
           const int i = idx / w, e = c0 + idx % w;
@@ -599,7 +605,7 @@ __global__ void __launch_bounds__(BJ_THREADS) gjacobi_kernel(float* __restrict__
               acc = fmaf(c.z, x[4 * q + 2], acc);
               acc = fmaf(c.w, x[4 * q + 3], acc);
             }
-            slots[(int64_t)sl * slot_elems + (int64_t)r * row_len + e] -= acc;
+            slots[(int64_t)sl * slot_tot + (int64_t)r * row_len + e] -= acc;
           }
         }
         __syncthreads();
@@ -623,7 +629,7 @@ __global__ void __launch_bounds__(BJ_THREADS) gjacobi_kernel(float* __restrict__
           if (i < n && j <= i) {
             int ocs, osl;
             pos_owner(j / bs, ocs, osl);
-            v = cluster.map_shared_rank(slots, ocs)[(int64_t)osl * slot_elems + (int64_t)(j % bs) * row_len + i];
+            v = cluster.map_shared_rank(slots, ocs)[(int64_t)osl * slot_tot + (int64_t)(j % bs) * row_len + i];
           }
           if (sl == 0) stage[(int64_t)r * row_len + j] = v;
           else if (k < REGS) hold[k] = v;
@@ -635,12 +641,12 @@ __global__ void __launch_bounds__(BJ_THREADS) gjacobi_kernel(float* __restrict__
         int k = 0;
         for (int idx = tid; idx < bs * m; idx += BJ_THREADS, ++k) {
           const int r = idx / m, j = idx % m;
-          float* row = slots + (int64_t)sl * slot_elems + (int64_t)r * row_len;
+          float* row = slots + (int64_t)sl * slot_tot + (int64_t)r * row_len;
           row[j] = (sl == 0) ? stage[(int64_t)r * row_len + j] : (k < REGS ? hold[k] : 0.f);
         }
         for (int idx = tid; idx < bs * n; idx += BJ_THREADS) {
           const int r = idx / n, c = idx % n;
-          slots[(int64_t)sl * slot_elems + (int64_t)r * row_len + m + c] = (B * bs + r == c) ? 1.f : 0.f;
+          slots[(int64_t)sl * slot_tot + (int64_t)r * row_len + m + c] = (B * bs + r == c) ? 1.f : 0.f;
         }
       }
       __syncthreads();
@@ -650,9 +656,9 @@ __global__ void __launch_bounds__(BJ_THREADS) gjacobi_kernel(float* __restrict__
   {
     double acc = 0.0;
     for (int64_t i = tid; i < 2 * (int64_t)slot_elems; i += BJ_THREADS) {
-      const int e = (int)(i % row_len);
-      if (e < m) {
-        const double v = (double)slots[i];
+      const int sl = (int)(i / slot_elems), j = (int)(i % slot_elems);
+      if (j % row_len < m) {
+        const double v = (double)slots[(int64_t)sl * slot_tot + j];
         acc += v * v;
       }
     }
@@ -680,14 +686,9 @@ __global__ void __launch_bounds__(BJ_THREADS) gjacobi_kernel(float* __restrict__
   const float abs_floor = (float)s_norm;
   const float ftol = (float)tol;
 
-  // Gram tile of this warp and the rows it reads
+  // Gram tile of this warp: 8 x 8 of the full 32 x 32, or 4 x 4 of the
+  // bs x bs cross block
   const int ti = warp >> 2, tj = warp & 3;
-  int offi[8], offj[8];
-#pragma unroll
-  for (int a = 0; a < 8; ++a) {
-    offi[a] = s_off[8 * ti + a];
-    offj[a] = s_off[8 * tj + a];
-  }
 
   int sweeps = 0;
   bool converged = (n < 2);
@@ -695,8 +696,17 @@ __global__ void __launch_bounds__(BJ_THREADS) gjacobi_kernel(float* __restrict__
   while (!converged && sweeps < JAC_MAX_SWEEPS) {
     const int par = sweeps & 1;
     for (int step = 0; step < nblk - 1; ++step) {
-      // ---- 1. Gram matrix of the working rows ----
-      {
+      // ---- 1. Gram matrix of the working rows: all of it on the first step
+      // of a sweep, else only the cross block (the two diagonal blocks are
+      // the tracked Gram matrices that came with the rows) ----
+      const bool all_pairs = (step == 0);
+      if (all_pairs) {
+        int offi[8], offj[8];
+#pragma unroll
+        for (int a = 0; a < 8; ++a) {
+          offi[a] = s_off[8 * ti + a];
+          offj[a] = s_off[8 * tj + a];
+        }
         float v[64];
 #pragma unroll
         for (int k = 0; k < 64; ++k) v[k] = 0.f;
@@ -726,6 +736,51 @@ __global__ void __launch_bounds__(BJ_THREADS) gjacobi_kernel(float* __restrict__
         const int a = lane >> 2, b = 2 * (lane & 3);
         sC[0][8 * ti + a][8 * tj + b] = v[0];
         sC[0][8 * ti + a][8 * tj + b + 1] = v[1];
+      } else {
+        int offa[4], offb[4];
+#pragma unroll
+        for (int a = 0; a < 4; ++a) {
+          offa[a] = (4 * ti + a < bs) ? s_off[4 * ti + a] : -1;
+          offb[a] = (4 * tj + a < bs) ? s_off[bs + 4 * tj + a] : -1;
+        }
+        float v[16];
+#pragma unroll
+        for (int k = 0; k < 16; ++k) v[k] = 0.f;
+        for (int e = lane; e < m; e += 32) {
+          float xa[4], xb[4];
+#pragma unroll
+          for (int a = 0; a < 4; ++a) {
+            xa[a] = offa[a] >= 0 ? slots[offa[a] + e] : 0.f;
+            xb[a] = offb[a] >= 0 ? slots[offb[a] + e] : 0.f;
+          }
+#pragma unroll
+          for (int a = 0; a < 4; ++a)
+#pragma unroll
+            for (int b = 0; b < 4; ++b) v[a * 4 + b] = fmaf(xa[a], xb[b], v[a * 4 + b]);
+        }
+        // reduce-scatter to one entry per lane pair (entry lane >> 1), then
+        // the last butterfly completes the sum on both lanes of the pair
+#pragma unroll
+        for (int h = 8, o = 16; o > 1; h >>= 1, o >>= 1) {
+          const bool up = (lane & o) != 0;
+#pragma unroll
+          for (int k = 0; k < h; ++k) {
+            const float send = up ? v[k] : v[k + h];
+            const float keep = up ? v[k + h] : v[k];
+            v[k] = keep + __shfl_xor_sync(0xffffffffu, send, o);
+          }
+        }
+        v[0] += __shfl_xor_sync(0xffffffffu, v[0], 1);
+        const int a = (lane >> 1) >> 2, b = (lane >> 1) & 3;
+        const int ra = 4 * ti + a, rb = 4 * tj + b;
+        if ((lane & 1) == 0 && ra < bs && rb < bs) {
+          sC[0][ra][bs + rb] = v[0];
+          sC[0][bs + rb][ra] = v[0];
+        }
+        for (int idx = tid; idx < 2 * bs * bs; idx += BJ_THREADS) {
+          const int sl = idx / (bs * bs), r = idx % (bs * bs);
+          sC[0][sl * bs + r / bs][sl * bs + r % bs] = slots[(int64_t)sl * slot_tot + slot_elems + r];
+        }
       }
       for (int i = tid; i < GJ_W * GJ_W; i += BJ_THREADS) sQ[i / GJ_W][i % GJ_W] = (i / GJ_W == i % GJ_W) ? 1.f : 0.f;
       if (tid == 0) s_any = 0;
@@ -738,7 +793,6 @@ __global__ void __launch_bounds__(BJ_THREADS) gjacobi_kernel(float* __restrict__
       // local row i with row bs + (i + u) mod bs: bs sub-steps).  Every pair
       // of rows is thus visited once per sweep.
       int cur = 0;
-      const bool all_pairs = (step == 0);
       const int nsub = all_pairs ? weff - 1 : bs;
       auto pair_p = [&](int i, int u) { return all_pairs ? rr_index(i, u, weff) : i; };
       auto pair_q = [&](int i, int u) {
@@ -819,6 +873,11 @@ __global__ void __launch_bounds__(BJ_THREADS) gjacobi_kernel(float* __restrict__
         __syncthreads();
         cur ^= 1;
       }
+      // the diagonal blocks of the rotated Gram matrix travel with the rows
+      for (int idx = tid; idx < 2 * bs * bs; idx += BJ_THREADS) {
+        const int sl = idx / (bs * bs), r = idx % (bs * bs);
+        slots[(int64_t)sl * slot_tot + slot_elems + r] = sC[cur][sl * bs + r / bs][sl * bs + r % bs];
+      }
 
       // ---- 3. apply Q to the working rows ----
       if (s_any) {
@@ -851,17 +910,17 @@ __global__ void __launch_bounds__(BJ_THREADS) gjacobi_kernel(float* __restrict__
         pos_owner(qs, src_cta[sl], src_slot[sl]);
       }
       cluster.sync();
-      const float* r0 = cluster.map_shared_rank(slots, src_cta[0]) + (int64_t)src_slot[0] * slot_elems;
-      const float* r1 = cluster.map_shared_rank(slots, src_cta[1]) + (int64_t)src_slot[1] * slot_elems;
+      const float* r0 = cluster.map_shared_rank(slots, src_cta[0]) + (int64_t)src_slot[0] * slot_tot;
+      const float* r1 = cluster.map_shared_rank(slots, src_cta[1]) + (int64_t)src_slot[1] * slot_tot;
       const int nb0 = *cluster.map_shared_rank(&s_blk[src_slot[0]], src_cta[0]);
       const int nb1 = *cluster.map_shared_rank(&s_blk[src_slot[1]], src_cta[1]);
-      const int n4 = slot_elems * (int)sizeof(float) / 16;
+      const int n4 = slot_tot * (int)sizeof(float) / 16;
       const uint4* s0 = reinterpret_cast<const uint4*>(r0);
       const uint4* s1 = reinterpret_cast<const uint4*>(r1);
       uint4* st4 = reinterpret_cast<uint4*>(stage);
-      uint4 regs[BJ_MAX_SLOT_BYTES / 16 / BJ_THREADS];
+      uint4 regs[GJ_MOVE_REGS];
 #pragma unroll
-      for (int j = 0; j < BJ_MAX_SLOT_BYTES / 16 / BJ_THREADS; ++j) {
+      for (int j = 0; j < GJ_MOVE_REGS; ++j) {
         const int idx = tid + j * BJ_THREADS;
         if (idx < n4) {
           st4[idx] = s0[idx];
@@ -870,9 +929,9 @@ __global__ void __launch_bounds__(BJ_THREADS) gjacobi_kernel(float* __restrict__
       }
       cluster.sync();
       uint4* d0 = reinterpret_cast<uint4*>(slots);
-      uint4* d1 = reinterpret_cast<uint4*>(slots + slot_elems);
+      uint4* d1 = reinterpret_cast<uint4*>(slots + slot_tot);
 #pragma unroll
-      for (int j = 0; j < BJ_MAX_SLOT_BYTES / 16 / BJ_THREADS; ++j) {
+      for (int j = 0; j < GJ_MOVE_REGS; ++j) {
         const int idx = tid + j * BJ_THREADS;
         if (idx < n4) {
           d0[idx] = st4[idx];
@@ -902,7 +961,7 @@ __global__ void __launch_bounds__(BJ_THREADS) gjacobi_kernel(float* __restrict__
       for (int r = warp; r < bs; r += BJ_WARPS) {
         const int gr = blk * bs + r;
         if (gr >= n) continue;
-        const float* row = slots + (int64_t)sl * slot_elems + (int64_t)r * row_len;
+        const float* row = slots + (int64_t)sl * slot_tot + (int64_t)r * row_len;
         float acc = 0.f;
         for (int e = lane; e < m; e += 32) acc = fmaf(row[e], row[e], acc);
         acc = wsum_t(acc);
@@ -920,7 +979,7 @@ __global__ void __launch_bounds__(BJ_THREADS) gjacobi_kernel(float* __restrict__
       for (int r = warp; r < bs; r += BJ_WARPS) {
         const int gr = blk * bs + r;
         if (gr >= n) continue;
-        const float* row = slots + (int64_t)sl * slot_elems + (int64_t)r * row_len;
+        const float* row = slots + (int64_t)sl * slot_tot + (int64_t)r * row_len;
         float acc = 0.f;
         for (int e = lane; e < m; e += 32) acc = fmaf(row[e], row[e], acc);
         acc = wsum_t(acc);
@@ -938,14 +997,14 @@ __global__ void __launch_bounds__(BJ_THREADS) gjacobi_kernel(float* __restrict__
       const int r = (int)(i / row_len), e = (int)(i % row_len);
       const int gr = blk * bs + r;
       if (gr >= n) continue;
-      const float v = slots[(int64_t)sl * slot_elems + i];
+      const float v = slots[(int64_t)sl * slot_tot + i];
       if (e < m) G[(int64_t)gr * ldg + e] = v;
       else Vt[(int64_t)gr * ldv + (e - m)] = v;
     }
     for (int r = warp; r < bs; r += BJ_WARPS) {
       const int gr = blk * bs + r;
       if (gr >= n) continue;
-      const float* row = slots + (int64_t)sl * slot_elems + (int64_t)r * row_len;
+      const float* row = slots + (int64_t)sl * slot_tot + (int64_t)r * row_len;
       float acc = 0.f;
       for (int e = lane; e < m; e += 32) acc = fmaf(row[e], row[e], acc);
       acc = wsum_t(acc);
@@ -1057,13 +1116,14 @@ static int launch_gjacobi(cudaStream_t st, float* G, int64_t ldg, float* Vt, int
   auto kern = gjacobi_kernel<MODE>;
   if (!attr_done) {
     SGT_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeNonPortableClusterSizeAllowed, 1));
-    SGT_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, 3 * BJ_MAX_SLOT_BYTES));
+    SGT_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, 3 * GJ_SLOT_CAP));
     attr_done = true;
   }
+  const int64_t gram_bytes = ((bsz * bsz + 3) & ~int64_t(3)) * (int64_t)sizeof(float);
   cudaLaunchConfig_t cfg = {};
   cfg.gridDim = dim3(csb, 1, 1);
   cfg.blockDim = dim3(BJ_THREADS, 1, 1);
-  cfg.dynamicSmemBytes = (size_t)3 * slot_bytes;
+  cfg.dynamicSmemBytes = (size_t)3 * (slot_bytes + gram_bytes);
   cfg.stream = st;
   cudaLaunchAttribute attr[1];
   attr[0].id = cudaLaunchAttributeClusterDimension;
