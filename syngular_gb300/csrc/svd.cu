@@ -93,6 +93,22 @@ __device__ __forceinline__ bool jacobi_rotation(T a, T b, T c, double tol, doubl
   }
 }
 
+// FP32 rotation of the Gram-form kernel: as jacobi_rotation<float>, plus the
+// tangent (no division for it), cs from the correctly rounded reciprocal
+// square root (one operation instead of a square root and a division).
+__device__ __forceinline__ bool rot_f32(float a, float b, float c, float tol, float abs_floor, float& cs_,
+                                        float& sn, float& tau, float& tn) {
+  if (!(fabsf(c) > tol * sqrtf(a) * sqrtf(b) && fabsf(c) > abs_floor)) return false;
+  const float zeta = __fdividef(b - a, 2.f * c);
+  const float t = __fdividef(copysignf(1.f, zeta), fabsf(zeta) + sqrtf(fmaf(zeta, zeta, 1.f)));
+  const float cf = __frsqrt_rn(fmaf(t, t, 1.f));
+  cs_ = cf;
+  sn = cf * t;
+  tau = __fdividef(sn, 1.f + cf);
+  tn = t;
+  return true;
+}
+
 // T = double: plain FP64.  T = float: the column data and dot products are
 // FP32 (warp-shuffle trees); the rotation angle is still formed in FP64.
 template <typename T>
@@ -453,13 +469,14 @@ __global__ void __launch_bounds__(BJ_THREADS) gjacobi_kernel(float* __restrict__
                                                              float* __restrict__ Vt, int64_t ldv, int n, int m,
                                                              int bs, double tol, float* __restrict__ norms,
                                                              int* __restrict__ status,
-                                                             const int* __restrict__ perm) {
+                                                             const int* __restrict__ perm,
+                                                             float* __restrict__ qlog, int* __restrict__ blog) {
   cg::cluster_group cluster = cg::this_cluster();
   const int cs = (int)cluster.num_blocks();
   const int rank = (int)cluster.block_rank();
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const int nblk = 2 * cs;
-  const int row_len = (MODE == 2) ? m : m + n;  // G part then Vt part
+  const int row_len = (MODE == 1 || MODE == 2) ? m : m + n;  // G part then Vt part
   const int slot_elems = bs * row_len;
   // each slot: bs rows, then the bs x bs Gram matrix of those rows as tracked
   // through the rotations (it travels with the rows)
@@ -796,7 +813,10 @@ __global__ void __launch_bounds__(BJ_THREADS) gjacobi_kernel(float* __restrict__
       const int nsub = all_pairs ? weff - 1 : bs;
       auto pair_p = [&](int i, int u) { return all_pairs ? rr_index(i, u, weff) : i; };
       auto pair_q = [&](int i, int u) {
-        if (!all_pairs) return bs + (i + u) % bs;
+        if (!all_pairs) {
+          const int t = i + u;
+          return bs + (t >= bs ? t - bs : t);
+        }
         return rr_index(weff - 1 - i, u, weff);
       };
       for (int sub = 0; sub < nsub; ++sub) {
@@ -810,13 +830,13 @@ __global__ void __launch_bounds__(BJ_THREADS) gjacobi_kernel(float* __restrict__
             pj = pair_p(lane, sub);
             qj = pair_q(lane, sub);
             const float a = fmaxf(sC[cur][pj][pj], 0.f), b = fmaxf(sC[cur][qj][qj], 0.f), c = sC[cur][pj][qj];
-            float c_, s_, t_;
-            if (jacobi_rotation<float>(a, b, c, (double)ftol, (double)abs_floor, lane, c_, s_, t_)) {
+            float c_, s_, t_, tn_;
+            if (rot_f32(a, b, c, ftol, abs_floor, c_, s_, t_, tn_)) {
               rj = 1;
               cj = c_;
               sj = s_;
               tj_ = t_;
-              tanj = s_ / c_;
+              tanj = tn_;
             }
           }
           const int ri = __shfl_sync(0xffffffffu, rj, i);
@@ -877,6 +897,18 @@ __global__ void __launch_bounds__(BJ_THREADS) gjacobi_kernel(float* __restrict__
       for (int idx = tid; idx < 2 * bs * bs; idx += BJ_THREADS) {
         const int sl = idx / (bs * bs), r = idx % (bs * bs);
         slots[(int64_t)sl * slot_tot + slot_elems + r] = sC[cur][sl * bs + r / bs][sl * bs + r % bs];
+      }
+      if constexpr (MODE == 1) {
+        // log Q and the two block ids (-1: no rotation) for gj_replay_kernel
+        const int64_t ls = ((int64_t)sweeps * (nblk - 1) + step) * cs + rank;
+        if (s_any) {
+          float4* qd = reinterpret_cast<float4*>(qlog + ls * (GJ_W * GJ_W));
+          for (int i = tid; i < GJ_W * GJ_W / 4; i += BJ_THREADS) qd[i] = reinterpret_cast<const float4*>(&sQ[0][0])[i];
+        }
+        if (tid == 0) {
+          blog[2 * ls] = s_any ? s_blk[0] : -1;
+          blog[2 * ls + 1] = s_blk[1];
+        }
       }
 
       // ---- 3. apply Q to the working rows ----
@@ -1015,6 +1047,80 @@ __global__ void __launch_bounds__(BJ_THREADS) gjacobi_kernel(float* __restrict__
   cluster.sync();
 }
 
+// Vt = (the logged rotations of gjacobi_kernel<1>, in order) applied to I.
+// Columns of Vt transform independently under row rotations, so each CTA
+// replays the whole log on a slice of RP_COLS columns held in shared memory
+// (all 2 cs bs block rows) and needs no other CTA.  Per logged step it loads
+// the cs rotation matrices, computes every working row of every rotated block
+// pair into registers, then writes them back.
+constexpr int RP_COLS = 8, RP_THREADS = 256;
+
+__global__ void __launch_bounds__(RP_THREADS) gj_replay_kernel(const float* __restrict__ qlog,
+                                                               const int* __restrict__ blog,
+                                                               const int* __restrict__ status, int n, int cs, int bs,
+                                                               float* __restrict__ Vt, int64_t ldv) {
+  extern __shared__ __align__(16) float rp_smem[];
+  const int nrows = 2 * cs * bs, weff = 2 * bs;
+  float* V = rp_smem;                   // [nrows][RP_COLS]
+  float* Qs = V + nrows * RP_COLS;      // [cs][GJ_W][GJ_W]
+  __shared__ int s_b[2 * 16];
+  const int c0 = blockIdx.x * RP_COLS, tid = threadIdx.x;
+  for (int i = tid; i < nrows * RP_COLS; i += RP_THREADS) V[i] = (i / RP_COLS == c0 + i % RP_COLS) ? 1.f : 0.f;
+  const int st = *status;
+  const int sweeps = st > 0 ? st : (st < 0 ? JAC_MAX_SWEEPS : 0);
+  const int64_t nsteps = (int64_t)sweeps * (2 * cs - 1);
+  const int tasks = cs * weff;  // (pair, working row)
+  for (int64_t ls = 0; ls < nsteps; ++ls) {
+    __syncthreads();
+    if (tid < 2 * cs) s_b[tid] = blog[ls * cs * 2 + tid];
+    const float4* src = reinterpret_cast<const float4*>(qlog + ls * cs * (GJ_W * GJ_W));
+    for (int i = tid; i < cs * GJ_W * GJ_W / 4; i += RP_THREADS) reinterpret_cast<float4*>(Qs)[i] = src[i];
+    __syncthreads();
+    float out[2][RP_COLS];
+    int orow[2];
+#pragma unroll
+    for (int k = 0; k < 2; ++k) {
+      orow[k] = -1;
+      const int t = tid + k * RP_THREADS;
+      if (t >= tasks) continue;
+      const int c = t / weff, r = t % weff;
+      const int A = s_b[2 * c], B = s_b[2 * c + 1];
+      if (A < 0) continue;
+      const float* q = Qs + (c * GJ_W + r) * GJ_W;
+#pragma unroll
+      for (int u = 0; u < RP_COLS; ++u) out[k][u] = 0.f;
+      for (int j = 0; j < weff; ++j) {
+        const float qj = q[j];
+        const int vr = (j < bs) ? A * bs + j : B * bs + (j - bs);
+        const float4 v0 = *reinterpret_cast<const float4*>(V + vr * RP_COLS);
+        const float4 v1 = *reinterpret_cast<const float4*>(V + vr * RP_COLS + 4);
+        out[k][0] = fmaf(qj, v0.x, out[k][0]);
+        out[k][1] = fmaf(qj, v0.y, out[k][1]);
+        out[k][2] = fmaf(qj, v0.z, out[k][2]);
+        out[k][3] = fmaf(qj, v0.w, out[k][3]);
+        out[k][4] = fmaf(qj, v1.x, out[k][4]);
+        out[k][5] = fmaf(qj, v1.y, out[k][5]);
+        out[k][6] = fmaf(qj, v1.z, out[k][6]);
+        out[k][7] = fmaf(qj, v1.w, out[k][7]);
+      }
+      orow[k] = (r < bs) ? A * bs + r : B * bs + (r - bs);
+    }
+    __syncthreads();
+#pragma unroll
+    for (int k = 0; k < 2; ++k) {
+      if (orow[k] < 0) continue;
+      float4* d = reinterpret_cast<float4*>(V + orow[k] * RP_COLS);
+      d[0] = make_float4(out[k][0], out[k][1], out[k][2], out[k][3]);
+      d[1] = make_float4(out[k][4], out[k][5], out[k][6], out[k][7]);
+    }
+  }
+  __syncthreads();
+  for (int i = tid; i < n * RP_COLS; i += RP_THREADS) {
+    const int r = i / RP_COLS, c = c0 + i % RP_COLS;
+    if (c < n) Vt[(int64_t)r * ldv + c] = V[i];
+  }
+}
+
 template <typename T>
 __global__ void eye_rows_kernel(T* Vt, int64_t ldv, int n) {
   for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < (int64_t)n * n;
@@ -1102,15 +1208,21 @@ size_t jacobi_rows_ws_bytes_f32(int64_t n, int64_t m) { return jacobi_rows_ws_by
 // Launch gjacobi_kernel<MODE> when its cluster layout fits (n in [64, 512],
 // blocks of <= 16 rows, slots within the shared-memory budget and a cluster
 // of that size schedulable); *launched reports whether it was.
-template <int MODE>
-static int launch_gjacobi(cudaStream_t st, float* G, int64_t ldg, float* Vt, int64_t ldv, int64_t n, int64_t m,
-                          float* norms, int* status, const int* perm, bool* launched) {
-  *launched = false;
-  if (n < 64 || n > 16 * GJ_W || (MODE >= 2 && m != n)) return SGT_OK;
+static int gj_cluster(int64_t n) {
   int csb = 2;
   while (csb < 16 && cdiv(n, 2 * csb) > GJ_W / 2) csb *= 2;
+  return csb;
+}
+
+template <int MODE>
+static int launch_gjacobi(cudaStream_t st, float* G, int64_t ldg, float* Vt, int64_t ldv, int64_t n, int64_t m,
+                          float* norms, int* status, const int* perm, bool* launched, float* qlog = nullptr,
+                          int* blog = nullptr) {
+  *launched = false;
+  if (n < 64 || n > 16 * GJ_W || (MODE >= 2 && m != n)) return SGT_OK;
+  const int csb = gj_cluster(n);
   const int64_t bsz = cdiv(n, 2 * csb);
-  const int64_t slot_bytes = bsz * (MODE == 2 ? m : m + n) * (int64_t)sizeof(float);
+  const int64_t slot_bytes = bsz * ((MODE == 1 || MODE == 2) ? m : m + n) * (int64_t)sizeof(float);
   if (bsz > GJ_W / 2 || slot_bytes > BJ_MAX_SLOT_BYTES || slot_bytes % 16 != 0) return SGT_OK;
   static bool attr_done = false;
   auto kern = gjacobi_kernel<MODE>;
@@ -1138,7 +1250,7 @@ static int launch_gjacobi(cudaStream_t st, float* G, int64_t ldg, float* Vt, int
     return SGT_OK;
   }
   SGT_CUDA(cudaLaunchKernelEx(&cfg, kern, G, ldg, Vt, ldv, (int)n, (int)m, (int)bsz, jacobi_tol<float>(m), norms,
-                              status, perm));
+                              status, perm, qlog, blog));
   note_launch();
   *launched = true;
   return SGT_OK;
@@ -1297,17 +1409,62 @@ __global__ void diag_order_kernel(const float* __restrict__ Z, int64_t ldz, int 
 
 }  // namespace
 
+// Rotation log of gjacobi_kernel<1>: one 32 x 32 matrix and two block ids
+// per CTA per outer step, for the sweep cap.
+static size_t gj_log_floats(int64_t n) {
+  const int cs = gj_cluster(n);
+  return (size_t)JAC_MAX_SWEEPS * (2 * cs - 1) * cs * GJ_W * GJ_W;
+}
+static size_t gj_log_ints(int64_t n) {
+  const int cs = gj_cluster(n);
+  return (size_t)JAC_MAX_SWEEPS * (2 * cs - 1) * cs * 2;
+}
+
+// Monotone in n: a workspace sized for the largest bond problem of a chain
+// also serves its smaller ones.
 size_t sym_eig_rows_ws_bytes(int64_t n) {
   Arena a = Arena::measuring();
   a.take<int>((size_t)n);  // diagonal order
+  if (n >= 64) {
+    const int64_t nl = std::min<int64_t>(n, 16 * GJ_W);
+    a.take<float>(gj_log_floats(nl));
+    a.take<int>(gj_log_ints(nl));
+  }
   return a.used + jacobi_rows_ws_bytes_t<float>(n, n);
 }
 
 int sym_eig_rows_f32(cudaStream_t st, float* Z, int64_t n, float* Vt, float* lam, int* status, Arena& ar,
                      int method) {
-  if ((method != 2 && method != 3) || n < 64 || n > 16 * GJ_W)
+  if (method < 1 || method > 3 || n < 64 || n > 16 * GJ_W)
     return jacobi_rows_f32(st, Z, n, n, n, Vt, n, lam, status, ar);
-  Arena ar0 = ar;  // for the fallback below, which needs none of the buffers taken here
+  Arena ar0 = ar;  // for the fallbacks below, which need none of the buffers taken here
+  if (method == 1) {
+    // rows of Z only in shared memory; the rotations are logged and replayed
+    // on Vt = I afterwards by all SMs (columns of Vt are independent)
+    float* qlog = ar.take<float>(gj_log_floats(n));
+    int* blog = ar.take<int>(gj_log_ints(n));
+    float* Gtmp = ar.take<float>((size_t)n * n);
+    float* Vtmp = ar.take<float>((size_t)n * n);
+    float* norms = ar.take<float>((size_t)n);
+    int* perm = ar.take<int>((size_t)n);
+    SGT_REQUIRE(ar.ok(), SGT_ERR_WORKSPACE, "sym_eig: workspace too small");
+    bool launched = false;
+    SGT_TRY(launch_gjacobi<1>(st, Z, n, Vt, n, n, n, norms, status, nullptr, &launched, qlog, blog));
+    if (!launched) return jacobi_rows_f32(st, Z, n, n, n, Vt, n, lam, status, ar0);
+    const int cs = gj_cluster(n);
+    const int bsz = (int)cdiv(n, 2 * cs);
+    const size_t smem = sizeof(float) * ((size_t)2 * cs * bsz * RP_COLS + (size_t)cs * GJ_W * GJ_W);
+    static bool rp_attr = false;
+    if (!rp_attr) {
+      SGT_CUDA(cudaFuncSetAttribute(gj_replay_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                    (int)(sizeof(float) * ((size_t)2 * 16 * (GJ_W / 2) * RP_COLS + 16 * GJ_W * GJ_W))));
+      rp_attr = true;
+    }
+    gj_replay_kernel<<<(unsigned)cdiv(n, RP_COLS), RP_THREADS, smem, st>>>(qlog, blog, status, (int)n, cs, bsz, Vt, n);
+    SGT_LAUNCHED();
+    SGT_TRY(sort_rows_t<float>(st, Z, n, n, n, Vt, n, lam, norms, perm, Gtmp, Vtmp));
+    return SGT_OK;
+  }
   int* order = ar.take<int>((size_t)n);
   float* Gtmp = ar.take<float>((size_t)n * n);
   float* Vtmp = ar.take<float>((size_t)n * n);
