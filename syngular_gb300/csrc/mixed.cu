@@ -177,15 +177,17 @@ __global__ void set_one_kernel(float* hi, float* lo) {
   lo[0] = 0.f;
 }
 
-// Eigenvalues lam (descending, = s of the Jacobi SVD of Z): spectra = sqrt(lam),
-// discarded = sum_{j >= keep} lam_j / sum lam_j.
+// Eigenvalues lam (descending) of Z_k, whose left Gram factor was scaled by
+// 2^-gexp: spectra = sqrt(lam 2^gexp), discarded = sum_{j >= keep} lam_j / sum lam_j.
 __global__ void gram_spectrum_kernel(const float* __restrict__ lam, int count, int keep,
-                                     double* __restrict__ spec_out, double* __restrict__ disc_out) {
+                                     double* __restrict__ spec_out, double* __restrict__ disc_out,
+                                     const int* __restrict__ gexp) {
   __shared__ double red[2][32];
   double tot = 0.0, drop = 0.0;
+  const int ge = gexp ? *gexp : 0;
   for (int j = threadIdx.x; j < count; j += blockDim.x) {
     double v = fmax((double)lam[j], 0.0);
-    if (spec_out) spec_out[j] = sqrt(v);
+    if (spec_out) spec_out[j] = sqrt(ldexp(v, ge));
     tot += v;
     if (j >= keep) drop += v;
   }
@@ -199,6 +201,35 @@ __global__ void gram_spectrum_kernel(const float* __restrict__ lam, int count, i
     double t = 0.0, d = 0.0;
     for (int w = 0; w < (int)(blockDim.x >> 5); ++w) t += red[0][w], d += red[1][w];
     if (disc_out) *disc_out = (t > 0.0) ? d / t : 0.0;
+  }
+}
+
+// max |x| as the bit pattern of a non-negative float (ordered like the value)
+__global__ void absmax_bits_kernel(const float* __restrict__ x, int64_t n, unsigned* __restrict__ out) {
+  float m = 0.f;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+    m = fmaxf(m, fabsf(x[i]));
+  for (int o = 16; o > 0; o >>= 1) m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, o));
+  if ((threadIdx.x & 31) == 0 && m > 0.f) atomicMax(out, __float_as_uint(m));
+}
+
+// x 2^-e split into TF32 hi / FP32 lo, e = the binary exponent of max |x|
+// (exact scaling: keeps the FP32 Gram recursion of long chains in range);
+// gexp_next = gexp_prev + e.
+__global__ void split_scaled_kernel(const float* __restrict__ x, float* __restrict__ hi, float* __restrict__ lo,
+                                    int64_t n, const unsigned* __restrict__ maxbits,
+                                    const int* __restrict__ gexp_prev, int* __restrict__ gexp_next) {
+  const float m = __uint_as_float(*maxbits);
+  int e = 0;
+  if (m > 0.f && isfinite(m)) frexpf(m, &e);
+  if (blockIdx.x == 0 && threadIdx.x == 0) *gexp_next = *gexp_prev + e;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    const float v = ldexpf(x[i], -e);
+    uint32_t h;
+    asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(h) : "f"(v));
+    const float fh = __uint_as_float(h);
+    hi[i] = fh;
+    lo[i] = v - fh;
   }
 }
 
@@ -345,6 +376,8 @@ static int mixed_round_impl(cudaStream_t st, int n, const double* const* W, cons
   double* Sd = ar.take<double>(chi * chi);
   int* stat = ar.take<int>(n + 1);
   int* tc_err = ar.take<int>(1);
+  int* gexp = ar.take<int>(n + 1);
+  unsigned* gmax = ar.take<unsigned>(1);
   const size_t jbytes = std::max(std::max(jacobi_rows_ws_bytes_f32(cmax, cmax), sym_eig_ws_bytes(cmax)),
                                  sym_eig_rows_ws_bytes(cmax));
   char* jscratch = ar.take<char>(jbytes);
@@ -352,6 +385,16 @@ static int mixed_round_impl(cudaStream_t st, int n, const double* const* W, cons
   SGT_REQUIRE(ar.ok(), SGT_ERR_WORKSPACE, "mpo_mps_round: workspace too small");
   SGT_CUDA(cudaMemsetAsync(stat, 0, sizeof(int) * (n + 1), st));
   SGT_CUDA(cudaMemsetAsync(tc_err, 0, sizeof(int), st));
+  SGT_CUDA(cudaMemsetAsync(gexp, 0, sizeof(int) * (n + 1), st));
+  // G_{k+1} (in Gacc) -> power-of-two scaled hi / lo, exponent into gexp[k + 1]
+  auto split_gram = [&](int k, int64_t count) -> int {
+    SGT_CUDA(cudaMemsetAsync(gmax, 0, sizeof(unsigned), st));
+    absmax_bits_kernel<<<gs(count), 256, 0, st>>>(Gacc, count, gmax);
+    SGT_LAUNCHED();
+    split_scaled_kernel<<<gs(count), 256, 0, st>>>(Gacc, Gh[k + 1], Gl[k + 1], count, gmax, gexp + k, gexp + k + 1);
+    SGT_LAUNCHED();
+    return SGT_OK;
+  };
 
   // ---- product cores in both layouts ----
   for (int k = 0; k < n; ++k) {
@@ -374,7 +417,7 @@ static int mixed_round_impl(cudaStream_t st, int n, const double* const* W, cons
   for (int k = 0; structured && k + 1 < n; ++k) {
     SGT_TRY(gram_step_structured(st, passes, Gh[k], Gl[k], X[k], xs[3 * k], xs[3 * k + 1], xs[3 * k + 2], W[k],
                                  w[k].b, w[k].o, w[k].b2, Gacc, gsc, tc_err));
-    SGT_TRY(split_tf32(st, Gacc, Gh[k + 1], Gl[k + 1], R[k + 1] * R[k + 1]));
+    SGT_TRY(split_gram(k, R[k + 1] * R[k + 1]));
   }
   for (int k = 0; !structured && k + 1 < n; ++k) {
     const int64_t r = R[k], r2 = R[k + 1];
@@ -388,7 +431,7 @@ static int mixed_round_impl(cudaStream_t st, int n, const double* const* W, cons
       SGT_TRY(gemm_nt_dispatch(st, passes, r2, r2, r, 1.f, Ah, Al, r, Hth, Htl, r, pi == 0 ? 0.f : 1.f, Gacc, r2,
                       tc_err));
     }
-    SGT_TRY(split_tf32(st, Gacc, Gh[k + 1], Gl[k + 1], r2 * r2));
+    SGT_TRY(split_gram(k, r2 * r2));
   }
   // ---- right-to-left projection and eigen-solves ----
   set_one_kernel<<<1, 1, 0, st>>>(Fth, Ftl);
@@ -441,7 +484,7 @@ static int mixed_round_impl(cudaStream_t st, int n, const double* const* W, cons
       spec_k = spectra + off;
     }
     gram_spectrum_kernel<<<1, 256, 0, st>>>(lam, (int)cnt[k], (int)keep, spec_k,
-                                            discarded ? discarded + (k - 1) : nullptr);
+                                            discarded ? discarded + (k - 1) : nullptr, gexp + k);
     SGT_LAUNCHED();
     // Ft_k (keep x r) = Vt[:keep] Y^T with Y = Yt^T (r x c)
     SGT_TRY(transpose_f32(st, Y, c, 0, Yt, r, 0, c, r, 1));

@@ -29,12 +29,6 @@ constexpr int JAC_MAX_SWEEPS = 60;
 
 namespace {
 
-__device__ __forceinline__ double wsum(double v) {
-#pragma unroll
-  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
-  return v;
-}
-
 __device__ __forceinline__ int rr_index(int i, int s, int np) {
   // circle method: position 0 fixed, the others rotate by s
   return i == 0 ? 0 : ((i - 1 + s) % (np - 1)) + 1;
@@ -93,18 +87,28 @@ __device__ __forceinline__ bool jacobi_rotation(T a, T b, T c, double tol, doubl
   }
 }
 
-// FP32 rotation of the Gram-form kernel: as jacobi_rotation<float>, plus the
-// tangent (no division for it), cs from the correctly rounded reciprocal
-// square root (one operation instead of a square root and a division).
-__device__ __forceinline__ bool rot_f32(float a, float b, float c, float tol, float abs_floor, float& cs_,
-                                        float& sn, float& tau, float& tn) {
-  if (!(fabsf(c) > tol * sqrtf(a) * sqrtf(b) && fabsf(c) > abs_floor)) return false;
+// Low-latency FP32 rotation for the Gram-form kernel's inner sweep, where the
+// dependent chain of one sub-step is the critical path: square roots and
+// quotients from the hardware reciprocal (square root) estimates, which only
+// choose the angle; cs = 1 / sqrt(1 + t^2) from the estimate plus one Newton
+// step y (3/2 - u y^2 / 2), so that cs^2 (1 + t^2) = 1 to about an ulp without
+// a systematic bias (a bias would drift the row norms over the thousands of
+// rotations a row sees).
+__device__ __forceinline__ bool rot_fast(float a, float b, float c, float tol, float abs_floor, float& cs_,
+                                         float& sn, float& tau, float& tn) {
+  const float sa = a * rsqrtf(a), sb = b * rsqrtf(b);  // a or b = 0: NaN, no rotation (c is 0 there)
+  if (!(fabsf(c) > tol * sa * sb && fabsf(c) > abs_floor)) return false;
   const float zeta = __fdividef(b - a, 2.f * c);
-  const float t = __fdividef(copysignf(1.f, zeta), fabsf(zeta) + sqrtf(fmaf(zeta, zeta, 1.f)));
-  const float cf = __frsqrt_rn(fmaf(t, t, 1.f));
-  cs_ = cf;
-  sn = cf * t;
-  tau = __fdividef(sn, 1.f + cf);
+  const float az = fabsf(zeta);
+  const float q = fmaf(zeta, zeta, 1.f);
+  const float sq = (az > 1e18f) ? az : q * rsqrtf(q);
+  const float t = __fdividef(copysignf(1.f, zeta), az + sq);
+  const float u = fmaf(t, t, 1.f);
+  float y = rsqrtf(u);
+  y = y * fmaf(-0.5f * u, y * y, 1.5f);
+  cs_ = y;
+  sn = y * t;
+  tau = __fdividef(sn, 1.f + y);
   tn = t;
   return true;
 }
@@ -821,17 +825,20 @@ __global__ void __launch_bounds__(BJ_THREADS) gjacobi_kernel(float* __restrict__
       };
       for (int sub = 0; sub < nsub; ++sub) {
         if (warp < bs) {
+          // warp i: the rows p_i, q_i of C (2 x 32 entries: lane l holds block
+          // (i, l / 2), row p_i or q_i by the parity of l) and of Q (lane = column)
           const int i = warp;
           const int pi = pair_p(i, sub), qi = pair_q(i, sub);
-          // lane j < bs: the rotation of pair j
+          const int j = lane >> 1, half = lane & 1;
+          // the rotation of pair j, on lanes 2j and 2j + 1
           float cj = 1.f, sj = 0.f, tj_ = 0.f, tanj = 0.f;
           int rj = 0, pj = 0, qj = 0;
-          if (lane < bs) {
-            pj = pair_p(lane, sub);
-            qj = pair_q(lane, sub);
+          if (j < bs) {
+            pj = pair_p(j, sub);
+            qj = pair_q(j, sub);
             const float a = fmaxf(sC[cur][pj][pj], 0.f), b = fmaxf(sC[cur][qj][qj], 0.f), c = sC[cur][pj][qj];
             float c_, s_, t_, tn_;
-            if (rot_f32(a, b, c, ftol, abs_floor, c_, s_, t_, tn_)) {
+            if (rot_fast(a, b, c, ftol, abs_floor, c_, s_, t_, tn_)) {
               rj = 1;
               cj = c_;
               sj = s_;
@@ -839,55 +846,48 @@ __global__ void __launch_bounds__(BJ_THREADS) gjacobi_kernel(float* __restrict__
               tanj = tn_;
             }
           }
-          const int ri = __shfl_sync(0xffffffffu, rj, i);
-          const float ci = __shfl_sync(0xffffffffu, cj, i), si = __shfl_sync(0xffffffffu, sj, i);
-          const float taui = __shfl_sync(0xffffffffu, tj_, i), tani = __shfl_sync(0xffffffffu, tanj, i);
+          const int ri = __shfl_sync(0xffffffffu, rj, 2 * i);
+          const float si = __shfl_sync(0xffffffffu, sj, 2 * i);
+          const float taui = __shfl_sync(0xffffffffu, tj_, 2 * i), tani = __shfl_sync(0xffffffffu, tanj, 2 * i);
+          (void)cj;
           const int nxt = cur ^ 1;
-          if (lane < bs) {
-            float xpp = sC[cur][pi][pj], xpq = sC[cur][pi][qj], xqp = sC[cur][qi][pj], xqq = sC[cur][qi][qj];
-            if (lane == i) {
+          if (j < bs) {
+            const float xpp = sC[cur][pi][pj], xpq = sC[cur][pi][qj], xqp = sC[cur][qi][pj], xqq = sC[cur][qi][qj];
+            float o0, o1;  // this lane's row (p_i or q_i) at columns p_j and q_j
+            if (j == i) {
               if (ri) {
-                ++my_rot;
-                s_any = 1;
-                const float c = xpq;
-                xpp = xpp - tani * c;
-                xqq = xqq + tani * c;
-                xpq = 0.f;
-                xqp = 0.f;
+                o0 = half ? 0.f : xpp - tani * xpq;
+                o1 = half ? xqq + tani * xpq : 0.f;
+              } else {
+                o0 = half ? xqp : xpp;
+                o1 = half ? xqq : xpq;
               }
             } else {
+              float rp = half ? xqp : xpp, rq = half ? xqq : xpq;
               if (ri) {  // rows p_i, q_i
-                const float a0 = xpp - si * (xqp + taui * xpp), b0 = xqp + si * (xpp - taui * xqp);
-                const float a1 = xpq - si * (xqq + taui * xpq), b1 = xqq + si * (xpq - taui * xqq);
-                xpp = a0;
-                xqp = b0;
-                xpq = a1;
-                xqq = b1;
+                rp = half ? xqp + si * (xpp - taui * xqp) : xpp - si * (xqp + taui * xpp);
+                rq = half ? xqq + si * (xpq - taui * xqq) : xpq - si * (xqq + taui * xpq);
               }
               if (rj) {  // columns p_j, q_j
-                const float a0 = xpp - sj * (xpq + tj_ * xpp), b0 = xpq + sj * (xpp - tj_ * xpq);
-                const float a1 = xqp - sj * (xqq + tj_ * xqp), b1 = xqq + sj * (xqp - tj_ * xqq);
-                xpp = a0;
-                xpq = b0;
-                xqp = a1;
-                xqq = b1;
+                o0 = rp - sj * (rq + tj_ * rp);
+                o1 = rq + sj * (rp - tj_ * rq);
+              } else {
+                o0 = rp;
+                o1 = rq;
               }
             }
-            sC[nxt][pi][pj] = xpp;
-            sC[nxt][pi][qj] = xpq;
-            sC[nxt][qi][pj] = xqp;
-            sC[nxt][qi][qj] = xqq;
-          } else if (lane >= 16 && ri) {
-            // rows p_i, q_i of Q, columns u and u + 16
-#pragma unroll
-            for (int h = 0; h < 2; ++h) {
-              const int e = (lane - 16) + 16 * h;
-              if (e < weff) {
-                const float x = sQ[pi][e], y = sQ[qi][e];
-                sQ[pi][e] = x - si * (y + taui * x);
-                sQ[qi][e] = y + si * (x - taui * y);
-              }
-            }
+            const int rr = half ? qi : pi;
+            sC[nxt][rr][pj] = o0;
+            sC[nxt][rr][qj] = o1;
+          }
+          if (ri && lane < weff) {
+            const float x = sQ[pi][lane], y = sQ[qi][lane];
+            sQ[pi][lane] = x - si * (y + taui * x);
+            sQ[qi][lane] = y + si * (x - taui * y);
+          }
+          if (ri && lane == 2 * i) {
+            ++my_rot;
+            s_any = 1;
           }
         }
         __syncthreads();
@@ -1050,10 +1050,13 @@ __global__ void __launch_bounds__(BJ_THREADS) gjacobi_kernel(float* __restrict__
 // Vt = (the logged rotations of gjacobi_kernel<1>, in order) applied to I.
 // Columns of Vt transform independently under row rotations, so each CTA
 // replays the whole log on a slice of RP_COLS columns held in shared memory
-// (all 2 cs bs block rows) and needs no other CTA.  Per logged step it loads
-// the cs rotation matrices, computes every working row of every rotated block
-// pair into registers, then writes them back.
-constexpr int RP_COLS = 8, RP_THREADS = 256;
+// (all 2 cs bs block rows) and needs no other CTA.  Per logged step it reads
+// the block ids, loads the rotation matrices of the pairs that rotated (row
+// stride padded to 36 floats: the 16-byte loads of the 8 rows a quarter-warp
+// reads fall in distinct banks), computes every working row of those pairs
+// into registers and writes them back; steps without rotations cost two
+// barriers.
+constexpr int RP_COLS = 8, RP_THREADS = 256, RP_QS = GJ_W + 4;
 
 __global__ void __launch_bounds__(RP_THREADS) gj_replay_kernel(const float* __restrict__ qlog,
                                                                const int* __restrict__ blog,
@@ -1062,8 +1065,9 @@ __global__ void __launch_bounds__(RP_THREADS) gj_replay_kernel(const float* __re
   extern __shared__ __align__(16) float rp_smem[];
   const int nrows = 2 * cs * bs, weff = 2 * bs;
   float* V = rp_smem;                   // [nrows][RP_COLS]
-  float* Qs = V + nrows * RP_COLS;      // [cs][GJ_W][GJ_W]
+  float* Qs = V + nrows * RP_COLS;      // [cs][GJ_W][RP_QS]
   __shared__ int s_b[2 * 16];
+  __shared__ int s_act;
   const int c0 = blockIdx.x * RP_COLS, tid = threadIdx.x;
   for (int i = tid; i < nrows * RP_COLS; i += RP_THREADS) V[i] = (i / RP_COLS == c0 + i % RP_COLS) ? 1.f : 0.f;
   const int st = *status;
@@ -1071,10 +1075,22 @@ __global__ void __launch_bounds__(RP_THREADS) gj_replay_kernel(const float* __re
   const int64_t nsteps = (int64_t)sweeps * (2 * cs - 1);
   const int tasks = cs * weff;  // (pair, working row)
   for (int64_t ls = 0; ls < nsteps; ++ls) {
+    if (tid == 0) s_act = 0;
     __syncthreads();
-    if (tid < 2 * cs) s_b[tid] = blog[ls * cs * 2 + tid];
+    if (tid < 2 * cs) {
+      const int b = blog[ls * cs * 2 + tid];
+      s_b[tid] = b;
+      if ((tid & 1) == 0 && b >= 0) s_act = 1;
+    }
+    __syncthreads();
+    if (!s_act) continue;
     const float4* src = reinterpret_cast<const float4*>(qlog + ls * cs * (GJ_W * GJ_W));
-    for (int i = tid; i < cs * GJ_W * GJ_W / 4; i += RP_THREADS) reinterpret_cast<float4*>(Qs)[i] = src[i];
+    for (int i = tid; i < cs * GJ_W * GJ_W / 4; i += RP_THREADS) {
+      const int c = i / (GJ_W * GJ_W / 4), rem = i % (GJ_W * GJ_W / 4);
+      if (s_b[2 * c] < 0) continue;
+      const int r = rem / (GJ_W / 4), q4 = rem % (GJ_W / 4);
+      *reinterpret_cast<float4*>(Qs + (c * GJ_W + r) * RP_QS + 4 * q4) = src[i];
+    }
     __syncthreads();
     float out[2][RP_COLS];
     int orow[2];
@@ -1086,22 +1102,31 @@ __global__ void __launch_bounds__(RP_THREADS) gj_replay_kernel(const float* __re
       const int c = t / weff, r = t % weff;
       const int A = s_b[2 * c], B = s_b[2 * c + 1];
       if (A < 0) continue;
-      const float* q = Qs + (c * GJ_W + r) * GJ_W;
+      const float* q = Qs + (c * GJ_W + r) * RP_QS;
 #pragma unroll
       for (int u = 0; u < RP_COLS; ++u) out[k][u] = 0.f;
-      for (int j = 0; j < weff; ++j) {
-        const float qj = q[j];
+      for (int j4 = 0; j4 < weff / 4; ++j4) {
+        const float4 q4 = *reinterpret_cast<const float4*>(q + 4 * j4);
+        const float qv[4] = {q4.x, q4.y, q4.z, q4.w};
+#pragma unroll
+        for (int jj = 0; jj < 4; ++jj) {
+          const int j = 4 * j4 + jj;
+          const int vr = (j < bs) ? A * bs + j : B * bs + (j - bs);
+          const float4 v0 = *reinterpret_cast<const float4*>(V + vr * RP_COLS);
+          const float4 v1 = *reinterpret_cast<const float4*>(V + vr * RP_COLS + 4);
+          out[k][0] = fmaf(qv[jj], v0.x, out[k][0]);
+          out[k][1] = fmaf(qv[jj], v0.y, out[k][1]);
+          out[k][2] = fmaf(qv[jj], v0.z, out[k][2]);
+          out[k][3] = fmaf(qv[jj], v0.w, out[k][3]);
+          out[k][4] = fmaf(qv[jj], v1.x, out[k][4]);
+          out[k][5] = fmaf(qv[jj], v1.y, out[k][5]);
+          out[k][6] = fmaf(qv[jj], v1.z, out[k][6]);
+          out[k][7] = fmaf(qv[jj], v1.w, out[k][7]);
+        }
+      }
+      for (int j = 4 * (weff / 4); j < weff; ++j) {
         const int vr = (j < bs) ? A * bs + j : B * bs + (j - bs);
-        const float4 v0 = *reinterpret_cast<const float4*>(V + vr * RP_COLS);
-        const float4 v1 = *reinterpret_cast<const float4*>(V + vr * RP_COLS + 4);
-        out[k][0] = fmaf(qj, v0.x, out[k][0]);
-        out[k][1] = fmaf(qj, v0.y, out[k][1]);
-        out[k][2] = fmaf(qj, v0.z, out[k][2]);
-        out[k][3] = fmaf(qj, v0.w, out[k][3]);
-        out[k][4] = fmaf(qj, v1.x, out[k][4]);
-        out[k][5] = fmaf(qj, v1.y, out[k][5]);
-        out[k][6] = fmaf(qj, v1.z, out[k][6]);
-        out[k][7] = fmaf(qj, v1.w, out[k][7]);
+        for (int u = 0; u < RP_COLS; ++u) out[k][u] = fmaf(q[j], V[vr * RP_COLS + u], out[k][u]);
       }
       orow[k] = (r < bs) ? A * bs + r : B * bs + (r - bs);
     }
@@ -1453,11 +1478,11 @@ int sym_eig_rows_f32(cudaStream_t st, float* Z, int64_t n, float* Vt, float* lam
     if (!launched) return jacobi_rows_f32(st, Z, n, n, n, Vt, n, lam, status, ar0);
     const int cs = gj_cluster(n);
     const int bsz = (int)cdiv(n, 2 * cs);
-    const size_t smem = sizeof(float) * ((size_t)2 * cs * bsz * RP_COLS + (size_t)cs * GJ_W * GJ_W);
+    const size_t smem = sizeof(float) * ((size_t)2 * cs * bsz * RP_COLS + (size_t)cs * GJ_W * RP_QS);
     static bool rp_attr = false;
     if (!rp_attr) {
       SGT_CUDA(cudaFuncSetAttribute(gj_replay_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                    (int)(sizeof(float) * ((size_t)2 * 16 * (GJ_W / 2) * RP_COLS + 16 * GJ_W * GJ_W))));
+                                    (int)(sizeof(float) * ((size_t)2 * 16 * (GJ_W / 2) * RP_COLS + 16 * GJ_W * RP_QS))));
       rp_attr = true;
     }
     gj_replay_kernel<<<(unsigned)cdiv(n, RP_COLS), RP_THREADS, smem, st>>>(qlog, blog, status, (int)n, cs, bsz, Vt, n);
