@@ -329,10 +329,14 @@ def run_gpu(args, rank, world, local_rank):
         alg_flops = tc_flops.value / tc_n.value
         achieved = alg_flops * passes / per_launch_s / 1e12
         traffic = None
-        tpath = os.path.join(ROOT, "profiles", "tc_gemm_tf32_traffic.json")
+        # DRAM bytes per launch of this kernel over the sweep's launch mix, from
+        # an ncu capture (dram__bytes_read.sum + dram__bytes_write.sum)
+        tpath = os.path.join(ROOT, "profiles", "tc_gemm_tf32_traffic.txt")
         if os.path.exists(tpath):
             with open(tpath) as f:
-                traffic = json.load(f).get("bytes_per_launch_4096cubed")
+                for ln in f:
+                    if ln.startswith("bytes_per_launch"):
+                        traffic = float(ln.split()[1])
         out["roofline"] = {
             "bound": "tensor", "kernel": "tc_gemm_tf32_kernel", "achieved": achieved, "peak": peak,
             "unit": "TFLOP/s", "frac": achieved / peak, "traffic": traffic,

@@ -96,6 +96,12 @@ inline int64_t cdiv(int64_t a, int64_t b) { return (a + b - 1) / b; }
 int gemm_f64(cudaStream_t st, bool ta, bool tb, int64_t M, int64_t N, int64_t K, double alpha,
              const double* A, int64_t lda, int64_t sA, const double* B, int64_t ldb, int64_t sB,
              double beta, double* C, int64_t ldc, int64_t sC, int64_t batch, int split_k = 0);
+// Deterministic split-K (K in `splits` equal chunks, ws = splits * M * N doubles,
+// summed in a fixed order) and the chunk count that fills the GPU.
+int gemm_f64_splitk(cudaStream_t st, bool ta, bool tb, int64_t M, int64_t N, int64_t K, double alpha,
+                    const double* A, int64_t lda, const double* B, int64_t ldb, double beta, double* C, int64_t ldc,
+                    double* ws, int splits);
+int splitk_count(int64_t M, int64_t N, int64_t K);
 
 // Elementwise helpers.
 int fill_f64(cudaStream_t st, double* p, int64_t n, double v);

@@ -106,7 +106,47 @@ __global__ void scale_matrix_kernel(double* C, int64_t ldc, int64_t sC, int64_t 
   }
 }
 
+// C = alpha * sum_z P[z] + beta * C (fixed order over z: deterministic)
+__global__ void splitk_reduce_kernel(const double* __restrict__ P, int splits, int64_t M, int64_t N, double alpha,
+                                     double beta, double* __restrict__ C, int64_t ldc) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < M * N; i += (int64_t)gridDim.x * blockDim.x) {
+    double acc = 0.0;
+    for (int z = 0; z < splits; ++z) acc += P[(int64_t)z * M * N + i];
+    double* c = C + (i / N) * ldc + (i % N);
+    *c = (beta == 0.0) ? alpha * acc : fma(beta, *c, alpha * acc);
+  }
+}
 }  // namespace
+
+// Deterministic split-K: the K range is cut into `splits` equal chunks (a
+// multiple of the K tile), computed as one batched launch into ws (splits x
+// M x N doubles) and summed in a fixed order.  Used where the output has too
+// few 64 x 64 tiles to occupy the GPU's FP64 pipes (the bond-sized GEMMs of
+// the mixed form and of the overlap sweep).  splits <= 1: plain gemm_f64.
+int gemm_f64_splitk(cudaStream_t st, bool ta, bool tb, int64_t M, int64_t N, int64_t K, double alpha,
+                    const double* A, int64_t lda, const double* B, int64_t ldb, double beta, double* C, int64_t ldc,
+                    double* ws, int splits) {
+  if (splits > 1 && (K % splits != 0 || (K / splits) % BK != 0)) splits = 1;
+  if (splits <= 1 || M <= 0 || N <= 0)
+    return gemm_f64(st, ta, tb, M, N, K, alpha, A, lda, 0, B, ldb, 0, beta, C, ldc, 0, 1, 1);
+  const int64_t kc = K / splits;
+  const int64_t sA = ta ? kc * lda : kc;  // K chunk z of A and B
+  const int64_t sB = tb ? kc : kc * ldb;
+  SGT_TRY(gemm_f64(st, ta, tb, M, N, kc, 1.0, A, lda, sA, B, ldb, sB, 0.0, ws, N, M * N, splits, 1));
+  const unsigned g = (unsigned)std::max<int64_t>(1, std::min<int64_t>(cdiv(M * N, 256), 152 * 8));
+  splitk_reduce_kernel<<<g, 256, 0, st>>>(ws, splits, M, N, alpha, beta, C, ldc);
+  SGT_LAUNCHED();
+  return SGT_OK;
+}
+
+// number of K chunks (<= 16) that brings an M x N output to ~128 or more 64 x 64 tiles
+int splitk_count(int64_t M, int64_t N, int64_t K) {
+  const int64_t tiles = cdiv(M, BM) * cdiv(N, BN);
+  int s = 1;
+  while (s < 16 && tiles * s * 2 <= 160 && K % (2 * s) == 0 && (K / (2 * s)) % BK == 0 && K / (2 * s) >= 4 * BK)
+    s *= 2;
+  return s;
+}
 
 int gemm_f64(cudaStream_t st, bool ta, bool tb, int64_t M, int64_t N, int64_t K, double alpha,
              const double* A, int64_t lda, int64_t sA, const double* B, int64_t ldb, int64_t sB,

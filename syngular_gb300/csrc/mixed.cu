@@ -82,6 +82,55 @@ __global__ void product_split_kernel(const double* __restrict__ X, const double*
   }
 }
 
+// x (FP64) -> FP32 pair hi + lo with hi = fl32(x), |x - hi - lo| <= 2^-48 |x|
+__global__ void f64_pair_kernel(const double* __restrict__ x, float* __restrict__ hi, float* __restrict__ lo,
+                                int64_t n) {
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    const double v = x[i];
+    const float h = (float)v;
+    hi[i] = h;
+    lo[i] = (float)(v - (double)h);
+  }
+}
+
+// The product core P[(a,b), o, (a2,b2)] = sum_i X[a,i,a2] W[b,i,o,b2] in FP32
+// arithmetic from the FP32 pairs of X and W: error-free products (FMA) and
+// two-sum accumulation carry ~44 bits, then the TF32 hi / FP32 lo split of
+// the result.  One CTA row per (a, b, o) row of P (grid.y), threads along
+// (a2, b2): FP32 throughput instead of GB300's FP64 rate, so the kernel is
+// bound by writing hi and lo.
+__global__ void product_pair_split_kernel(const float* __restrict__ Xh, const float* __restrict__ Xl,
+                                          const float* __restrict__ Wh, const float* __restrict__ Wl,
+                                          float* __restrict__ Phi, float* __restrict__ Plo, int Bd, int I, int O,
+                                          int A2, int B2, int ncol) {
+  const int r = blockIdx.y;
+  const int o = r % O, ab = r / O, b = ab % Bd, a = ab / Bd;
+  const int c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= ncol) return;
+  const int a2 = c / B2, b2 = c - a2 * B2;
+  float sum = 0.f, t = 0.f;
+  for (int i = 0; i < I; ++i) {
+    const int64_t xi = ((int64_t)a * I + i) * A2 + a2;
+    const int64_t wi = (((int64_t)b * I + i) * O + o) * B2 + b2;
+    const float xh = Xh[xi], xl = Xl[xi], wh = Wh[wi], wl = Wl[wi];
+    const float prod = xh * wh;
+    const float e = fmaf(xh, wh, -prod);
+    const float cross = fmaf(xh, wl, xl * wh);
+    const float s2 = sum + prod;
+    const float bb = s2 - sum;
+    const float err = (sum - (s2 - bb)) + (prod - bb);
+    sum = s2;
+    t += err + e + cross;
+  }
+  const float v = sum + t;
+  uint32_t h;
+  asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(h) : "f"(v));
+  const float fh = __uint_as_float(h);
+  const int64_t idx = (int64_t)r * ncol + c;
+  Phi[idx] = fh;
+  Plo[idx] = (sum - fh) + t;
+}
+
 // dst[b] (cols x rows, ldd) = src[b]^T (rows x cols, lds), batch stride sb / db.
 __global__ void transpose_f32_kernel(float* __restrict__ dst, int64_t ldd, int64_t db,
                                      const float* __restrict__ src, int64_t lds, int64_t sb,
@@ -374,6 +423,16 @@ static int mixed_round_impl(cudaStream_t st, int n, const double* const* W, cons
   float* lam = ar.take<float>(cmax);
   double* Vd = ar.take<double>(chi * cmax);
   double* Sd = ar.take<double>(chi * chi);
+  int64_t xmax = 1, wmax = 1;
+  for (int k = 0; k < n; ++k) {
+    xmax = std::max<int64_t>(xmax, xs[3 * k] * xs[3 * k + 1] * xs[3 * k + 2]);
+    wmax = std::max<int64_t>(wmax, w[k].b * w[k].i * w[k].o * w[k].b2);
+  }
+  float* pXh = ar.take<float>(xmax);
+  float* pXl = ar.take<float>(xmax);
+  float* pWh = ar.take<float>(wmax);
+  float* pWl = ar.take<float>(wmax);
+  double* skw = ar.take<double>(16 * chi * cmax);  // split-K partials of the FP64 re-orthonormalisation
   int* stat = ar.take<int>(n + 1);
   int* tc_err = ar.take<int>(1);
   int* gexp = ar.take<int>(n + 1);
@@ -400,9 +459,21 @@ static int mixed_round_impl(cudaStream_t st, int n, const double* const* W, cons
   for (int k = 0; k < n; ++k) {
     const int64_t sz = R[k] * Pd[k] * R[k + 1];
     const int64_t a2 = xs[3 * k + 2];
-    product_split_kernel<<<gs(sz), 256, 0, st>>>(X[k], W[k], Ph[k], Pl[k], w[k].b, w[k].i, w[k].o, a2,
-                                                  w[k].b2, sz);
-    SGT_LAUNCHED();
+    const int64_t nrow = R[k] * Pd[k], ncol = R[k + 1];
+    const int64_t xsz = xs[3 * k] * xs[3 * k + 1] * xs[3 * k + 2], wsz = w[k].b * w[k].i * w[k].o * w[k].b2;
+    if (nrow <= 65535 && ncol < ((int64_t)1 << 31)) {
+      f64_pair_kernel<<<gs(xsz), 256, 0, st>>>(X[k], pXh, pXl, xsz);
+      SGT_LAUNCHED();
+      f64_pair_kernel<<<gs(wsz), 256, 0, st>>>(W[k], pWh, pWl, wsz);
+      SGT_LAUNCHED();
+      product_pair_split_kernel<<<dim3((unsigned)cdiv(ncol, 256), (unsigned)nrow), 256, 0, st>>>(
+          pXh, pXl, pWh, pWl, Ph[k], Pl[k], (int)w[k].b, (int)w[k].i, (int)w[k].o, (int)a2, (int)w[k].b2, (int)ncol);
+      SGT_LAUNCHED();
+    } else {
+      product_split_kernel<<<gs(sz), 256, 0, st>>>(X[k], W[k], Ph[k], Pl[k], w[k].b, w[k].i, w[k].o, a2,
+                                                    w[k].b2, sz);
+      SGT_LAUNCHED();
+    }
     if (structured) continue;
     // Pt[p] (R' x R) = (P[:, p, :])^T, P[:, p, :] is R x R' with row stride p*R'
     SGT_TRY(transpose_f32(st, Pth[k], R[k], R[k + 1] * R[k], Ph[k], Pd[k] * R[k + 1], R[k + 1], R[k],
@@ -474,9 +545,11 @@ static int mixed_round_impl(cudaStream_t st, int n, const double* const* W, cons
     // V <- 1.5 V - 0.5 (V V^T) V (the FP32 rotations leave |V V^T - I| ~ 1e-6)
     f32_to_f64_kernel<<<gs(keep * c), 256, 0, st>>>(Vt, c, Vd, c, keep, c);
     SGT_LAUNCHED();
-    SGT_TRY(gemm_f64(st, false, true, keep, keep, c, 1.0, Vd, c, 0, Vd, c, 0, 0.0, Sd, keep, 0, 1));
+    SGT_TRY(gemm_f64_splitk(st, false, true, keep, keep, c, 1.0, Vd, c, Vd, c, 0.0, Sd, keep, skw,
+                            splitk_count(keep, keep, c)));
     SGT_TRY(copy2d_f64(st, out[k], c, Vd, c, keep, c));
-    SGT_TRY(gemm_f64(st, false, false, keep, c, keep, -0.5, Sd, keep, 0, Vd, c, 0, 1.5, out[k], c, 0, 1));
+    SGT_TRY(gemm_f64_splitk(st, false, false, keep, c, keep, -0.5, Sd, keep, Vd, c, 1.5, out[k], c, skw,
+                            splitk_count(keep, c, keep)));
     double* spec_k = nullptr;
     if (spectra) {
       int64_t off = 0;

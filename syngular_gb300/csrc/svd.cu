@@ -1050,13 +1050,25 @@ __global__ void __launch_bounds__(BJ_THREADS) gjacobi_kernel(float* __restrict__
 // Vt = (the logged rotations of gjacobi_kernel<1>, in order) applied to I.
 // Columns of Vt transform independently under row rotations, so each CTA
 // replays the whole log on a slice of RP_COLS columns held in shared memory
-// (all 2 cs bs block rows) and needs no other CTA.  Per logged step it reads
-// the block ids, loads the rotation matrices of the pairs that rotated (row
-// stride padded to 36 floats: the 16-byte loads of the 8 rows a quarter-warp
-// reads fall in distinct banks), computes every working row of those pairs
-// into registers and writes them back; steps without rotations cost two
-// barriers.
+// (all 2 cs bs block rows) and needs no other CTA.  The log of step s + 1
+// (the cs rotation matrices, rows padded to 36 floats so that the 16-byte
+// loads of the 8 rows a quarter-warp reads fall in distinct banks, and the
+// block ids) streams into the other half of a double buffer with cp.async
+// while step s computes every working row of its rotated pairs into
+// registers; the rows are written back after a barrier.
 constexpr int RP_COLS = 8, RP_THREADS = 256, RP_QS = GJ_W + 4;
+
+__device__ __forceinline__ void cp_async16(void* dst, const void* src) {
+  const unsigned d = (unsigned)__cvta_generic_to_shared(dst);
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(d), "l"(src) : "memory");
+}
+__device__ __forceinline__ void cp_async4(void* dst, const void* src) {
+  const unsigned d = (unsigned)__cvta_generic_to_shared(dst);
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 4;\n" ::"r"(d), "l"(src) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
+template <int N>
+__device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory"); }
 
 __global__ void __launch_bounds__(RP_THREADS) gj_replay_kernel(const float* __restrict__ qlog,
                                                                const int* __restrict__ blog,
@@ -1064,71 +1076,76 @@ __global__ void __launch_bounds__(RP_THREADS) gj_replay_kernel(const float* __re
                                                                float* __restrict__ Vt, int64_t ldv) {
   extern __shared__ __align__(16) float rp_smem[];
   const int nrows = 2 * cs * bs, weff = 2 * bs;
-  float* V = rp_smem;                   // [nrows][RP_COLS]
-  float* Qs = V + nrows * RP_COLS;      // [cs][GJ_W][RP_QS]
-  __shared__ int s_b[2 * 16];
-  __shared__ int s_act;
+  float* V = rp_smem;                                   // [nrows][RP_COLS]
+  float* Qb = V + nrows * RP_COLS;                      // [2][cs][GJ_W][RP_QS]
+  __shared__ int s_b[2][2 * 16];
   const int c0 = blockIdx.x * RP_COLS, tid = threadIdx.x;
+  const int qstride = cs * GJ_W * RP_QS;
   for (int i = tid; i < nrows * RP_COLS; i += RP_THREADS) V[i] = (i / RP_COLS == c0 + i % RP_COLS) ? 1.f : 0.f;
   const int st = *status;
   const int sweeps = st > 0 ? st : (st < 0 ? JAC_MAX_SWEEPS : 0);
   const int64_t nsteps = (int64_t)sweeps * (2 * cs - 1);
   const int tasks = cs * weff;  // (pair, working row)
-  for (int64_t ls = 0; ls < nsteps; ++ls) {
-    if (tid == 0) s_act = 0;
-    __syncthreads();
-    if (tid < 2 * cs) {
-      const int b = blog[ls * cs * 2 + tid];
-      s_b[tid] = b;
-      if ((tid & 1) == 0 && b >= 0) s_act = 1;
-    }
-    __syncthreads();
-    if (!s_act) continue;
-    const float4* src = reinterpret_cast<const float4*>(qlog + ls * cs * (GJ_W * GJ_W));
+  auto prefetch = [&](int64_t ls, int buf) {
+    const float* src = qlog + ls * cs * (GJ_W * GJ_W);
+    float* dst = Qb + buf * qstride;
     for (int i = tid; i < cs * GJ_W * GJ_W / 4; i += RP_THREADS) {
-      const int c = i / (GJ_W * GJ_W / 4), rem = i % (GJ_W * GJ_W / 4);
-      if (s_b[2 * c] < 0) continue;
-      const int r = rem / (GJ_W / 4), q4 = rem % (GJ_W / 4);
-      *reinterpret_cast<float4*>(Qs + (c * GJ_W + r) * RP_QS + 4 * q4) = src[i];
+      const int cr = i / (GJ_W / 4), q4 = i % (GJ_W / 4);  // cr = pair * GJ_W + row
+      cp_async16(dst + cr * RP_QS + 4 * q4, src + 4 * i);
+    }
+    if (tid < 2 * cs) cp_async4(&s_b[buf][tid], blog + ls * cs * 2 + tid);
+    cp_async_commit();
+  };
+  if (nsteps > 0) prefetch(0, 0);
+  for (int64_t ls = 0; ls < nsteps; ++ls) {
+    const int cur = (int)(ls & 1);
+    if (ls + 1 < nsteps) {
+      prefetch(ls + 1, cur ^ 1);
+      cp_async_wait<1>();
+    } else {
+      cp_async_wait<0>();
     }
     __syncthreads();
+    int any = 0;
+    for (int c = 0; c < cs; ++c) any |= (s_b[cur][2 * c] >= 0);
     float out[2][RP_COLS];
-    int orow[2];
+    int orow[2] = {-1, -1};
+    if (any) {
 #pragma unroll
-    for (int k = 0; k < 2; ++k) {
-      orow[k] = -1;
-      const int t = tid + k * RP_THREADS;
-      if (t >= tasks) continue;
-      const int c = t / weff, r = t % weff;
-      const int A = s_b[2 * c], B = s_b[2 * c + 1];
-      if (A < 0) continue;
-      const float* q = Qs + (c * GJ_W + r) * RP_QS;
+      for (int k = 0; k < 2; ++k) {
+        const int t = tid + k * RP_THREADS;
+        if (t >= tasks) continue;
+        const int c = t / weff, r = t % weff;
+        const int A = s_b[cur][2 * c], B = s_b[cur][2 * c + 1];
+        if (A < 0) continue;
+        const float* q = Qb + cur * qstride + (c * GJ_W + r) * RP_QS;
 #pragma unroll
-      for (int u = 0; u < RP_COLS; ++u) out[k][u] = 0.f;
-      for (int j4 = 0; j4 < weff / 4; ++j4) {
-        const float4 q4 = *reinterpret_cast<const float4*>(q + 4 * j4);
-        const float qv[4] = {q4.x, q4.y, q4.z, q4.w};
+        for (int u = 0; u < RP_COLS; ++u) out[k][u] = 0.f;
+        for (int j4 = 0; j4 < weff / 4; ++j4) {
+          const float4 q4 = *reinterpret_cast<const float4*>(q + 4 * j4);
+          const float qv[4] = {q4.x, q4.y, q4.z, q4.w};
 #pragma unroll
-        for (int jj = 0; jj < 4; ++jj) {
-          const int j = 4 * j4 + jj;
-          const int vr = (j < bs) ? A * bs + j : B * bs + (j - bs);
-          const float4 v0 = *reinterpret_cast<const float4*>(V + vr * RP_COLS);
-          const float4 v1 = *reinterpret_cast<const float4*>(V + vr * RP_COLS + 4);
-          out[k][0] = fmaf(qv[jj], v0.x, out[k][0]);
-          out[k][1] = fmaf(qv[jj], v0.y, out[k][1]);
-          out[k][2] = fmaf(qv[jj], v0.z, out[k][2]);
-          out[k][3] = fmaf(qv[jj], v0.w, out[k][3]);
-          out[k][4] = fmaf(qv[jj], v1.x, out[k][4]);
-          out[k][5] = fmaf(qv[jj], v1.y, out[k][5]);
-          out[k][6] = fmaf(qv[jj], v1.z, out[k][6]);
-          out[k][7] = fmaf(qv[jj], v1.w, out[k][7]);
+          for (int jj = 0; jj < 4; ++jj) {
+            const int j = 4 * j4 + jj;
+            const int vr = (j < bs) ? A * bs + j : B * bs + (j - bs);
+            const float4 v0 = *reinterpret_cast<const float4*>(V + vr * RP_COLS);
+            const float4 v1 = *reinterpret_cast<const float4*>(V + vr * RP_COLS + 4);
+            out[k][0] = fmaf(qv[jj], v0.x, out[k][0]);
+            out[k][1] = fmaf(qv[jj], v0.y, out[k][1]);
+            out[k][2] = fmaf(qv[jj], v0.z, out[k][2]);
+            out[k][3] = fmaf(qv[jj], v0.w, out[k][3]);
+            out[k][4] = fmaf(qv[jj], v1.x, out[k][4]);
+            out[k][5] = fmaf(qv[jj], v1.y, out[k][5]);
+            out[k][6] = fmaf(qv[jj], v1.z, out[k][6]);
+            out[k][7] = fmaf(qv[jj], v1.w, out[k][7]);
+          }
         }
+        for (int j = 4 * (weff / 4); j < weff; ++j) {
+          const int vr = (j < bs) ? A * bs + j : B * bs + (j - bs);
+          for (int u = 0; u < RP_COLS; ++u) out[k][u] = fmaf(q[j], V[vr * RP_COLS + u], out[k][u]);
+        }
+        orow[k] = (r < bs) ? A * bs + r : B * bs + (r - bs);
       }
-      for (int j = 4 * (weff / 4); j < weff; ++j) {
-        const int vr = (j < bs) ? A * bs + j : B * bs + (j - bs);
-        for (int u = 0; u < RP_COLS; ++u) out[k][u] = fmaf(q[j], V[vr * RP_COLS + u], out[k][u]);
-      }
-      orow[k] = (r < bs) ? A * bs + r : B * bs + (r - bs);
     }
     __syncthreads();
 #pragma unroll
@@ -1478,11 +1495,11 @@ int sym_eig_rows_f32(cudaStream_t st, float* Z, int64_t n, float* Vt, float* lam
     if (!launched) return jacobi_rows_f32(st, Z, n, n, n, Vt, n, lam, status, ar0);
     const int cs = gj_cluster(n);
     const int bsz = (int)cdiv(n, 2 * cs);
-    const size_t smem = sizeof(float) * ((size_t)2 * cs * bsz * RP_COLS + (size_t)cs * GJ_W * RP_QS);
+    const size_t smem = sizeof(float) * ((size_t)2 * cs * bsz * RP_COLS + (size_t)2 * cs * GJ_W * RP_QS);
     static bool rp_attr = false;
     if (!rp_attr) {
       SGT_CUDA(cudaFuncSetAttribute(gj_replay_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                    (int)(sizeof(float) * ((size_t)2 * 16 * (GJ_W / 2) * RP_COLS + 16 * GJ_W * RP_QS))));
+                                    (int)(sizeof(float) * ((size_t)2 * 16 * (GJ_W / 2) * RP_COLS + 2 * 16 * GJ_W * RP_QS))));
       rp_attr = true;
     }
     gj_replay_kernel<<<(unsigned)cdiv(n, RP_COLS), RP_THREADS, smem, st>>>(qlog, blog, status, (int)n, cs, bsz, Vt, n);

@@ -154,8 +154,12 @@ __global__ void reduce_status_kernel(const int* __restrict__ st, int n, int* __r
 // ============================================================================
 // overlap
 // ============================================================================
+// splitk: use deterministic split-K partials (16 x the largest product in
+// the workspace) for the bond-sized FP64 GEMMs; the fixed-capacity entry
+// point (noalloc.cu) runs without.
 static int overlap_impl(cudaStream_t st, int n, const double* const* X, const int64_t* xs,
-                        const double* const* Y, const int64_t* ys, double* result, Arena& ar) {
+                        const double* const* Y, const int64_t* ys, double* result, Arena& ar,
+                        bool splitk = true) {
   auto sx = shapes_of(n, xs), sy = shapes_of(n, ys);
   SGT_TRY(check_chain(n, sx, "overlap(X)"));
   SGT_TRY(check_chain(n, sy, "overlap(Y)"));
@@ -172,6 +176,7 @@ static int overlap_impl(cudaStream_t st, int n, const double* const* X, const in
   double* T = ar.take<double>(tmax);
   double* expo = ar.take<double>(1);
   double* one = ar.take<double>(1);
+  double* skw = splitk ? ar.take<double>(16 * std::max(emax, tmax)) : nullptr;
   if (ar.measure) return SGT_OK;
   SGT_REQUIRE(ar.ok(), SGT_ERR_WORKSPACE, "overlap: workspace too small");
   SGT_TRY(fill_f64(st, one, 1, 1.0));
@@ -182,10 +187,12 @@ static int overlap_impl(cudaStream_t st, int n, const double* const* X, const in
   for (int k = 0; k < n; ++k) {
     const int64_t a = sx[k].l, p = sx[k].p, a2 = sx[k].r, c = sy[k].l, c2 = sy[k].r;
     // T (a x p*c2) = E (a x c) * Y_k (c x p*c2)
-    SGT_TRY(gemm_f64(st, false, false, a, p * c2, c, 1.0, E, c, 0, Y[k], p * c2, 0, 0.0, T, p * c2, 0, 1));
+    SGT_TRY(gemm_f64_splitk(st, false, false, a, p * c2, c, 1.0, E, c, Y[k], p * c2, 0.0, T, p * c2, skw,
+                            skw ? splitk_count(a, p * c2, c) : 1));
     double* En = bufs[k & 1];
     // E' (a2 x c2) = X_k^T (a2 x a*p) * T (a*p x c2)
-    SGT_TRY(gemm_f64(st, true, false, a2, c2, a * p, 1.0, X[k], a2, 0, T, c2, 0, 0.0, En, c2, 0, 1));
+    SGT_TRY(gemm_f64_splitk(st, true, false, a2, c2, a * p, 1.0, X[k], a2, T, c2, 0.0, En, c2, skw,
+                            skw ? splitk_count(a2, c2, a * p) : 1));
     rescale_pow2_kernel<<<1, 256, 0, st>>>(En, a2 * c2, expo, result, k == n - 1);
     SGT_LAUNCHED();
     E = En;
@@ -655,16 +662,17 @@ static int svd_round_impl(cudaStream_t st, int n, const double* const* cores, co
   return SGT_OK;
 }
 
+// the fixed-capacity variant (no split-K partials) for sgt_overlap_sweep_noalloc
 size_t overlap_ws_size(int n, const int64_t* xs, const int64_t* ys) {
   Arena a = Arena::measuring();
-  if (overlap_impl(nullptr, n, nullptr, xs, nullptr, ys, nullptr, a) != SGT_OK) return 0;
+  if (overlap_impl(nullptr, n, nullptr, xs, nullptr, ys, nullptr, a, false) != SGT_OK) return 0;
   return a.used;
 }
 
 int overlap_ws_run(cudaStream_t st, int n, const double* const* X, const int64_t* xs,
                    const double* const* Y, const int64_t* ys, double* result, void* ws, size_t ws_bytes) {
   Arena a(ws, ws_bytes);
-  return overlap_impl(st, n, X, xs, Y, ys, result, a);
+  return overlap_impl(st, n, X, xs, Y, ys, result, a, false);
 }
 
 size_t svd_round_ws(int n, const int64_t* shape, int64_t chi) {

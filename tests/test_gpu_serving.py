@@ -83,11 +83,15 @@ def test_budget_admission_and_rejection():
     from syngular_gb300.serving import Job, latency_stats
 
     rng = np.random.default_rng(9)
-    srv = server_with_sessions(rng, 4, budget=16 << 10, slots=4).start()  # 16 KB budget
+    srv = server_with_sessions(rng, 4, slots=4)
     big = Job(kind="round", session="s0", chi=8, precision=0)
+    ok = Job(kind="overlap", session="s1", other="s1")
+    f_ok, f_big = srv.footprint(ok), srv.footprint(big)
+    assert 0 < f_ok < f_big
+    srv.budget = (f_ok + f_big) // 2  # admits the overlap, not the round
+    srv.start()
     srv.submit(big)
     assert big.done.wait(60)
-    ok = Job(kind="overlap", session="s1", other="s1")
     srv.submit(ok)
     assert ok.done.wait(60)
     srv.stop()
