@@ -476,13 +476,18 @@ def run_serving(args):
     from syngular_gb300 import _lib as L
     from syngular_gb300.serving import Job, RoundServer, latency_stats
 
+    t_start = time.perf_counter()
+
+    def log(msg):
+        print("[serving %7.1f s] %s" % (time.perf_counter() - t_start, msg), file=sys.stderr, flush=True)
+
     rng = np.random.default_rng(11)
     srv = RoundServer(budget_bytes=120 << 30, slots=8)
     nsess = args.sessions
     for i in range(nsess):
         n = int(rng.integers(8, 129))
         d = int(rng.choice([2, 4]))
-        chi = int(round(math.exp(rng.uniform(math.log(8), math.log(512)))))
+        chi = int(round(math.exp(rng.uniform(math.log(8), math.log(args.chi_max)))))
         D = int(rng.choice([4, 16]))
         dims = [1] + [chi] * (n - 1) + [1]
         X = [rng.standard_normal((dims[k], d, dims[k + 1])) / math.sqrt(chi * d) for k in range(n)]
@@ -491,6 +496,7 @@ def run_serving(args):
         srv.add_session("s%d" % i, mps=X, mpo=W)
         srv.sessions["s%d" % i]["chi"] = chi
     srv.start()
+    log("%d sessions resident" % nsess)
     # seeded Poisson arrivals
     t = 0.0
     arrivals = []
@@ -509,10 +515,12 @@ def run_serving(args):
         j = Job(kind=kind, session=sid, chi=chi, precision=L.PREC_TF32X3, other=sid, job_id=k,
                 arrival=t0 + ta)
         jobs.append(srv.submit(j))
+    log("%d jobs submitted" % len(jobs))
     deadline = time.perf_counter() + args.drain
     for j in jobs:
         j.done.wait(max(0.0, deadline - time.perf_counter()))
     wall = time.perf_counter() - t0
+    log("drained: %d of %d done" % (sum(1 for j in jobs if j.done.is_set()), len(jobs)))
     srv.stop()
     done = [j for j in jobs if j.done.is_set() and j.error is None]
     rejected = [j for j in jobs if j.error is not None]
@@ -522,8 +530,8 @@ def run_serving(args):
         "n_gpus": 1, "higher_is_better": True, "dtype": "tf32x3/f32 (round), f64 (add_round, overlap)",
         "data": "synthetic seeded Poisson stream",
         "config": {"workload": "config5 stream: %.0f jobs/s for %.1f s, %d resident sessions, N~U[8,128], "
-                               "d in {2,4}, chi log-uniform [8,512], D in {4,16}, HBM budget 120 GB"
-                               % (args.rate, args.duration, nsess), "slots": 8},
+                               "d in {2,4}, chi log-uniform [8,%d], D in {4,16}, HBM budget 120 GB"
+                               % (args.rate, args.duration, nsess, args.chi_max), "slots": 8},
         "submitted": len(jobs), "completed": len(done), "rejected_or_failed": len(rejected),
         "unfinished": len(jobs) - len(done) - len(rejected), "latency": stats, "wall_s": wall,
     }
@@ -543,10 +551,13 @@ def main():
     ap.add_argument("--workload", default="config2", choices=["config2", "batched", "serving"])
     ap.add_argument("--instances", type=int, default=512)
     ap.add_argument("--plain-sample", type=int, default=8)
-    ap.add_argument("--rate", type=float, default=2000.0)
-    ap.add_argument("--duration", type=float, default=2.0)
-    ap.add_argument("--sessions", type=int, default=64)
+    ap.add_argument("--rate", type=float, default=10.0)
+    ap.add_argument("--duration", type=float, default=5.0)
+    ap.add_argument("--sessions", type=int, default=16)
     ap.add_argument("--drain", type=float, default=120.0)
+    ap.add_argument("--chi-max", type=int, default=128,
+                    help="serving sessions: upper end of the log-uniform bond range (bond problems d*chi "
+                         "above 512 leave the cluster-resident eigensolver)")
     ap.add_argument("--sites", type=int, default=64, help="chain length (64 = the headline workload; shorter "
                     "chains only for profiling captures)")
     args = ap.parse_args()
