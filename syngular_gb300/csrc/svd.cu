@@ -493,6 +493,7 @@ __global__ void __launch_bounds__(BJ_THREADS) gjacobi_kernel(float* __restrict__
   float* stage = slots + 2 * slot_tot;              // one slot
   __shared__ __align__(16) float sC[2][GJ_W][GJ_W];
   __shared__ __align__(16) float sQ[GJ_W][GJ_W];
+  __shared__ __align__(16) float sQt[GJ_W][GJ_W];
   __shared__ int s_off[GJ_W];
   __shared__ int s_blk[2];
   __shared__ int s_rot[2];
@@ -912,7 +913,49 @@ __global__ void __launch_bounds__(BJ_THREADS) gjacobi_kernel(float* __restrict__
       }
 
       // ---- 3. apply Q to the working rows ----
-      if (s_any) {
+      if (s_any && (row_len & 7) == 0) {
+        // register tiles: thread = 4 output rows x 8 columns, Q^T rows as one
+        // 16-byte broadcast per K step, X rows as two; all reads finish before
+        // the in-place writes
+        for (int i = tid; i < GJ_W * GJ_W; i += BJ_THREADS) sQt[i % GJ_W][i / GJ_W] = sQ[i / GJ_W][i % GJ_W];
+        __syncthreads();
+        const int rg = lane & 7, cgl = lane >> 3;
+        for (int ebase = 0; ebase < row_len; ebase += BJ_THREADS) {
+          const int e0 = ebase + (warp * 4 + cgl) * 8;
+          float acc[4][8];
+#pragma unroll
+          for (int a = 0; a < 4; ++a)
+#pragma unroll
+            for (int u = 0; u < 8; ++u) acc[a][u] = 0.f;
+          if (e0 < row_len) {
+            for (int k = 0; k < weff; ++k) {
+              const float4 q = *reinterpret_cast<const float4*>(&sQt[k][4 * rg]);
+              const float* xr = slots + s_off[k] + e0;
+              const float4 x0 = *reinterpret_cast<const float4*>(xr);
+              const float4 x1 = *reinterpret_cast<const float4*>(xr + 4);
+              const float qa[4] = {q.x, q.y, q.z, q.w};
+              const float xv[8] = {x0.x, x0.y, x0.z, x0.w, x1.x, x1.y, x1.z, x1.w};
+#pragma unroll
+              for (int a = 0; a < 4; ++a)
+#pragma unroll
+                for (int u = 0; u < 8; ++u) acc[a][u] = fmaf(qa[a], xv[u], acc[a][u]);
+            }
+          }
+          __syncthreads();
+          if (e0 < row_len) {
+#pragma unroll
+            for (int a = 0; a < 4; ++a) {
+              const int r = 4 * rg + a;
+              if (r < weff) {
+                float4* d = reinterpret_cast<float4*>(slots + s_off[r] + e0);
+                d[0] = make_float4(acc[a][0], acc[a][1], acc[a][2], acc[a][3]);
+                d[1] = make_float4(acc[a][4], acc[a][5], acc[a][6], acc[a][7]);
+              }
+            }
+          }
+          __syncthreads();
+        }
+      } else if (s_any) {
         for (int e = tid; e < row_len; e += BJ_THREADS) {
           float x[GJ_W];
 #pragma unroll
