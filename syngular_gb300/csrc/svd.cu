@@ -722,48 +722,27 @@ __global__ void __launch_bounds__(BJ_THREADS) gjacobi_kernel(float* __restrict__
       // of a sweep, else only the cross block (the two diagonal blocks are
       // the tracked Gram matrices that came with the rows) ----
       const bool all_pairs = (step == 0);
-      if (all_pairs) {
-        int offi[8], offj[8];
-#pragma unroll
-        for (int a = 0; a < 8; ++a) {
-          offi[a] = s_off[8 * ti + a];
-          offj[a] = s_off[8 * tj + a];
+      // 4 x 4 tiles of C, lanes striding the row length, reduce-scatter to one
+      // entry per lane pair: all 64 tiles of the 32 x 32 matrix on the first
+      // step (4 per warp), else the 16 tiles of the cross block (1 per warp)
+      // with the diagonal blocks taken from the tracked Gram matrices
+      const int ntile = all_pairs ? 4 : 1;
+      for (int tt = 0; tt < ntile; ++tt) {
+        int ra0, rb0;  // first row of the tile's A and B rows (local indices)
+        if (all_pairs) {
+          const int t = warp * 4 + tt;  // 0..63 over an 8 x 8 grid of 4 x 4 tiles
+          ra0 = 4 * (t >> 3);
+          rb0 = 4 * (t & 7);
+        } else {
+          ra0 = 4 * ti;
+          rb0 = bs + 4 * tj;
         }
-        float v[64];
-#pragma unroll
-        for (int k = 0; k < 64; ++k) v[k] = 0.f;
-        for (int e = lane; e < m; e += 32) {
-          float xi[8], xj[8];
-#pragma unroll
-          for (int a = 0; a < 8; ++a) {
-            xi[a] = offi[a] >= 0 ? slots[offi[a] + e] : 0.f;
-            xj[a] = offj[a] >= 0 ? slots[offj[a] + e] : 0.f;
-          }
-#pragma unroll
-          for (int a = 0; a < 8; ++a)
-#pragma unroll
-            for (int b = 0; b < 8; ++b) v[a * 8 + b] = fmaf(xi[a], xj[b], v[a * 8 + b]);
-        }
-        // reduce-scatter over the 32 lanes: lane L ends with entries 2L, 2L+1
-#pragma unroll
-        for (int h = 32, o = 16; o > 0; h >>= 1, o >>= 1) {
-          const bool up = (lane & o) != 0;
-#pragma unroll
-          for (int k = 0; k < h; ++k) {
-            const float send = up ? v[k] : v[k + h];
-            const float keep = up ? v[k + h] : v[k];
-            v[k] = keep + __shfl_xor_sync(0xffffffffu, send, o);
-          }
-        }
-        const int a = lane >> 2, b = 2 * (lane & 3);
-        sC[0][8 * ti + a][8 * tj + b] = v[0];
-        sC[0][8 * ti + a][8 * tj + b + 1] = v[1];
-      } else {
+        const int alim = all_pairs ? weff : bs, blim = all_pairs ? weff : 2 * bs;
         int offa[4], offb[4];
 #pragma unroll
-        for (int a = 0; a < 4; ++a) {
-          offa[a] = (4 * ti + a < bs) ? s_off[4 * ti + a] : -1;
-          offb[a] = (4 * tj + a < bs) ? s_off[bs + 4 * tj + a] : -1;
+        for (int q = 0; q < 4; ++q) {
+          offa[q] = (ra0 + q < alim) ? s_off[ra0 + q] : -1;
+          offb[q] = (rb0 + q < blim && (all_pairs || rb0 + q >= bs)) ? s_off[rb0 + q] : -1;
         }
         float v[16];
 #pragma unroll
@@ -771,17 +750,15 @@ __global__ void __launch_bounds__(BJ_THREADS) gjacobi_kernel(float* __restrict__
         for (int e = lane; e < m; e += 32) {
           float xa[4], xb[4];
 #pragma unroll
-          for (int a = 0; a < 4; ++a) {
-            xa[a] = offa[a] >= 0 ? slots[offa[a] + e] : 0.f;
-            xb[a] = offb[a] >= 0 ? slots[offb[a] + e] : 0.f;
+          for (int q = 0; q < 4; ++q) {
+            xa[q] = offa[q] >= 0 ? slots[offa[q] + e] : 0.f;
+            xb[q] = offb[q] >= 0 ? slots[offb[q] + e] : 0.f;
           }
 #pragma unroll
-          for (int a = 0; a < 4; ++a)
+          for (int q = 0; q < 4; ++q)
 #pragma unroll
-            for (int b = 0; b < 4; ++b) v[a * 4 + b] = fmaf(xa[a], xb[b], v[a * 4 + b]);
+            for (int u = 0; u < 4; ++u) v[q * 4 + u] = fmaf(xa[q], xb[u], v[q * 4 + u]);
         }
-        // reduce-scatter to one entry per lane pair (entry lane >> 1), then
-        // the last butterfly completes the sum on both lanes of the pair
 #pragma unroll
         for (int h = 8, o = 16; o > 1; h >>= 1, o >>= 1) {
           const bool up = (lane & o) != 0;
@@ -793,12 +770,13 @@ __global__ void __launch_bounds__(BJ_THREADS) gjacobi_kernel(float* __restrict__
           }
         }
         v[0] += __shfl_xor_sync(0xffffffffu, v[0], 1);
-        const int a = (lane >> 1) >> 2, b = (lane >> 1) & 3;
-        const int ra = 4 * ti + a, rb = 4 * tj + b;
-        if ((lane & 1) == 0 && ra < bs && rb < bs) {
-          sC[0][ra][bs + rb] = v[0];
-          sC[0][bs + rb][ra] = v[0];
+        const int ra = ra0 + ((lane >> 1) >> 2), rb = rb0 + ((lane >> 1) & 3);
+        if ((lane & 1) == 0 && ra < alim && rb < blim) {
+          sC[0][ra][rb] = v[0];
+          if (!all_pairs) sC[0][rb][ra] = v[0];
         }
+      }
+      if (!all_pairs) {
         for (int idx = tid; idx < 2 * bs * bs; idx += BJ_THREADS) {
           const int sl = idx / (bs * bs), r = idx % (bs * bs);
           sC[0][sl * bs + r / bs][sl * bs + r % bs] = slots[(int64_t)sl * slot_tot + slot_elems + r];
