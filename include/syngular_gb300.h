@@ -277,6 +277,32 @@ SGT_API int sgt_sym_eig_f32(float* Z, int64_t n, float* Vt, float* lam, int* sta
  * k = 1, or the value of SGT_EIG_TOL. */
 SGT_API int sgt_eig_method(int method);
 
+/* Batched MPO x MPS + TT-SVD round + overlap over `count` independent
+ * instances of uneven size (replaces the per-instance loop a caller of the
+ * reference would write around `(W @ X) >> chi` and `X | Z`; no single
+ * reference function).  sgt_batched_plan_create sizes every instance's
+ * workspace (max of the fused round and the overlap), deals the instances
+ * longest-first onto `lanes` stream lanes and returns the workspace one launch
+ * needs; it is host-only (no device calls).  sgt_batched_launch forks the
+ * lanes off `stream` with events, runs each lane's instances in order inside
+ * its own workspace region and joins the lanes back: no allocation, no host
+ * synchronisation, capturable into a CUDA graph.  The lanes' streams and
+ * events are created on the first launch and released by
+ * sgt_batched_plan_destroy.  One plan must not be launched concurrently from
+ * two threads. */
+typedef struct sgt_batched_plan_s* sgt_batched_plan;
+SGT_API int sgt_batched_plan_create(int count, const int* n, const int64_t* const* wshape,
+                                    const int64_t* const* xshape, const int64_t* chi, int precision,
+                                    int lanes, sgt_batched_plan* plan, size_t* ws_bytes);
+SGT_API int sgt_batched_plan_lane(const struct sgt_batched_plan_s* plan, int instance);
+SGT_API int sgt_batched_plan_out_shape(const struct sgt_batched_plan_s* plan, int instance,
+                                       int64_t* out_shape);
+SGT_API int sgt_batched_launch(sgt_batched_plan plan, const double* const* const* W,
+                               const double* const* const* X, double* const* const* out,
+                               double* const* spectra, double* const* discarded, int* const* status,
+                               double* const* overlap, void* ws, size_t ws_bytes, void* stream);
+SGT_API void sgt_batched_plan_destroy(sgt_batched_plan plan);
+
 /* hi = TF32 rounding of x (round to nearest, ties away), lo = x - hi (lo may be NULL). */
 SGT_API int sgt_split_tf32(const float* x, float* hi, float* lo, int64_t n, void* stream);
 

@@ -145,6 +145,120 @@ class BatchedRound:
         return [int(inst.status.item()) for inst in self.instances]
 
 
+def _vp_array(items):
+    arr = (ctypes.c_void_p * len(items))(*items)
+    return arr
+
+
+class NativePlan:
+    """Host side of the library's batched plan (sgt_batched_plan_create): the
+    per-instance workspace sizes, the deal of instances onto stream lanes and
+    the rounded core shapes.  Needs no GPU."""
+
+    def __init__(self, shapes, precision: int = L.PREC_TF32X3, lanes: int = 4):
+        # shapes: list of (wshape list (4 n), xshape list (3 n), chi)
+        self.count = len(shapes)
+        self.n = [len(x) // 3 for _, x, _ in shapes]
+        self._keep = []
+        narr = (ctypes.c_int * self.count)(*self.n)
+        warrs = [L.i64_array(w)[1] for w, _, _ in shapes]
+        xarrs = [L.i64_array(x)[1] for _, x, _ in shapes]
+        self._keep += [narr, warrs, xarrs]
+        wp = _vp_array([ctypes.cast(a, ctypes.c_void_p).value for a in warrs])
+        xp = _vp_array([ctypes.cast(a, ctypes.c_void_p).value for a in xarrs])
+        chis = (ctypes.c_int64 * self.count)(*[int(c) for _, _, c in shapes])
+        self._keep += [wp, xp, chis]
+        self.handle = ctypes.c_void_p()
+        wsb = ctypes.c_size_t()
+        L.call("sgt_batched_plan_create", self.count, narr, wp, xp, chis, int(precision), int(lanes),
+               ctypes.byref(self.handle), ctypes.byref(wsb))
+        self.ws_bytes = int(wsb.value)
+        lib = L.load()
+        self.lane = [int(lib.sgt_batched_plan_lane(self.handle, i)) for i in range(self.count)]
+        self.out_shapes = []
+        for i in range(self.count):
+            o = (ctypes.c_int64 * (3 * self.n[i]))()
+            L.call("sgt_batched_plan_out_shape", self.handle, i, o)
+            self.out_shapes.append([tuple(o[3 * k:3 * k + 3]) for k in range(self.n[i])])
+
+    def __del__(self):
+        try:
+            if getattr(self, "handle", None) is not None and self.handle.value:
+                L.load().sgt_batched_plan_destroy(self.handle)
+                self.handle = ctypes.c_void_p()
+        except Exception:
+            pass
+
+
+class NativeBatchedRound:
+    """The batch run through sgt_batched_launch (one library call that forks the
+    lanes off the current stream and joins them): same results as BatchedRound,
+    graph-capturable."""
+
+    def __init__(self, instances: List[Instance], precision: int = L.PREC_TF32X3, lanes: int = 4):
+        self.instances = instances
+        self.plan = NativePlan([(i.wsh, i.xsh, i.chi) for i in instances], precision, lanes)
+        dev = L.device()
+        self._keep = []
+        W, X, O, SP, DI, ST, OV = [], [], [], [], [], [], []
+        for inst, oshape in zip(instances, self.plan.out_shapes):
+            inst.out = [torch.empty(s, dtype=torch.float64, device=dev) for s in oshape]
+            inst.spectra = torch.zeros(max(1, sum(self._counts(inst))), dtype=torch.float64, device=dev)
+            inst.disc = torch.zeros(max(1, inst.n - 1), dtype=torch.float64, device=dev)
+            inst.status = torch.zeros(1, dtype=torch.int32, device=dev)
+            inst.ovl = torch.zeros(2, dtype=torch.float64, device=dev)
+            for lst, ts in ((W, inst.W), (X, inst.X), (O, inst.out)):
+                _p, arr = L.ptr_array(ts)
+                self._keep.append(arr)
+                lst.append(ctypes.cast(arr, ctypes.c_void_p).value)
+            SP.append(inst.spectra.data_ptr())
+            DI.append(inst.disc.data_ptr())
+            ST.append(inst.status.data_ptr())
+            OV.append(inst.ovl.data_ptr())
+        self._arrs = [_vp_array(v) for v in (W, X, O, SP, DI, ST, OV)]
+        self.ws = torch.empty(max(1, self.plan.ws_bytes), dtype=torch.uint8, device=dev)
+        self.graph: Optional[torch.cuda.CUDAGraph] = None
+
+    @staticmethod
+    def _counts(inst):
+        psh, _p = L.shape_array(inst.pshapes)
+        out = (ctypes.c_int64 * (3 * inst.n))()
+        cnt = (ctypes.c_int64 * max(1, inst.n - 1))()
+        L.call("sgt_svd_round_shapes", inst.n, psh, inst.chi, ctypes.cast(out, L._PI64), ctypes.cast(cnt, L._PI64))
+        return [cnt[k] for k in range(inst.n - 1)]
+
+    def launch(self):
+        W, X, O, SP, DI, ST, OV = self._arrs
+        L.call("sgt_batched_launch", self.plan.handle, W, X, O, SP, DI, ST, OV, L.ptr(self.ws), self.ws.numel(),
+               L.stream_ptr())
+
+    def capture(self):
+        self.launch()
+        torch.cuda.synchronize()
+        g = torch.cuda.CUDAGraph()
+        side = torch.cuda.Stream()
+        side.wait_stream(torch.cuda.current_stream())
+        with torch.cuda.stream(side):
+            with torch.cuda.graph(g, stream=side):
+                self.launch()
+        torch.cuda.current_stream().wait_stream(side)
+        self.graph = g
+        return g
+
+    def replay(self):
+        if self.graph is None:
+            self.capture()
+        self.graph.replay()
+
+    def overlaps(self) -> List[float]:
+        from .tensor._ops import decode_overlap
+
+        return [decode_overlap(inst.ovl.cpu().tolist()) for inst in self.instances]
+
+    def statuses(self) -> List[int]:
+        return [int(inst.status.item()) for inst in self.instances]
+
+
 def shape_class(instances: List[Instance]) -> str:
     r = max(i.rmax for i in instances)
     nb = int(round(sum(i.n for i in instances) / max(1, len(instances))))

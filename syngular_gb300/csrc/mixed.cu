@@ -573,6 +573,49 @@ static int mixed_round_impl(cudaStream_t st, int n, const double* const* W, cons
   return SGT_OK;
 }
 
+namespace {
+__global__ void identity_cores_kernel(double* __restrict__ eye, const int* __restrict__ dims, int n, int stride) {
+  for (int k = blockIdx.x; k < n; k += gridDim.x) {
+    const int d = dims[k];
+    for (int i = threadIdx.x; i < d * d; i += blockDim.x) eye[(int64_t)k * stride + i] = (i / d == i % d) ? 1.0 : 0.0;
+  }
+}
+}  // namespace
+
+// TT-SVD rounding of a plain chain in the Gram form: the chain equals the
+// product of a bond-1 identity MPO with itself, so the MPO x MPS pipeline
+// applies unchanged (one d x d identity core per site, built on the device).
+int mixed_round_chain(cudaStream_t st, int n, const double* const* X, const int64_t* xs, int64_t chi,
+                      int precision, double* const* out, double* spectra, double* discarded, int* status,
+                      Arena& ar) {
+  SGT_REQUIRE(precision == SGT_PREC_TF32 || precision == SGT_PREC_TF32X3, SGT_ERR_INVALID,
+              "round: precision %d has no Gram form", precision);
+  std::vector<int64_t> w4(4 * (size_t)n);
+  std::vector<int> dims(n);
+  int64_t dmax = 1;
+  for (int k = 0; k < n; ++k) {
+    const int64_t d = xs[3 * k + 1];
+    w4[4 * k] = 1;
+    w4[4 * k + 1] = d;
+    w4[4 * k + 2] = d;
+    w4[4 * k + 3] = 1;
+    dims[k] = (int)d;
+    dmax = std::max(dmax, d);
+  }
+  double* eye = ar.take<double>((size_t)n * dmax * dmax);
+  int* ddims = ar.take<int>((size_t)n);
+  std::vector<const double*> W(n, nullptr);
+  if (!ar.measure) {
+    SGT_REQUIRE(ar.ok(), SGT_ERR_WORKSPACE, "round: workspace too small");
+    SGT_CUDA(cudaMemcpyAsync(ddims, dims.data(), sizeof(int) * n, cudaMemcpyHostToDevice, st));
+    identity_cores_kernel<<<(unsigned)std::min(n, 1024), 128, 0, st>>>(eye, ddims, n, (int)(dmax * dmax));
+    SGT_LAUNCHED();
+    for (int k = 0; k < n; ++k) W[k] = eye + (int64_t)k * dmax * dmax;
+  }
+  return mixed_round_impl(st, n, W.data(), w4.data(), X, xs, chi, precision == SGT_PREC_TF32 ? 1 : 3, out, spectra,
+                          discarded, status, ar);
+}
+
 static int mpo_mps_round_impl(cudaStream_t st, int n, const double* const* W, const int64_t* ws4,
                               const double* const* X, const int64_t* xs, int64_t chi, int precision,
                               double* const* out, double* spectra, double* discarded, int* status,

@@ -14,6 +14,9 @@
 #include "common.cuh"
 
 namespace sgt {
+int mixed_round_chain(cudaStream_t st, int n, const double* const* X, const int64_t* xs, int64_t chi,
+                      int precision, double* const* out, double* spectra, double* discarded, int* status,
+                      Arena& ar);
 
 // ---- declarations of helpers defined in other translation units ----------
 int frob_norm_f64(cudaStream_t st, const double* p, int64_t n, double* out);
@@ -528,8 +531,9 @@ static int svd_round_impl(cudaStream_t st, int n, const double* const* cores, co
   auto s = shapes_of(n, shp);
   SGT_TRY(check_chain(n, s, "svd_round"));
   SGT_REQUIRE(chi >= 1, SGT_ERR_INVALID, "svd_round: chi must be >= 1");
-  SGT_REQUIRE(precision == SGT_PREC_F64, SGT_ERR_INVALID,
-              "svd_round: precision %d is served by the mixed-precision path", precision);
+  if (precision == SGT_PREC_TF32 || precision == SGT_PREC_TF32X3)
+    return mixed_round_chain(st, n, cores, shp, chi, precision, out, spectra, discarded, status, ar);
+  SGT_REQUIRE(precision == SGT_PREC_F64, SGT_ERR_INVALID, "svd_round: unsupported precision %d", precision);
   SGT_REQUIRE(s[0].l == 1 && s[n - 1].r == 1, SGT_ERR_INVALID, "svd_round: boundary bonds must be 1");
   std::vector<int64_t> b, x, cnt;
   svd_round_plan(n, s, chi, b, x, cnt);

@@ -91,3 +91,33 @@ def test_no_cpu_fallback_without_gpu():
 
     with pytest.raises(RuntimeError, match="CUDA"):
         MatrixProductState.zeros((2, 2), (2,))
+
+
+def test_batched_plan_host_only():
+    """sgt_batched_plan_create is host-only: workspace sizes, the longest-first
+    deal onto lanes and the rounded shapes, without a GPU."""
+    import numpy as np
+
+    from syngular_gb300.batched import NativePlan
+
+    rng = np.random.default_rng(5)
+    shapes, chis = [], []
+    for _ in range(9):
+        n = int(rng.integers(3, 8))
+        d = int(rng.choice([2, 3]))
+        chi = int(rng.integers(2, 9))
+        D = int(rng.choice([1, 2, 3]))
+        xb = [1] + [chi] * (n - 1) + [1]
+        wb = [1] + [D] * (n - 1) + [1]
+        xs = [v for k in range(n) for v in (xb[k], d, xb[k + 1])]
+        ws = [v for k in range(n) for v in (wb[k], d, d, wb[k + 1])]
+        shapes.append((ws, xs, chi))
+    plan = NativePlan(shapes, precision=0, lanes=4)
+    assert plan.ws_bytes > 0 and plan.ws_bytes % 256 == 0
+    assert sorted(set(plan.lane)) == [0, 1, 2, 3]
+    for (ws, xs, chi), oshape in zip(shapes, plan.out_shapes):
+        n = len(xs) // 3
+        p = [(xs[3 * k] * ws[4 * k], ws[4 * k + 2], xs[3 * k + 2] * ws[4 * k + 3]) for k in range(n)]
+        assert len(oshape) == n and oshape[0][0] == 1 and oshape[-1][2] == 1
+        for k in range(n - 1):
+            assert oshape[k][2] == oshape[k + 1][0] and oshape[k][2] <= chi

@@ -67,3 +67,30 @@ def test_autotune_caches_choice(tmp_path, monkeypatch):
     assert r1["streams"] in (1, 2) and set(r1["trials"]) <= {"1", "2"}
     r2 = B.autotune(insts, precision=0, candidates=(1, 2), reps=1)
     assert r2 == r1
+
+
+@pytest.mark.parametrize("prec,tol", [(0, 1e-12), (4, 1e-6)])
+def test_native_batched_launch(prec, tol):
+    """sgt_batched_launch (one library call, lanes forked off the current
+    stream) gives every instance the result of its own sgt_mpo_mps_round +
+    sgt_overlap_sweep, eagerly and from a captured graph."""
+    from syngular_gb300.batched import NativeBatchedRound
+    from syngular_gb300.tensor import _ops
+
+    rng = np.random.default_rng(31 + prec)
+    insts, ref = make(rng, 7)
+    b = NativeBatchedRound(insts, precision=prec, lanes=3)
+    b.launch()
+    torch.cuda.synchronize()
+    first = b.overlaps()
+    assert all(s >= 0 for s in b.statuses())
+    for inst, got, (ov, nrm) in zip(insts, first, ref):
+        assert abs(got - ov) <= tol * nrm
+        Z, spec, counts, disc, st = _ops.mpo_mps_round(inst.W, inst.X, inst.chi, prec)
+        alone = _ops.overlap(inst.X, Z)
+        assert abs(got - alone) <= 1e-12 * nrm
+    for inst in insts:
+        inst.ovl.zero_()
+    b.replay()
+    torch.cuda.synchronize()
+    assert b.overlaps() == first

@@ -85,3 +85,32 @@ def test_mpo_mps_round_eig_methods(method):
     nz = np.sqrt(O.overlap(Zr, Zr))
     fid = abs(_ops.overlap(Z, Zd)) / (np.sqrt(abs(_ops.overlap(Z, Z))) * nz)
     assert 1 - fid < 1e-8
+
+
+@pytest.mark.parametrize("n,d,chi,cut,summed", [(8, 2, 32, 16, False), (6, 3, 20, 12, False), (8, 2, 24, 24, True)])
+def test_svd_round_gram_form(n, d, chi, cut, summed):
+    """TT-SVD rounding of a plain chain (and of a direct sum) through the Gram
+    form: the chain is routed through the MPO x MPS pipeline with bond-1
+    identity cores; 3xTF32 against the FP64 oracle."""
+    from syngular_gb300.tensor import _ops
+
+    rng = np.random.default_rng(500 + n * d + chi)
+    X = O.random_mps_cores(rng, n, d, chi)
+    if summed:
+        X = O.direct_sum(X, O.random_mps_cores(rng, n, d, chi))
+    Zr, spec_r, disc_r = O.tt_svd_round(X, cut)
+    Z, spec, counts, disc, status = _ops.svd_round(dev(X), cut, 4)
+    torch.cuda.synchronize()
+    assert int(status.item()) >= 0
+    assert [tuple(z.shape) for z in Z] == [z.shape for z in Zr]
+    Xd = dev(X)
+    ov, ovr = _ops.overlap(Xd, Z), O.overlap(X, Zr)
+    nx, nz = np.sqrt(O.overlap(X, X)), np.sqrt(O.overlap(Zr, Zr))
+    assert abs(ov - ovr) / (nx * nz) < 1e-6
+    s = spec.cpu().numpy()
+    off = 0
+    for k in range(n - 1):
+        m = min(counts[k], len(spec_r[k]), cut)
+        np.testing.assert_allclose(s[off:off + m], spec_r[k][:m], rtol=0, atol=1e-4 * spec_r[k][0])
+        off += counts[k]
+    np.testing.assert_allclose(disc.cpu().numpy(), disc_r, rtol=0, atol=1e-5)
