@@ -131,7 +131,34 @@ __global__ void __launch_bounds__(JAC_THREADS) jacobi_kernel(T* __restrict__ G, 
   const int npairs = np / 2;
 
   __shared__ int s_rot[2];
+  __shared__ double s_part[JAC_WARPS];
+  __shared__ double s_norm;
   if (threadIdx.x < 2) s_rot[threadIdx.x] = 0;
+  // n > 512: pairs with |g_p . g_q| below m (eps |G|_F)^2 are rounding noise
+  // and are not rotated (on such problems rows at the noise level otherwise
+  // keep rotating against each other up to the sweep cap; on smaller ones the
+  // floor would stop rotations that still move the leading vectors)
+  double abs_floor = 0.0;
+  if (n > 512) {
+    double acc = 0.0;
+    for (int j = gw; j < n; j += nw) {
+      const T* gj = G + (int64_t)j * ldg;
+      for (int64_t e = lane; e < m; e += 32) acc += (double)gj[e] * (double)gj[e];
+    }
+    for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+    if (lane == 0) s_part[warp] = acc;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      double t = 0.0;
+      for (int w = 0; w < JAC_WARPS; ++w) t += s_part[w];
+      s_norm = t;
+    }
+    cluster.sync();
+    double tot = 0.0;
+    for (int r = 0; r < cs; ++r) tot += *cluster.map_shared_rank(&s_norm, r);
+    const double fl = (sizeof(T) == 4 ? (double)FLT_EPSILON : DBL_EPSILON) * sqrt(tot);
+    abs_floor = (double)m * fl * fl;
+  }
   cluster.sync();
 
   int sweeps = 0;
@@ -161,7 +188,7 @@ __global__ void __launch_bounds__(JAC_THREADS) jacobi_kernel(T* __restrict__ G, 
         b = wsum_t(b);
         c = wsum_t(c);
         T cs_, sn, tau;
-        if (jacobi_rotation<T>(a, b, c, tol, 0.0, lane, cs_, sn, tau)) {
+        if (jacobi_rotation<T>(a, b, c, tol, abs_floor, lane, cs_, sn, tau)) {
           ++my_rot;
           for (int64_t e = lane; e < m; e += 32) {
             T x = gp[e], y = gq[e];
