@@ -508,7 +508,10 @@ __global__ void __launch_bounds__(BJ_THREADS) gjacobi_kernel(float* __restrict__
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const int nblk = 2 * cs;
   const int row_len = (MODE == 1 || MODE == 2) ? m : m + n;  // G part then Vt part
-  const int slot_elems = bs * row_len;
+  // MODE 1 pads each row by 4 floats: the apply's 16-byte stores of 8 rows
+  // at one column offset then fall in different banks
+  const int rs = (MODE == 1 && (row_len & 7) == 0) ? row_len + 4 : row_len;
+  const int slot_elems = bs * rs;
   // each slot: bs rows, then the bs x bs Gram matrix of those rows as tracked
   // through the rotations (it travels with the rows)
   const int gstride = (bs * bs + 3) & ~3;
@@ -522,7 +525,7 @@ __global__ void __launch_bounds__(BJ_THREADS) gjacobi_kernel(float* __restrict__
   __shared__ __align__(16) float sQ[GJ_W][GJ_W];
   __shared__ __align__(16) float sQt[GJ_W][GJ_W];
   __shared__ int s_off[GJ_W];
-  __shared__ int s_blk[2];
+  __shared__ int s_blk[2][2];  // [parity][slot]: block ids, double-buffered for the MODE 1 move
   __shared__ int s_rot[2];
   __shared__ int s_any;
   __shared__ double s_norm;
@@ -538,12 +541,19 @@ __global__ void __launch_bounds__(BJ_THREADS) gjacobi_kernel(float* __restrict__
     }
   };
   auto slot_pos = [&](int c, int slot) { return slot == 0 ? c : nblk - 1 - c; };
+  // MODE 1 double-buffers the slots (buffers sl and 2 + sl; the block at the
+  // fixed circle position 0 never moves): mp is the parity of the moves done
+  int mp = 0;
+  auto curo = [&](int sl) -> int64_t {
+    if (MODE == 1 && mp && !(rank == 0 && sl == 0)) return (int64_t)(2 + sl) * slot_tot;
+    return (int64_t)sl * slot_tot;
+  };
 
-  if (tid < GJ_W) s_off[tid] = (tid < weff) ? (tid / bs) * slot_tot + (tid % bs) * row_len : -1;
+  if (tid < GJ_W) s_off[tid] = (tid < weff) ? (tid / bs) * slot_tot + (tid % bs) * rs : -1;
   for (int sl = 0; sl < 2; ++sl) {
     const int blk = slot_pos(rank, sl);
-    if (tid == 0) s_blk[sl] = blk;
-    for (int64_t i = tid; i < slot_elems; i += BJ_THREADS) {
+    if (tid == 0) s_blk[0][sl] = blk;
+    for (int64_t i = tid; i < (int64_t)bs * row_len; i += BJ_THREADS) {
       const int r = (int)(i / row_len), e = (int)(i % row_len);
       const int gr = blk * bs + r;
       float v = 0.f;
@@ -552,7 +562,7 @@ __global__ void __launch_bounds__(BJ_THREADS) gjacobi_kernel(float* __restrict__
         else if (e < m) v = G[(int64_t)gr * ldg + e];
         else v = ((e - m) == gr) ? 1.f : 0.f;
       }
-      slots[(int64_t)sl * slot_tot + i] = v;
+      slots[(int64_t)sl * slot_tot + (int64_t)r * rs + e] = v;
     }
   }
   float shift = 0.f;
@@ -706,7 +716,7 @@ __global__ void __launch_bounds__(BJ_THREADS) gjacobi_kernel(float* __restrict__
     double acc = 0.0;
     for (int64_t i = tid; i < 2 * (int64_t)slot_elems; i += BJ_THREADS) {
       const int sl = (int)(i / slot_elems), j = (int)(i % slot_elems);
-      if (j % row_len < m) {
+      if (j % rs < m) {
         const double v = (double)slots[(int64_t)sl * slot_tot + j];
         acc += v * v;
       }
@@ -806,7 +816,7 @@ __global__ void __launch_bounds__(BJ_THREADS) gjacobi_kernel(float* __restrict__
       if (!all_pairs) {
         for (int idx = tid; idx < 2 * bs * bs; idx += BJ_THREADS) {
           const int sl = idx / (bs * bs), r = idx % (bs * bs);
-          sC[0][sl * bs + r / bs][sl * bs + r % bs] = slots[(int64_t)sl * slot_tot + slot_elems + r];
+          sC[0][sl * bs + r / bs][sl * bs + r % bs] = slots[curo(sl) + slot_elems + r];
         }
       }
       for (int i = tid; i < GJ_W * GJ_W; i += BJ_THREADS) sQ[i / GJ_W][i % GJ_W] = (i / GJ_W == i % GJ_W) ? 1.f : 0.f;
@@ -902,7 +912,7 @@ __global__ void __launch_bounds__(BJ_THREADS) gjacobi_kernel(float* __restrict__
       // the diagonal blocks of the rotated Gram matrix travel with the rows
       for (int idx = tid; idx < 2 * bs * bs; idx += BJ_THREADS) {
         const int sl = idx / (bs * bs), r = idx % (bs * bs);
-        slots[(int64_t)sl * slot_tot + slot_elems + r] = sC[cur][sl * bs + r / bs][sl * bs + r % bs];
+        slots[curo(sl) + slot_elems + r] = sC[cur][sl * bs + r / bs][sl * bs + r % bs];
       }
       if constexpr (MODE == 1) {
         // log Q and the two block ids (-1: no rotation) for gj_replay_kernel
@@ -912,17 +922,22 @@ __global__ void __launch_bounds__(BJ_THREADS) gjacobi_kernel(float* __restrict__
           for (int i = tid; i < GJ_W * GJ_W / 4; i += BJ_THREADS) qd[i] = reinterpret_cast<const float4*>(&sQ[0][0])[i];
         }
         if (tid == 0) {
-          blog[2 * ls] = s_any ? s_blk[0] : -1;
-          blog[2 * ls + 1] = s_blk[1];
+          blog[2 * ls] = s_any ? s_blk[mp][0] : -1;
+          blog[2 * ls + 1] = s_blk[mp][1];
         }
       }
 
       // ---- 3. apply Q to the working rows ----
       if (s_any && (row_len & 7) == 0) {
-        // register tiles: thread = 4 output rows x 8 columns, Q^T rows as one
-        // 16-byte broadcast per K step, X rows as two; all reads finish before
-        // the in-place writes
-        for (int i = tid; i < GJ_W * GJ_W; i += BJ_THREADS) sQt[i % GJ_W][i / GJ_W] = sQ[i / GJ_W][i % GJ_W];
+        // register tiles: thread rg = output rows rg, rg + 8, rg + 16, rg + 24
+        // x 8 columns (eight consecutive rows per 16-byte store phase, which
+        // the padded row stride puts in distinct banks), Q^T rows as one
+        // 16-byte broadcast per K step (sQt[k][4 rg + a] = Q[rg + 8 a][k]),
+        // X rows as two; all reads finish before the in-place writes
+        for (int i = tid; i < GJ_W * GJ_W; i += BJ_THREADS) {
+          const int r = i / GJ_W, k = i % GJ_W;
+          sQt[k][4 * (r & 7) + (r >> 3)] = sQ[r][k];
+        }
         __syncthreads();
         const int rg = lane & 7, cgl = lane >> 3;
         for (int ebase = 0; ebase < row_len; ebase += BJ_THREADS) {
@@ -950,7 +965,7 @@ __global__ void __launch_bounds__(BJ_THREADS) gjacobi_kernel(float* __restrict__
           if (e0 < row_len) {
 #pragma unroll
             for (int a = 0; a < 4; ++a) {
-              const int r = 4 * rg + a;
+              const int r = rg + 8 * a;
               if (r < weff) {
                 float4* d = reinterpret_cast<float4*>(slots + s_off[r] + e0);
                 d[0] = make_float4(acc[a][0], acc[a][1], acc[a][2], acc[a][3]);
@@ -989,11 +1004,34 @@ __global__ void __launch_bounds__(BJ_THREADS) gjacobi_kernel(float* __restrict__
         const int qs = (q == 0) ? 0 : (q == 1 ? nblk - 1 : q - 1);
         pos_owner(qs, src_cta[sl], src_slot[sl]);
       }
+      if constexpr (MODE == 1) {
+        // pull straight into the other buffer of each moving slot: a buffer
+        // is only overwritten after the next step's cluster barrier, by when
+        // every CTA has finished reading it, so one barrier per step suffices
+        cluster.sync();
+        const int nmp = mp ^ 1;
+        const int n4 = slot_tot * (int)sizeof(float) / 16;
+        for (int sl = 0; sl < 2; ++sl) {
+          if (rank == 0 && sl == 0) continue;
+          const int sc = src_cta[sl], ss = src_slot[sl];
+          const int64_t soff = (sc == 0 && ss == 0) ? 0 : (int64_t)(mp ? 2 + ss : ss) * slot_tot;
+          const int64_t doff = (int64_t)(nmp ? 2 + sl : sl) * slot_tot;
+          const uint4* src4 = reinterpret_cast<const uint4*>(cluster.map_shared_rank(slots, sc) + soff);
+          uint4* dst4 = reinterpret_cast<uint4*>(slots + doff);
+          for (int idx = tid; idx < n4; idx += BJ_THREADS) dst4[idx] = src4[idx];
+          if (tid == 0) s_blk[nmp][sl] = *cluster.map_shared_rank(&s_blk[mp][ss], sc);
+        }
+        if (rank == 0 && tid == 0) s_blk[nmp][0] = s_blk[mp][0];
+        mp = nmp;
+        if (tid < GJ_W) s_off[tid] = (tid < weff) ? (int)curo(tid / bs) + (tid % bs) * rs : -1;
+        __syncthreads();
+        continue;
+      }
       cluster.sync();
       const float* r0 = cluster.map_shared_rank(slots, src_cta[0]) + (int64_t)src_slot[0] * slot_tot;
       const float* r1 = cluster.map_shared_rank(slots, src_cta[1]) + (int64_t)src_slot[1] * slot_tot;
-      const int nb0 = *cluster.map_shared_rank(&s_blk[src_slot[0]], src_cta[0]);
-      const int nb1 = *cluster.map_shared_rank(&s_blk[src_slot[1]], src_cta[1]);
+      const int nb0 = *cluster.map_shared_rank(&s_blk[0][src_slot[0]], src_cta[0]);
+      const int nb1 = *cluster.map_shared_rank(&s_blk[0][src_slot[1]], src_cta[1]);
       const int n4 = slot_tot * (int)sizeof(float) / 16;
       const uint4* s0 = reinterpret_cast<const uint4*>(r0);
       const uint4* s1 = reinterpret_cast<const uint4*>(r1);
@@ -1019,8 +1057,8 @@ __global__ void __launch_bounds__(BJ_THREADS) gjacobi_kernel(float* __restrict__
         }
       }
       if (tid == 0) {
-        s_blk[0] = nb0;
-        s_blk[1] = nb1;
+        s_blk[0][0] = nb0;
+        s_blk[0][1] = nb1;
       }
       __syncthreads();
     }
@@ -1036,12 +1074,12 @@ __global__ void __launch_bounds__(BJ_THREADS) gjacobi_kernel(float* __restrict__
     if (tid == 0) s_rot[par] = 0;
   }
   for (int sl = 0; sl < 2; ++sl) {
-    const int blk = s_blk[sl];
+    const int blk = s_blk[mp][sl];
     if (MODE == 2) {
       for (int r = warp; r < bs; r += BJ_WARPS) {
         const int gr = blk * bs + r;
         if (gr >= n) continue;
-        const float* row = slots + (int64_t)sl * slot_tot + (int64_t)r * row_len;
+        const float* row = slots + curo(sl) + (int64_t)r * rs;
         float acc = 0.f;
         for (int e = lane; e < m; e += 32) acc = fmaf(row[e], row[e], acc);
         acc = wsum_t(acc);
@@ -1059,7 +1097,7 @@ __global__ void __launch_bounds__(BJ_THREADS) gjacobi_kernel(float* __restrict__
       for (int r = warp; r < bs; r += BJ_WARPS) {
         const int gr = blk * bs + r;
         if (gr >= n) continue;
-        const float* row = slots + (int64_t)sl * slot_tot + (int64_t)r * row_len;
+        const float* row = slots + curo(sl) + (int64_t)r * rs;
         float acc = 0.f;
         for (int e = lane; e < m; e += 32) acc = fmaf(row[e], row[e], acc);
         acc = wsum_t(acc);
@@ -1073,18 +1111,18 @@ __global__ void __launch_bounds__(BJ_THREADS) gjacobi_kernel(float* __restrict__
       }
       continue;
     }
-    for (int64_t i = tid; i < slot_elems; i += BJ_THREADS) {
+    for (int64_t i = tid; i < (int64_t)bs * row_len; i += BJ_THREADS) {
       const int r = (int)(i / row_len), e = (int)(i % row_len);
       const int gr = blk * bs + r;
       if (gr >= n) continue;
-      const float v = slots[(int64_t)sl * slot_tot + i];
+      const float v = slots[curo(sl) + (int64_t)r * rs + e];
       if (e < m) G[(int64_t)gr * ldg + e] = v;
       else Vt[(int64_t)gr * ldv + (e - m)] = v;
     }
     for (int r = warp; r < bs; r += BJ_WARPS) {
       const int gr = blk * bs + r;
       if (gr >= n) continue;
-      const float* row = slots + (int64_t)sl * slot_tot + (int64_t)r * row_len;
+      const float* row = slots + curo(sl) + (int64_t)r * rs;
       float acc = 0.f;
       for (int e = lane; e < m; e += 32) acc = fmaf(row[e], row[e], acc);
       acc = wsum_t(acc);
@@ -1312,7 +1350,9 @@ static int launch_gjacobi(cudaStream_t st, float* G, int64_t ldg, float* Vt, int
   if (n < 64 || n > 16 * GJ_W || (MODE >= 2 && m != n)) return SGT_OK;
   const int csb = gj_cluster(n);
   const int64_t bsz = cdiv(n, 2 * csb);
-  const int64_t slot_bytes = bsz * ((MODE == 1 || MODE == 2) ? m : m + n) * (int64_t)sizeof(float);
+  int64_t rlen = (MODE == 1 || MODE == 2) ? m : m + n;
+  if (MODE == 1 && rlen % 8 == 0) rlen += 4;  // the kernel's row padding
+  const int64_t slot_bytes = bsz * rlen * (int64_t)sizeof(float);
   if (bsz > GJ_W / 2 || slot_bytes > BJ_MAX_SLOT_BYTES || slot_bytes % 16 != 0) return SGT_OK;
   static bool attr_done = false;
   auto kern = gjacobi_kernel<MODE>;
@@ -1322,10 +1362,12 @@ static int launch_gjacobi(cudaStream_t st, float* G, int64_t ldg, float* Vt, int
     attr_done = true;
   }
   const int64_t gram_bytes = ((bsz * bsz + 3) & ~int64_t(3)) * (int64_t)sizeof(float);
+  const int64_t dyn = (MODE == 1 ? 4 : 3) * (slot_bytes + gram_bytes);
+  if (dyn > 3 * GJ_SLOT_CAP) return SGT_OK;
   cudaLaunchConfig_t cfg = {};
   cfg.gridDim = dim3(csb, 1, 1);
   cfg.blockDim = dim3(BJ_THREADS, 1, 1);
-  cfg.dynamicSmemBytes = (size_t)3 * (slot_bytes + gram_bytes);
+  cfg.dynamicSmemBytes = (size_t)dyn;
   cfg.stream = st;
   cudaLaunchAttribute attr[1];
   attr[0].id = cudaLaunchAttributeClusterDimension;
