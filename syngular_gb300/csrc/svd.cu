@@ -784,17 +784,48 @@ __global__ void __launch_bounds__(BJ_THREADS) gjacobi_kernel(float* __restrict__
         float v[16];
 #pragma unroll
         for (int k = 0; k < 16; ++k) v[k] = 0.f;
-        for (int e = lane; e < m; e += 32) {
-          float xa[4], xb[4];
+        auto gram_scalar = [&]() {
+          for (int e = lane; e < m; e += 32) {
+            float xa[4], xb[4];
 #pragma unroll
-          for (int q = 0; q < 4; ++q) {
-            xa[q] = offa[q] >= 0 ? slots[offa[q] + e] : 0.f;
-            xb[q] = offb[q] >= 0 ? slots[offb[q] + e] : 0.f;
+            for (int q = 0; q < 4; ++q) {
+              xa[q] = offa[q] >= 0 ? slots[offa[q] + e] : 0.f;
+              xb[q] = offb[q] >= 0 ? slots[offb[q] + e] : 0.f;
+            }
+#pragma unroll
+            for (int q = 0; q < 4; ++q)
+#pragma unroll
+              for (int u = 0; u < 4; ++u) v[q * 4 + u] = fmaf(xa[q], xb[u], v[q * 4 + u]);
           }
+        };
+        if constexpr (MODE == 1) {
+          if (((m | rs) & 3) == 0) {
+            // 16-byte loads (row offsets and length multiples of 4 floats): a
+            // quarter of the iterations of the scalar loop
+            const float4 z4 = make_float4(0.f, 0.f, 0.f, 0.f);
+            for (int e = 4 * lane; e < m; e += 128) {
+              float4 xa[4], xb[4];
 #pragma unroll
-          for (int q = 0; q < 4; ++q)
+              for (int q = 0; q < 4; ++q) {
+                xa[q] = offa[q] >= 0 ? *reinterpret_cast<const float4*>(slots + offa[q] + e) : z4;
+                xb[q] = offb[q] >= 0 ? *reinterpret_cast<const float4*>(slots + offb[q] + e) : z4;
+              }
 #pragma unroll
-            for (int u = 0; u < 4; ++u) v[q * 4 + u] = fmaf(xa[q], xb[u], v[q * 4 + u]);
+              for (int q = 0; q < 4; ++q)
+#pragma unroll
+                for (int u = 0; u < 4; ++u) {
+                  float t = v[q * 4 + u];
+                  t = fmaf(xa[q].x, xb[u].x, t);
+                  t = fmaf(xa[q].y, xb[u].y, t);
+                  t = fmaf(xa[q].z, xb[u].z, t);
+                  v[q * 4 + u] = fmaf(xa[q].w, xb[u].w, t);
+                }
+            }
+          } else {
+            gram_scalar();
+          }
+        } else {
+          gram_scalar();
         }
 #pragma unroll
         for (int h = 8, o = 16; o > 1; h >>= 1, o >>= 1) {
