@@ -343,6 +343,36 @@ def to_tensor(cores: Cores) -> np.ndarray:
     return T.reshape(phys)
 
 
+def mps_apply(cores: Cores, gate: np.ndarray, index: int) -> Cores:
+    """``MatrixProductState.apply(gate, index)`` with ``strict=True``
+    (``tensor/matrix_product_state.py:487-534``): a dense operator with axes
+    ``(out_1..out_m, in_1..in_m)`` acts on sites ``index .. index+m-1``; the
+    contracted window ``T[l, out.., r]`` is split back left to right by complete
+    QR, keeping ``Q[:, :r_k]`` (``r_k`` the site's original right bond) as core
+    k and reshaping ``R[:r_k, :]`` to ``(r_k, -1, r_{k+1})`` (the reference's
+    reshape, row-major, whatever the window length); the last window core is
+    the remainder.  Shapes follow the reference's ``tensoricization``, so a
+    window whose sizes do not fit raises numpy's ValueError as it does."""
+    shapes = [tuple(c.shape) for c in cores]
+    out = list(cores)
+    m = gate.ndim // 2
+    T = cores[index]
+    for k in range(index + 1, index + m):
+        T = np.tensordot(T, cores[k], axes=([T.ndim - 1], [0]))
+    l, r = T.shape[0], T.shape[-1]
+    p_in = int(np.prod(gate.shape[m:]))
+    p_out = int(np.prod(gate.shape[:m]))
+    T = np.einsum("oi,lir->lor", gate.reshape(p_out, p_in), T.reshape(l, p_in, r))
+    T = T.reshape((l,) + tuple(gate.shape[:m]) + (r,))
+    for k in range(index, index + m - 1):
+        L_ = T.reshape(T.shape[1] * T.shape[0], -1)
+        Q, R = _complete_qr_keep(L_, shapes[k][2])
+        out[k] = np.reshape(Q, shapes[k])
+        T = R.reshape((shapes[k][2], -1, shapes[k + 1][2]))
+    out[index + m - 1] = np.reshape(T, shapes[index + m - 1])
+    return out
+
+
 def mpo_to_tensor(cores: Cores) -> np.ndarray:
     """Dense ``(*in, *out)`` tensor of an MPO
     (``tensor/matrix_product_operator.py:405-416``)."""

@@ -302,6 +302,79 @@ def to_tensor_device(cores: Cores) -> torch.Tensor:
     return T.reshape(-1)
 
 
+def _reshape_or_raise(count: int, shape) -> None:
+    """numpy's reshape rule: ``count`` elements into ``shape`` (one -1 allowed)."""
+    known = 1
+    for s in shape:
+        if s != -1:
+            known *= int(s)
+    ok = (count == known) if -1 not in shape else (known > 0 and count % known == 0)
+    if not ok:
+        raise ValueError("cannot reshape array of size %d into shape %s" % (count, tuple(shape)))
+
+
+def apply_window(cores: Cores, gate: torch.Tensor, index: int) -> Cores:
+    """``MatrixProductState.apply`` (matrix_product_state.py:487-534) on the
+    device: contract sites ``index .. index+m-1`` into ``T[l, in.., r]`` (GEMM
+    chain), apply the dense operator (axes ``(out_1..out_m, in_1..in_m)``) as one
+    batched GEMM over the left bond, then split ``T`` back left to right: the
+    QR of ``L = T(l * p, rest)`` keeps the first ``r_k`` columns of the complete
+    Q as core k (``r_k`` the site's original right bond; same sign convention as
+    the reference's complete QR) and carries ``R[:r_k, :] = Q^T L`` reshaped,
+    row-major, to ``(r_k, -1, r_{k+1})`` exactly as the reference does.  Returns
+    a new list (the window replaced, other cores shared); the input is left
+    unchanged.  Shapes that numpy cannot reshape raise ValueError."""
+    _check(cores)
+    g = L.as_device(gate)
+    if not g.is_contiguous():
+        g = g.contiguous()
+    m = g.dim() // 2
+    n = len(cores)
+    if m < 1 or index < 0 or index + m > n:
+        raise IndexError("list index out of range")
+    shapes = [tuple(int(s) for s in c.shape) for c in cores]
+    out_legs = tuple(int(s) for s in g.shape[:m])
+    p_out = int(np.prod(out_legs))
+    p_in = int(np.prod(g.shape[m:]))
+    win = cores[index:index + m]
+    lw, rw = shapes[index][0], shapes[index + m - 1][-1]
+    phys_in = int(np.prod([shape3(c)[1] for c in win]))
+    if phys_in != p_in:
+        raise ValueError("operands could not be broadcast together: operator input %d vs sites %d"
+                         % (p_in, phys_in))
+    T = to_tensor_device(win) if m > 1 else win[0].reshape(-1)
+    # T'[l] (p_out x r) = G (p_out x p_in) @ T[l] (p_in x r), batched over l
+    Tg = empty((lw, p_out, rw))
+    L.call("sgt_gemm_f64", 0, 0, p_out, rw, p_in, 1.0, L.ptr(g), p_in, 0, L.ptr(T), rw, p_in * rw,
+           0.0, L.ptr(Tg), rw, p_out * rw, lw, L.stream_ptr())
+    out = list(cores)
+    rows, cur = lw, Tg.reshape(-1)
+    first_leg = out_legs[0]
+    for k in range(index, index + m - 1):
+        mrows = rows * first_leg
+        ncols = cur.numel() // mrows
+        rank = shapes[k][2]
+        keep = min(rank, mrows)
+        _reshape_or_raise(mrows * keep, shapes[k])
+        A = cur.reshape(mrows, ncols).clone()
+        Q = empty((mrows, keep))
+        tau = empty((min(mrows, ncols),))
+        ws = L.workspace(L.query("sgt_qr_workspace_size", mrows, ncols, keep))
+        L.call("sgt_qr", L.ptr(A), mrows, ncols, ncols, L.ptr(tau), L.ptr(Q), keep, L.ptr(ws), ws.numel(),
+               L.stream_ptr())
+        out[k] = Q.reshape(shapes[k])
+        # R[:keep, :] = Q^T L
+        Rk = empty((keep, ncols))
+        _gemm(True, False, keep, ncols, mrows, 1.0, Q, keep, cur, ncols, 0.0, Rk, ncols)
+        nxt_r = shapes[k + 1][2]
+        _reshape_or_raise(keep * ncols, (rank, -1, nxt_r))
+        mid = keep * ncols // (rank * nxt_r)
+        rows, first_leg, cur = rank, mid, Rk.reshape(-1)
+    _reshape_or_raise(cur.numel(), shapes[index + m - 1])
+    out[index + m - 1] = cur.reshape(shapes[index + m - 1])
+    return out
+
+
 def retrieve(cores: Cores, indices: Sequence[int]) -> float:
     """One element (matrix_product_state.py:546-551): product of the slices
     ``core_k[:, i_k, :]``."""

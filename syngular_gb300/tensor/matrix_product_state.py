@@ -201,6 +201,19 @@ class MatrixProductState:
             return out
         return _ops.qr_truncate(cores, dim)
 
+    def apply(self, operator, index, strict=True, mode="compress"):
+        """A dense operator (axes ``(out_1..out_m, in_1..in_m)``, numpy or
+        torch) on sites ``index .. index+m-1``, split back into cores of the
+        original shapes by truncated QR (mps:487-534), on the device.  With
+        ``strict`` it works on a copy and returns it.  The reference has no
+        working copy when ``strict`` is False and raises NameError; so does this.
+        ``mode`` is accepted and unused, as in the reference."""
+        if not strict:
+            raise NameError("name 'that' is not defined")
+        that = self.copy()
+        that.sites = _ops.apply_window(that.sites, operator, int(index))
+        return that
+
     def retrieve(self, indices):
         """One tensor element (mps:546-551)."""
         return np.float64(_ops.retrieve(self.sites, indices))

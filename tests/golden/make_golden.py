@@ -380,21 +380,65 @@ def random_cases(st: Store):
     st.put("decompose_mpo", "Z_shape", np.array(D.shape))
 
 
+def apply_cases(st: Store):
+    """``MatrixProductState.apply`` (tensor/matrix_product_state.py:487-534)."""
+    import importlib.util
+    spec = importlib.util.spec_from_file_location(
+        "syngular_gate", os.path.join(ref_shim.REFERENCE_ROOT, "quantum", "gate.py"))
+    gate = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(gate)  # numpy-only module (the quantum package needs matplotlib)
+
+    # test/test_mps.py:9-19 test_apply: CX on sites 1, 2 of arange(8)
+    x = np.arange(8).reshape((2, 2, 2))
+    with quiet():
+        X = MPS(x, bond_shape=(2, 2)).decompose()
+        g = np.asarray(gate.CX, dtype=np.float64).reshape((2, 2, 2, 2))
+        Y = X.apply(g, 1)
+    st.put("test_apply", "x", cores(X))
+    st.put("test_apply", "gate", g)
+    st.put("test_apply", "index", 1)
+    st.put("test_apply", "out", cores(Y))
+    st.put("test_apply", "x_after", cores(X))  # strict: the input is unchanged
+
+    # seeded cores, one- and two-site operators (gates and general matrices)
+    rng = np.random.default_rng(2024)
+    cases = [
+        ("h_site0", (2, 2, 2, 2, 2), (2, 4, 4, 2), np.asarray(gate.H, dtype=np.float64), 0),
+        ("x_site4", (2, 2, 2, 2, 2), (2, 4, 4, 2), np.asarray(gate.X, dtype=np.float64), 4),
+        ("cx_site1", (2, 2, 2, 2, 2), (2, 4, 4, 2), np.asarray(gate.CX, dtype=np.float64).reshape(2, 2, 2, 2), 1),
+        ("swap_site3", (2, 2, 2, 2, 2), (2, 4, 4, 2), np.asarray(gate.SWAP, dtype=np.float64).reshape(2, 2, 2, 2), 3),
+        ("rand2_d3", (3, 3, 3, 3), (3, 9, 3), rng.standard_normal((3, 3, 3, 3)), 1),
+        ("rand1_d4", (4, 4, 4), (4, 4), rng.standard_normal((4, 4)), 1),
+        ("rand2_d2_wide", (2, 2, 2, 2, 2, 2), (2, 4, 8, 4, 2), rng.standard_normal((2, 2, 2, 2)), 2),
+    ]
+    for name, phys, bonds, g, idx in cases:
+        xs = rnd_mps(rng, phys, bonds)
+        with quiet():
+            X = MPS.from_sites([c.copy() for c in xs])
+            Y = X.apply(g, idx)
+        st.put(name, "x", xs)
+        st.put(name, "gate", g)
+        st.put(name, "index", idx)
+        st.put(name, "out", cores(Y))
+
+
+GROUPS = {
+    "readme_flow": readme_flow,
+    "config1": config1,
+    "known_answers": known_answers,
+    "random_cases": random_cases,
+    "apply_cases": apply_cases,
+}
+
+
 def main():
+    """``python make_golden.py [group ...]``: every group, or the ones named."""
     import time
     t0 = time.time()
-    st = Store()
-    readme_flow(st)
-    st.save("readme_flow.npz")
-    st = Store()
-    config1(st)
-    st.save("config1.npz")
-    st = Store()
-    known_answers(st)
-    st.save("known_answers.npz")
-    st = Store()
-    random_cases(st)
-    st.save("random_cases.npz")
+    for name in (sys.argv[1:] or list(GROUPS)):
+        st = Store()
+        GROUPS[name](st)
+        st.save(name + ".npz")
     print("golden fixtures written to", HERE, "in %.1f s" % (time.time() - t0))
 
 

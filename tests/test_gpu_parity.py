@@ -410,3 +410,41 @@ def test_svd_round_exact_when_chi_covers_rank():
     P = O.mpo_mps_product(W, X)
     Z, *_ = _ops.svd_round(_ops.contract_mpo_mps(dev(W), dev(X)), 1000)
     assert rel(O.to_tensor(host(Z)), O.to_tensor(P)) < 1e-12
+
+
+APPLY_CASES = ["test_apply", "h_site0", "x_site4", "cx_site1", "swap_site3", "rand2_d3", "rand1_d4",
+               "rand2_d2_wide"]
+
+
+@pytest.mark.parametrize("case", APPLY_CASES)
+def test_mps_apply(golden, case):
+    """MatrixProductState.apply on the device against the reference's cores
+    (same QR sign convention, so the cores agree directly) and the oracle; the
+    input state is unchanged (strict copy)."""
+    g = golden("apply_cases.npz")
+    xs, gate, idx = g(case, "x"), g(case, "gate"), int(g(case, "index"))
+    X = mps(xs)
+    Y = X.apply(gate, idx)
+    ref = g(case, "out")
+    out = host(Y.sites)
+    assert [c.shape for c in out] == [c.shape for c in ref]
+    for a, b in zip(out, ref):
+        assert rel(a, b) < TOL
+    for a, b in zip(out, O.mps_apply(xs, gate, idx)):
+        assert rel(a, b) < TOL
+    for a, b in zip(host(X.sites), xs):
+        np.testing.assert_array_equal(a, b)
+    assert Y.shape == X.shape
+
+
+def test_mps_apply_errors():
+    """The reference's failures: no working copy without strict (NameError),
+    a window past the last site (IndexError)."""
+    rng = np.random.default_rng(3)
+    xs = [rng.standard_normal(s) for s in [(1, 2, 2), (2, 2, 2), (2, 2, 1)]]
+    X = mps(xs)
+    cx = np.eye(4)[[0, 1, 3, 2]].reshape(2, 2, 2, 2)
+    with pytest.raises(NameError):
+        X.apply(cx, 0, strict=False)
+    with pytest.raises(IndexError):
+        X.apply(cx, 2)

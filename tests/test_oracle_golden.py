@@ -185,3 +185,27 @@ def test_tt_svd_round_identities():
     Z, spec, disc = O.tt_svd_round(P, 3)
     err = np.linalg.norm(O.to_tensor(Z) - T) ** 2 / np.linalg.norm(T) ** 2
     assert err <= sum(disc) * (1 + 1e-9)
+
+
+APPLY_CASES = ["test_apply", "h_site0", "x_site4", "cx_site1", "swap_site3", "rand2_d3", "rand1_d4",
+               "rand2_d2_wide"]
+
+
+@pytest.mark.parametrize("case", APPLY_CASES)
+def test_mps_apply(golden, case):
+    """MatrixProductState.apply: the oracle's cores agree with the reference's
+    directly (complete QR keeps LAPACK's sign convention), and the input chain is
+    left unchanged (strict copy)."""
+    g = golden("apply_cases.npz")
+    xs = g(case, "x")
+    before = [c.copy() for c in xs]
+    out = O.mps_apply(xs, g(case, "gate"), int(g(case, "index")))
+    ref = g(case, "out")
+    assert [c.shape for c in out] == [c.shape for c in ref]
+    for a, b in zip(out, ref):
+        assert rel(a, b) < TOL
+    for a, b in zip(xs, before):
+        np.testing.assert_array_equal(a, b)
+    if case == "test_apply":
+        for a, b in zip(xs, g(case, "x_after")):
+            np.testing.assert_array_equal(a, b)
