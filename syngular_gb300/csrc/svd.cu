@@ -1166,14 +1166,15 @@ __global__ void __launch_bounds__(BJ_THREADS) gjacobi_kernel(float* __restrict__
 
 // Vt = (the logged rotations of gjacobi_kernel<1>, in order) applied to I.
 // Columns of Vt transform independently under row rotations, so each CTA
-// replays the whole log on a slice of RP_COLS columns held in shared memory
-// (all 2 cs bs block rows) and needs no other CTA.  The log of step s + 1
+// replays the whole log on a slice of COLS (4 or 8) columns held in shared
+// memory (all 2 cs bs block rows) and needs no other CTA; 4-column slices
+// spread a 512-column Vt over 128 CTAs instead of 64.  The log of step s + 1
 // (the cs rotation matrices, rows padded to 36 floats so that the 16-byte
 // loads of the 8 rows a quarter-warp reads fall in distinct banks, and the
 // block ids) streams into the other half of a double buffer with cp.async
 // while step s computes every working row of its rotated pairs into
 // registers; the rows are written back after a barrier.
-constexpr int RP_COLS = 8, RP_THREADS = 256, RP_QS = GJ_W + 4;
+constexpr int RP_THREADS = 256, RP_QS = GJ_W + 4;
 
 __device__ __forceinline__ void cp_async16(void* dst, const void* src) {
   const unsigned d = (unsigned)__cvta_generic_to_shared(dst);
@@ -1187,18 +1188,19 @@ __device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commi
 template <int N>
 __device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory"); }
 
+template <int COLS>
 __global__ void __launch_bounds__(RP_THREADS) gj_replay_kernel(const float* __restrict__ qlog,
                                                                const int* __restrict__ blog,
                                                                const int* __restrict__ status, int n, int cs, int bs,
                                                                float* __restrict__ Vt, int64_t ldv) {
   extern __shared__ __align__(16) float rp_smem[];
   const int nrows = 2 * cs * bs, weff = 2 * bs;
-  float* V = rp_smem;                                   // [nrows][RP_COLS]
-  float* Qb = V + nrows * RP_COLS;                      // [2][cs][GJ_W][RP_QS]
+  float* V = rp_smem;                                   // [nrows][COLS]
+  float* Qb = V + nrows * COLS;                      // [2][cs][GJ_W][RP_QS]
   __shared__ int s_b[2][2 * 16];
-  const int c0 = blockIdx.x * RP_COLS, tid = threadIdx.x;
+  const int c0 = blockIdx.x * COLS, tid = threadIdx.x;
   const int qstride = cs * GJ_W * RP_QS;
-  for (int i = tid; i < nrows * RP_COLS; i += RP_THREADS) V[i] = (i / RP_COLS == c0 + i % RP_COLS) ? 1.f : 0.f;
+  for (int i = tid; i < nrows * COLS; i += RP_THREADS) V[i] = (i / COLS == c0 + i % COLS) ? 1.f : 0.f;
   const int st = *status;
   const int sweeps = st > 0 ? st : (st < 0 ? JAC_MAX_SWEEPS : 0);
   const int64_t nsteps = (int64_t)sweeps * (2 * cs - 1);
@@ -1225,7 +1227,7 @@ __global__ void __launch_bounds__(RP_THREADS) gj_replay_kernel(const float* __re
     __syncthreads();
     int any = 0;
     for (int c = 0; c < cs; ++c) any |= (s_b[cur][2 * c] >= 0);
-    float out[2][RP_COLS];
+    float out[2][COLS];
     int orow[2] = {-1, -1};
     if (any) {
 #pragma unroll
@@ -1237,7 +1239,7 @@ __global__ void __launch_bounds__(RP_THREADS) gj_replay_kernel(const float* __re
         if (A < 0) continue;
         const float* q = Qb + cur * qstride + (c * GJ_W + r) * RP_QS;
 #pragma unroll
-        for (int u = 0; u < RP_COLS; ++u) out[k][u] = 0.f;
+        for (int u = 0; u < COLS; ++u) out[k][u] = 0.f;
         for (int j4 = 0; j4 < weff / 4; ++j4) {
           const float4 q4 = *reinterpret_cast<const float4*>(q + 4 * j4);
           const float qv[4] = {q4.x, q4.y, q4.z, q4.w};
@@ -1245,21 +1247,20 @@ __global__ void __launch_bounds__(RP_THREADS) gj_replay_kernel(const float* __re
           for (int jj = 0; jj < 4; ++jj) {
             const int j = 4 * j4 + jj;
             const int vr = (j < bs) ? A * bs + j : B * bs + (j - bs);
-            const float4 v0 = *reinterpret_cast<const float4*>(V + vr * RP_COLS);
-            const float4 v1 = *reinterpret_cast<const float4*>(V + vr * RP_COLS + 4);
-            out[k][0] = fmaf(qv[jj], v0.x, out[k][0]);
-            out[k][1] = fmaf(qv[jj], v0.y, out[k][1]);
-            out[k][2] = fmaf(qv[jj], v0.z, out[k][2]);
-            out[k][3] = fmaf(qv[jj], v0.w, out[k][3]);
-            out[k][4] = fmaf(qv[jj], v1.x, out[k][4]);
-            out[k][5] = fmaf(qv[jj], v1.y, out[k][5]);
-            out[k][6] = fmaf(qv[jj], v1.z, out[k][6]);
-            out[k][7] = fmaf(qv[jj], v1.w, out[k][7]);
+#pragma unroll
+            for (int h = 0; h < COLS / 4; ++h) {
+              const float4 v = *reinterpret_cast<const float4*>(V + vr * COLS + 4 * h);
+              out[k][4 * h + 0] = fmaf(qv[jj], v.x, out[k][4 * h + 0]);
+              out[k][4 * h + 1] = fmaf(qv[jj], v.y, out[k][4 * h + 1]);
+              out[k][4 * h + 2] = fmaf(qv[jj], v.z, out[k][4 * h + 2]);
+              out[k][4 * h + 3] = fmaf(qv[jj], v.w, out[k][4 * h + 3]);
+            }
           }
         }
         for (int j = 4 * (weff / 4); j < weff; ++j) {
           const int vr = (j < bs) ? A * bs + j : B * bs + (j - bs);
-          for (int u = 0; u < RP_COLS; ++u) out[k][u] = fmaf(q[j], V[vr * RP_COLS + u], out[k][u]);
+#pragma unroll
+          for (int u = 0; u < COLS; ++u) out[k][u] = fmaf(q[j], V[vr * COLS + u], out[k][u]);
         }
         orow[k] = (r < bs) ? A * bs + r : B * bs + (r - bs);
       }
@@ -1268,14 +1269,15 @@ __global__ void __launch_bounds__(RP_THREADS) gj_replay_kernel(const float* __re
 #pragma unroll
     for (int k = 0; k < 2; ++k) {
       if (orow[k] < 0) continue;
-      float4* d = reinterpret_cast<float4*>(V + orow[k] * RP_COLS);
-      d[0] = make_float4(out[k][0], out[k][1], out[k][2], out[k][3]);
-      d[1] = make_float4(out[k][4], out[k][5], out[k][6], out[k][7]);
+      float4* d = reinterpret_cast<float4*>(V + orow[k] * COLS);
+#pragma unroll
+      for (int h = 0; h < COLS / 4; ++h)
+        d[h] = make_float4(out[k][4 * h], out[k][4 * h + 1], out[k][4 * h + 2], out[k][4 * h + 3]);
     }
   }
   __syncthreads();
-  for (int i = tid; i < n * RP_COLS; i += RP_THREADS) {
-    const int r = i / RP_COLS, c = c0 + i % RP_COLS;
+  for (int i = tid; i < n * COLS; i += RP_THREADS) {
+    const int r = i / COLS, c = c0 + i % COLS;
     if (c < n) Vt[(int64_t)r * ldv + c] = V[i];
   }
 }
@@ -1616,14 +1618,22 @@ int sym_eig_rows_f32(cudaStream_t st, float* Z, int64_t n, float* Vt, float* lam
     if (!launched) return jacobi_rows_f32(st, Z, n, n, n, Vt, n, lam, status, ar0);
     const int cs = gj_cluster(n);
     const int bsz = (int)cdiv(n, 2 * cs);
-    const size_t smem = sizeof(float) * ((size_t)2 * cs * bsz * RP_COLS + (size_t)2 * cs * GJ_W * RP_QS);
+    // 8-column slices unless that leaves most SMs idle
+    const int cols = cdiv(n, 8) >= 128 ? 8 : 4;
+    const size_t smem = sizeof(float) * ((size_t)2 * cs * bsz * cols + (size_t)2 * cs * GJ_W * RP_QS);
     static bool rp_attr = false;
     if (!rp_attr) {
-      SGT_CUDA(cudaFuncSetAttribute(gj_replay_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                    (int)(sizeof(float) * ((size_t)2 * 16 * (GJ_W / 2) * RP_COLS + 2 * 16 * GJ_W * RP_QS))));
+      const size_t qb = sizeof(float) * (size_t)2 * 16 * GJ_W * RP_QS;
+      SGT_CUDA(cudaFuncSetAttribute(gj_replay_kernel<8>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                    (int)(sizeof(float) * (size_t)2 * 16 * (GJ_W / 2) * 8 + qb)));
+      SGT_CUDA(cudaFuncSetAttribute(gj_replay_kernel<4>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                    (int)(sizeof(float) * (size_t)2 * 16 * (GJ_W / 2) * 4 + qb)));
       rp_attr = true;
     }
-    gj_replay_kernel<<<(unsigned)cdiv(n, RP_COLS), RP_THREADS, smem, st>>>(qlog, blog, status, (int)n, cs, bsz, Vt, n);
+    if (cols == 8)
+      gj_replay_kernel<8><<<(unsigned)cdiv(n, 8), RP_THREADS, smem, st>>>(qlog, blog, status, (int)n, cs, bsz, Vt, n);
+    else
+      gj_replay_kernel<4><<<(unsigned)cdiv(n, 4), RP_THREADS, smem, st>>>(qlog, blog, status, (int)n, cs, bsz, Vt, n);
     SGT_LAUNCHED();
     SGT_TRY(sort_rows_t<float>(st, Z, n, n, n, Vt, n, lam, norms, perm, Gtmp, Vtmp));
     return SGT_OK;
