@@ -249,6 +249,18 @@ SGT_API int sgt_tc_gemm_f32(int passes, int64_t M, int64_t N, int64_t K, float a
                             const float* B_hi, const float* B_lo, int64_t ldb, float beta,
                             float* C, int64_t ldc, int* err, void* stream);
 
+/* The same GEMM with a workspace: when the output has too few 128 x 128 tiles
+ * to occupy the GPU, K is split over up to 8 CTAs per tile, each storing its
+ * partial tile into the workspace, and a second kernel adds the slices in a
+ * fixed order into beta * C (deterministic).  The size query gives the bytes
+ * that allow the full split (0: no split for this shape); a smaller workspace
+ * gives fewer splits, none at 0 bytes. */
+SGT_API size_t sgt_tc_gemm_f32_workspace_size(int64_t M, int64_t N, int64_t K);
+SGT_API int sgt_tc_gemm_f32_ws(int passes, int64_t M, int64_t N, int64_t K, float alpha,
+                               const float* A_hi, const float* A_lo, int64_t lda,
+                               const float* B_hi, const float* B_lo, int64_t ldb, float beta,
+                               float* C, int64_t ldc, int* err, void* ws, size_t ws_bytes, void* stream);
+
 /* Event timing of tensor-core GEMM launches: enable = 1 starts recording a
  * CUDA event pair around every sgt tcgen05 GEMM launch (on its stream);
  * enable = 0 stops, waits for the recorded events and returns the summed

@@ -68,6 +68,8 @@ SIGNATURES = {
     "sgt_jacobi_svd_workspace_size": (_c_size, [_c_i64, _c_i64]),
     "sgt_jacobi_svd": (_c_int, [_c_vp, _c_i64, _c_i64, _c_vp, _c_vp, _c_vp, _c_vp, _c_size, _c_vp]),
     "sgt_tc_gemm_f32": (_c_int, [_c_int, _c_i64, _c_i64, _c_i64, ctypes.c_float, _c_vp, _c_vp, _c_i64, _c_vp, _c_vp, _c_i64, ctypes.c_float, _c_vp, _c_i64, _c_vp, _c_vp]),
+    "sgt_tc_gemm_f32_workspace_size": (_c_size, [_c_i64, _c_i64, _c_i64]),
+    "sgt_tc_gemm_f32_ws": (_c_int, [_c_int, _c_i64, _c_i64, _c_i64, ctypes.c_float, _c_vp, _c_vp, _c_i64, _c_vp, _c_vp, _c_i64, ctypes.c_float, _c_vp, _c_i64, _c_vp, _c_vp, _c_size, _c_vp]),
     "sgt_split_tf32": (_c_int, [_c_vp, _c_vp, _c_vp, _c_i64, _c_vp]),
     "sgt_launch_count": (ctypes.c_ulonglong, []),
     "sgt_sym_eig_f32_workspace_size": (_c_size, [_c_i64]),

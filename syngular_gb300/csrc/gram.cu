@@ -23,10 +23,10 @@ namespace sgt {
 
 int tc_gemm_tf32(cudaStream_t st, int passes, int64_t M, int64_t N, int64_t K, float alpha,
                  const float* Ahi, const float* Alo, int64_t lda, const float* Bhi, const float* Blo,
-                 int64_t ldb, float beta, float* C, int64_t ldc, int* err);
+                 int64_t ldb, float beta, float* C, int64_t ldc, int* err, float* part, int64_t part_floats);
 int gemm_nt_dispatch(cudaStream_t st, int passes, int64_t M, int64_t N, int64_t K, float alpha, const float* Ah,
                      const float* Al, int64_t lda, const float* Bh, const float* Bl, int64_t ldb, float beta,
-                     float* C, int64_t ldc, int* err);
+                     float* C, int64_t ldc, int* err, float* part = nullptr, int64_t part_floats = 0);
 
 namespace {
 

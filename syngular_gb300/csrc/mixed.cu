@@ -38,7 +38,7 @@ void svd_round_plan_public(int n, const int64_t* shape, int64_t chi, std::vector
                            std::vector<int64_t>& x, std::vector<int64_t>& cnt);
 int tc_gemm_tf32(cudaStream_t st, int passes, int64_t M, int64_t N, int64_t K, float alpha,
                  const float* Ahi, const float* Alo, int64_t lda, const float* Bhi, const float* Blo,
-                 int64_t ldb, float beta, float* C, int64_t ldc, int* err);
+                 int64_t ldb, float beta, float* C, int64_t ldc, int* err, float* part, int64_t part_floats);
 int split_tf32(cudaStream_t st, const float* x, float* hi, float* lo, int64_t n);
 int split_f64(cudaStream_t st, const double* x, int64_t ldx, float* hi, float* lo, int64_t rows,
               int64_t cols);
@@ -335,15 +335,18 @@ struct Site4 {
 }  // namespace
 
 // C = alpha A B^T + beta C (A: M x K, B: N x K, row-major fp32 hi/lo pairs).
-// tcgen05 when TMA can address the operands, CUDA cores otherwise.
+// tcgen05 when TMA can address the operands, CUDA cores otherwise; `part`
+// (part_floats floats, may be null) lets the tensor-core GEMM split K when the
+// output has few tiles.
 int gemm_nt_dispatch(cudaStream_t st, int passes, int64_t M, int64_t N, int64_t K, float alpha, const float* Ah,
             const float* Al, int64_t lda, const float* Bh, const float* Bl, int64_t ldb, float beta,
-            float* C, int64_t ldc, int* err) {
+            float* C, int64_t ldc, int* err, float* part = nullptr, int64_t part_floats = 0) {
   if (M <= 0 || N <= 0) return SGT_OK;
   auto al16 = [](const void* p) { return (reinterpret_cast<uintptr_t>(p) & 15) == 0; };
   const bool tc_ok = K >= 16 && lda % 4 == 0 && ldb % 4 == 0 && al16(Ah) && al16(Bh) &&
                      (passes == 1 || (al16(Al) && al16(Bl))) && M * N * K >= (int64_t)1 << 22;
-  if (tc_ok) return tc_gemm_tf32(st, passes, M, N, K, alpha, Ah, Al, lda, Bh, Bl, ldb, beta, C, ldc, err);
+  if (tc_ok)
+    return tc_gemm_tf32(st, passes, M, N, K, alpha, Ah, Al, lda, Bh, Bl, ldb, beta, C, ldc, err, part, part_floats);
   dim3 g((unsigned)cdiv(N, 64), (unsigned)cdiv(M, 64));
   gemm_nt_f32_kernel<<<g, 256, 0, st>>>(M, N, std::max<int64_t>(K, 0), alpha, Ah, passes == 3 ? Al : nullptr,
                                         lda, Bh, passes == 3 ? Bl : nullptr, ldb, beta, C, ldc);
@@ -433,6 +436,9 @@ static int mixed_round_impl(cudaStream_t st, int n, const double* const* W, cons
   float* pWh = ar.take<float>(wmax);
   float* pWl = ar.take<float>(wmax);
   double* skw = ar.take<double>(16 * chi * cmax);  // split-K partials of the FP64 re-orthonormalisation
+  // split-K slices of the tensor-core GEMMs whose outputs have few tiles
+  const int64_t tcp = std::min<int64_t>((int64_t)1 << 21, 8 * rmax * std::max<int64_t>(cmax, chi));
+  float* tcpart = ar.take<float>(tcp);
   int* stat = ar.take<int>(n + 1);
   int* tc_err = ar.take<int>(1);
   int* gexp = ar.take<int>(n + 1);
@@ -512,7 +518,7 @@ static int mixed_round_impl(cudaStream_t st, int n, const double* const* W, cons
     // Yt (c x r): rows p*xc..: Ft (xc x r2) * P[:, p, :]^T
     for (int64_t pi = 0; pi < p; ++pi) {
       SGT_TRY(gemm_nt_dispatch(st, passes, xc, r, r2, 1.f, Fth, Ftl, r2, Ph[k] + pi * r2, Pl[k] + pi * r2, p * r2,
-                      0.f, Yt + pi * xc * r, r, tc_err));
+                      0.f, Yt + pi * xc * r, r, tc_err, tcpart, tcp));
     }
     if (k == 0) {
       // core_0[0][p][c] = Yt[p*xc + c][0]
@@ -528,12 +534,13 @@ static int mixed_round_impl(cudaStream_t st, int n, const double* const* W, cons
       const int64_t chik = xs[3 * k], Dk = w[k].b;
       SGT_TRY(transpose_f32(st, Ytp, chik, r, Yt, Dk, r, chik, Dk, c));
       SGT_TRY(split_tf32(st, Ytp, Y, Yl, c * r));  // Y / Yl reused as the split of Ytp
-      SGT_TRY(gemm_nt_dispatch(st, passes, c, r, r, 1.f, Y, Yl, r, Gh[k], Gl[k], r, 0.f, GY, r, tc_err));
+      SGT_TRY(gemm_nt_dispatch(st, passes, c, r, r, 1.f, Y, Yl, r, Gh[k], Gl[k], r, 0.f, GY, r, tc_err, tcpart, tcp));
     } else {
-      SGT_TRY(gemm_nt_dispatch(st, passes, c, r, r, 1.f, Yth, Ytl, r, Gh[k], Gl[k], r, 0.f, GY, r, tc_err));
+      SGT_TRY(gemm_nt_dispatch(st, passes, c, r, r, 1.f, Yth, Ytl, r, Gh[k], Gl[k], r, 0.f, GY, r, tc_err, tcpart,
+                               tcp));
     }
     SGT_TRY(split_tf32(st, GY, GYh, GYl, c * r));
-    SGT_TRY(gemm_nt_dispatch(st, passes, c, c, r, 1.f, Yth, Ytl, r, GYh, GYl, r, 0.f, Z, c, tc_err));
+    SGT_TRY(gemm_nt_dispatch(st, passes, c, c, r, 1.f, Yth, Ytl, r, GYh, GYl, r, 0.f, Z, c, tc_err, tcpart, tcp));
     symmetrize_kernel<<<gs(c * c), 256, 0, st>>>(Z, c);
     SGT_LAUNCHED();
     // eigenpairs of the symmetric Z: one-sided Jacobi on the rows of Z (block,
@@ -563,7 +570,7 @@ static int mixed_round_impl(cudaStream_t st, int n, const double* const* W, cons
     SGT_TRY(transpose_f32(st, Y, c, 0, Yt, r, 0, c, r, 1));
     SGT_TRY(split_tf32(st, Y, Yh, Yl, r * c));
     SGT_TRY(split_f64(st, out[k], c, Vh, Vl, keep, c));
-    SGT_TRY(gemm_nt_dispatch(st, passes, keep, r, c, 1.f, Vh, Vl, c, Yh, Yl, c, 0.f, Ftn, r, tc_err));
+    SGT_TRY(gemm_nt_dispatch(st, passes, keep, r, c, 1.f, Vh, Vl, c, Yh, Yl, c, 0.f, Ftn, r, tc_err, tcpart, tcp));
     SGT_TRY(split_tf32(st, Ftn, Fth, Ftl, keep * r));
   }
   if (status) {

@@ -16,6 +16,11 @@
 // touch TMEM lanes 32*(w%4)..+31, which are tile rows.
 // Every mbarrier wait has an iteration limit; on expiry the kernel records an
 // error code, skips the remaining work, still frees its TMEM and returns.
+//
+// Split K: with gridDim.z = S > 1, CTA z walks K-tiles [z kps, (z + 1) kps)
+// and stores alpha * its partial tile into slice z of a workspace; a second
+// kernel adds the S slices in a fixed order into beta * C (deterministic).
+// Used when the output has too few 128 x 128 tiles to occupy the GPU.
 #include <cuda.h>
 #include <cudaTypedefs.h>
 
@@ -134,6 +139,8 @@ struct TcArgs {
   float alpha, beta;
   int passes;
   int* err;
+  int kps;          // K-tiles per split (all of them without a split)
+  int64_t pstride;  // elements between the split slices of C
 };
 
 __device__ __forceinline__ void mbar_arrive(uint64_t* bar) {
@@ -164,7 +171,8 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
 
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int m0 = blockIdx.y * TC_BM, n0 = blockIdx.x * TC_BN;
-  const int KT = (args.K + TC_BK - 1) / TC_BK;
+  const int kt0 = (int)blockIdx.z * args.kps;
+  const int KT = min((args.K + TC_BK - 1) / TC_BK - kt0, args.kps);
 
   if (threadIdx.x == 0) {
     s_fail = 0;
@@ -206,7 +214,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
         }
         if (*(volatile int*)&s_fail) break;
         mbar_expect_tx(&full[s], bytes);
-        const int kx = kt * TC_BK;
+        const int kx = (kt0 + kt) * TC_BK;
         tma_load_2d(tile(s, 0), &mA, &full[s], kx, m0);
         tma_load_2d(tile(s, 1), &mB, &full[s], kx, n0);
         if (npass == 3) {
@@ -281,7 +289,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
     ok = ok && !*(volatile int*)&s_fail;
     const int row = m0 + q * 32 + lane;
     if (ok && row < args.M) {
-      float* crow = args.C + (int64_t)row * args.ldc + n0;
+      float* crow = args.C + (int64_t)blockIdx.z * args.pstride + (int64_t)row * args.ldc + n0;
 #pragma unroll
       for (int i = 0; i < TC_BN; ++i) {
         if (n0 + i < args.N) {
@@ -297,6 +305,18 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
     asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(TC_TMEM_COLS));
   }
   if (threadIdx.x == 0 && s_fail && args.err) atomicExch(args.err, 1);
+}
+
+// C = beta C + sum_z part[z] (slices M x N, row-major), z in order.
+__global__ void splitk_sum_f32_kernel(const float* __restrict__ part, int S, int64_t M, int64_t N, float beta,
+                                      float* __restrict__ C, int64_t ldc) {
+  const int64_t mn = M * N;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < mn; i += (int64_t)gridDim.x * blockDim.x) {
+    float acc = part[i];
+    for (int z = 1; z < S; ++z) acc += part[(int64_t)z * mn + i];
+    float* c = C + (i / N) * ldc + (i % N);
+    *c = (beta == 0.f) ? acc : fmaf(beta, *c, acc);
+  }
 }
 
 // cvt.rna.tf32.f32: hi = TF32 rounding of x, lo = x - hi.
@@ -372,9 +392,23 @@ std::vector<ProfRec> g_prof;
 
 }  // namespace
 
+// Number of K splits for an M x N x K product with `part_floats` floats of
+// workspace: enough 128 x 128 tiles x splits to cover ~148 SMs, at least 8
+// K-tiles (256 K) per split, at most 8 splits.
+int tc_splits(int64_t M, int64_t N, int64_t K, int64_t part_floats) {
+  const int64_t tiles = cdiv(N, TC_BN) * cdiv(M, TC_BM);
+  const int64_t kt = cdiv(K, TC_BK);
+  if (part_floats <= 0 || tiles >= 120) return 1;
+  int64_t S = std::min<int64_t>(std::min<int64_t>(8, cdiv(148, tiles)), kt / 8);
+  while (S > 1 && S * M * N > part_floats) --S;
+  if (S <= 1) return 1;
+  const int64_t kps = cdiv(kt, S);
+  return (int)cdiv(kt, kps);
+}
+
 int tc_gemm_tf32(cudaStream_t st, int passes, int64_t M, int64_t N, int64_t K, float alpha,
                  const float* Ahi, const float* Alo, int64_t lda, const float* Bhi, const float* Blo,
-                 int64_t ldb, float beta, float* C, int64_t ldc, int* err) {
+                 int64_t ldb, float beta, float* C, int64_t ldc, int* err, float* part, int64_t part_floats) {
   SGT_REQUIRE(passes == 1 || passes == 3, SGT_ERR_INVALID, "tc_gemm: passes must be 1 or 3");
   SGT_REQUIRE(M > 0 && N > 0 && K > 0, SGT_ERR_INVALID, "tc_gemm: empty problem");
   SGT_REQUIRE(M < (1ll << 31) && N < (1ll << 31) && K < (1ll << 31), SGT_ERR_INVALID, "tc_gemm: too large");
@@ -397,8 +431,17 @@ int tc_gemm_tf32(cudaStream_t st, int passes, int64_t M, int64_t N, int64_t K, f
                                   (int)tc_smem_bytes(3)));
     attr_set = true;
   }
-  TcArgs args{C, ldc, (int)M, (int)N, (int)K, alpha, beta, passes, err};
-  dim3 grid((unsigned)cdiv(N, TC_BN), (unsigned)cdiv(M, TC_BM));
+  const int S = part ? tc_splits(M, N, K, part_floats) : 1;
+  const int KTall = (int)cdiv(K, TC_BK);
+  const int kps = (int)cdiv(KTall, S);
+  TcArgs args{C, ldc, (int)M, (int)N, (int)K, alpha, beta, passes, err, kps, 0};
+  if (S > 1) {  // partial tiles into the workspace, summed below
+    args.C = part;
+    args.ldc = N;
+    args.beta = 0.f;
+    args.pstride = M * N;
+  }
+  dim3 grid((unsigned)cdiv(N, TC_BN), (unsigned)cdiv(M, TC_BM), (unsigned)S);
   SGT_REQUIRE(grid.y <= 65535, SGT_ERR_INVALID, "tc_gemm: M too large");
   ProfRec rec{};
   if (g_prof_on) {
@@ -408,6 +451,11 @@ int tc_gemm_tf32(cudaStream_t st, int passes, int64_t M, int64_t N, int64_t K, f
   }
   tc_gemm_tf32_kernel<<<grid, TC_THREADS, smem, st>>>(ma, mal, mb, mbl, args);
   SGT_LAUNCHED();
+  if (S > 1) {
+    splitk_sum_f32_kernel<<<(unsigned)std::min<int64_t>(cdiv(M * N, 256), 152 * 8), 256, 0, st>>>(part, S, M, N,
+                                                                                                  beta, C, ldc);
+    SGT_LAUNCHED();
+  }
   if (g_prof_on) {
     SGT_CUDA(cudaEventRecord(rec.b, st));
     rec.flops = 2.0 * (double)M * (double)N * (double)K;
@@ -440,7 +488,20 @@ extern "C" SGT_API int sgt_tc_gemm_f32(int passes, int64_t M, int64_t N, int64_t
                                        const float* B_hi, const float* B_lo, int64_t ldb, float beta,
                                        float* C, int64_t ldc, int* err, void* stream) {
   return sgt::tc_gemm_tf32(sgt::as_stream(stream), passes, M, N, K, alpha, A_hi, A_lo, lda, B_hi, B_lo,
-                           ldb, beta, C, ldc, err);
+                           ldb, beta, C, ldc, err, nullptr, 0);
+}
+
+extern "C" SGT_API size_t sgt_tc_gemm_f32_workspace_size(int64_t M, int64_t N, int64_t K) {
+  const int S = sgt::tc_splits(M, N, K, (int64_t)1 << 40);
+  return S > 1 ? (size_t)S * (size_t)M * (size_t)N * sizeof(float) : 0;
+}
+
+extern "C" SGT_API int sgt_tc_gemm_f32_ws(int passes, int64_t M, int64_t N, int64_t K, float alpha,
+                                          const float* A_hi, const float* A_lo, int64_t lda, const float* B_hi,
+                                          const float* B_lo, int64_t ldb, float beta, float* C, int64_t ldc,
+                                          int* err, void* ws, size_t ws_bytes, void* stream) {
+  return sgt::tc_gemm_tf32(sgt::as_stream(stream), passes, M, N, K, alpha, A_hi, A_lo, lda, B_hi, B_lo,
+                           ldb, beta, C, ldc, err, static_cast<float*>(ws), (int64_t)(ws_bytes / sizeof(float)));
 }
 
 extern "C" SGT_API int sgt_tc_profile(int enable, double* ms, double* flops, long long* launches) {

@@ -60,6 +60,11 @@ def test_workspace_queries_and_shape_checks(lib):
     bad, _b = L.shape_array([(1, 2, 4), (3, 2, 1)])
     assert L.query("sgt_overlap_workspace_size", 2, bad, bad) == 0
     assert b"bond mismatch" in lib.sgt_last_error()
+    # split-K slices of the tensor-core GEMM: only for outputs with few tiles
+    assert L.query("sgt_tc_gemm_f32_workspace_size", 512, 512, 4096) == 8 * 512 * 512 * 4
+    assert L.query("sgt_tc_gemm_f32_workspace_size", 256, 4096, 4096) == 3 * 256 * 4096 * 4
+    assert L.query("sgt_tc_gemm_f32_workspace_size", 4096, 4096, 4096) == 0
+    assert L.query("sgt_tc_gemm_f32_workspace_size", 128, 128, 64) == 0
 
 
 def test_svd_round_shapes_match_oracle(lib):
