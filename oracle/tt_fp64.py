@@ -373,6 +373,28 @@ def mps_apply(cores: Cores, gate: np.ndarray, index: int) -> Cores:
     return out
 
 
+def mul(kind1: str, cores1: Cores, kind2: str, cores2: Cores, bonds1=None, bonds2=None):
+    """``syngular.mul(op1, op2, mode="standard")`` (``tensor/utils.py:8-73``);
+    ``kind`` is "mps" or "mpo", ``bonds`` the objects' ``bond_shape``
+    attributes (default: the cores' bonds).  MPS x MPO and MPO x MPS: the site
+    product with the state-major fused bond, then ``>> min_bond``; MPS x MPS:
+    the overlap; MPO x MPO: ``op2``'s output leg contracted with ``op1``'s input
+    leg, ``op2``-major fused bond (utils.py:61-71), then ``>> min_bond``.
+    Returns (kind, cores) or ("scalar", value)."""
+    b1 = bond_shape_of(cores1) if bonds1 is None else tuple(bonds1)
+    b2 = bond_shape_of(cores2) if bonds2 is None else tuple(bonds2)
+    if len(cores1) != len(cores2):
+        raise Exception("both operator do not have the same number of sites")
+    min_bond = min(min(b1), min(b2))
+    if kind1 == "mps" and kind2 == "mpo":
+        return "mps", qr_truncate(mpo_mps_product(cores2, cores1), min_bond)
+    if kind1 == "mpo" and kind2 == "mps":
+        return "mps", qr_truncate(mpo_mps_product(cores1, cores2), min_bond)
+    if kind1 == "mps" and kind2 == "mps":
+        return "scalar", overlap(cores1, cores2)
+    return "mpo", qr_truncate(mpo_mpo_product(cores2, cores1), min_bond)
+
+
 def mpo_to_tensor(cores: Cores) -> np.ndarray:
     """Dense ``(*in, *out)`` tensor of an MPO
     (``tensor/matrix_product_operator.py:405-416``)."""

@@ -422,12 +422,43 @@ def apply_cases(st: Store):
         st.put(name, "out", cores(Y))
 
 
+def mul_cases(st: Store):
+    """``syngular.mul`` (tensor/utils.py:8-73) on decomposed seeded operands."""
+    from syngular.tensor.utils import mul
+
+    rng = np.random.default_rng(77)
+    x = rng.standard_normal((2, 3, 2))
+    y = rng.standard_normal((2, 3, 2))
+    w = rng.standard_normal((2, 3, 2, 2, 3, 2))
+    v = rng.standard_normal((2, 3, 2, 2, 3, 2))
+    with quiet():
+        X = MPS(x, bond_shape=(2, 3)).decompose()
+        Y = MPS(y, bond_shape=(2, 3)).decompose()
+        W = MPO(w, bond_shape=(2, 2)).decompose()
+        V = MPO(v, bond_shape=(3, 2)).decompose()
+        xw = mul(X, W)
+        wx = mul(W, X)
+        xy = mul(X, Y)
+        wv = mul(W, V)
+    st.put("mul", "X", cores(X))
+    st.put("mul", "Y", cores(Y))
+    st.put("mul", "W", cores(W))
+    st.put("mul", "V", cores(V))
+    st.put("mul", "XW", cores(xw))
+    st.put("mul", "XW_tensor", xw.to_tensor())
+    st.put("mul", "WX", cores(wx))
+    st.put("mul", "XY", float(xy))
+    st.put("mul", "WV", cores(wv))
+    st.put("mul", "WV_tensor", wv.to_tensor())
+
+
 GROUPS = {
     "readme_flow": readme_flow,
     "config1": config1,
     "known_answers": known_answers,
     "random_cases": random_cases,
     "apply_cases": apply_cases,
+    "mul_cases": mul_cases,
 }
 
 

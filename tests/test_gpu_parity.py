@@ -448,3 +448,28 @@ def test_mps_apply_errors():
         X.apply(cx, 0, strict=False)
     with pytest.raises(IndexError):
         X.apply(cx, 2)
+
+
+def test_mul(golden):
+    """syngular.mul (tensor/utils.py:8-73) against the reference: shapes and
+    reconstructions of MPS x MPO, MPO x MPS and MPO x MPO (each ending with
+    >> min_bond), the MPS x MPS overlap, and the site-count error."""
+    import syngular_gb300 as syn
+
+    g = golden("mul_cases.npz")
+    X, Y = mps(g("mul", "X")), mps(g("mul", "Y"))
+    W, V = mpo(g("mul", "W")), mpo(g("mul", "V"))
+    xw = syn.mul(X, W)
+    assert [tuple(s) for s in xw.shape] == [c.shape for c in g("mul", "XW")]
+    assert rel(xw.to_tensor(), g("mul", "XW_tensor")) < TOL
+    wx = syn.mul(W, X)
+    assert [tuple(s) for s in wx.shape] == [c.shape for c in g("mul", "WX")]
+    assert rel(wx.to_tensor(), O.to_tensor(g("mul", "WX"))) < TOL
+    xy = syn.mul(X, Y)
+    ref = float(g("mul", "XY"))
+    assert abs(float(xy) - ref) <= TOL * abs(ref)
+    wv = syn.mul(W, V)
+    assert [tuple(s) for s in wv.shape] == [c.shape for c in g("mul", "WV")]
+    assert rel(wv.to_tensor(), g("mul", "WV_tensor")) < TOL
+    with pytest.raises(Exception, match="same number of sites"):
+        syn.mul(X, mpo(g("mul", "W")[:2]))

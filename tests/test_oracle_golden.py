@@ -209,3 +209,27 @@ def test_mps_apply(golden, case):
     if case == "test_apply":
         for a, b in zip(xs, g(case, "x_after")):
             np.testing.assert_array_equal(a, b)
+
+
+def test_mul(golden):
+    """syngular.mul (tensor/utils.py:8-73): the oracle's products against the
+    reference's, cores directly (same QR sign convention) and reconstructions."""
+    g = golden("mul_cases.npz")
+    X, Y, W, V = g("mul", "X"), g("mul", "Y"), g("mul", "W"), g("mul", "V")
+    kind, xw = O.mul("mps", X, "mpo", W)
+    assert kind == "mps"
+    for a, b in zip(xw, g("mul", "XW")):
+        assert rel(a, b) < TOL
+    assert rel(O.to_tensor(xw), g("mul", "XW_tensor")) < TOL
+    _, wx = O.mul("mpo", W, "mps", X)
+    for a, b in zip(wx, g("mul", "WX")):
+        assert rel(a, b) < TOL
+    kind, xy = O.mul("mps", X, "mps", Y)
+    assert kind == "scalar" and abs(xy - float(g("mul", "XY"))) <= TOL * abs(xy)
+    kind, wv = O.mul("mpo", W, "mpo", V)
+    assert kind == "mpo"
+    for a, b in zip(wv, g("mul", "WV")):
+        assert rel(a, b) < TOL
+    assert rel(O.mpo_to_tensor(wv), g("mul", "WV_tensor")) < TOL
+    with pytest.raises(Exception, match="same number of sites"):
+        O.mul("mps", X, "mpo", W[:2])
