@@ -267,6 +267,14 @@ SGT_API int sgt_tc_gemm_f32_ws(int passes, int64_t M, int64_t N, int64_t K, floa
  * kernel milliseconds, algorithmic flops (2 M N K per launch) and launches. */
 SGT_API int sgt_tc_profile(int enable, double* ms, double* flops, long long* launches);
 
+/* Event timing of the cluster-resident FP32 eigensolver (the Gram form's bond
+ * solve, gjacobi_kernel<1>): enable = 1 starts recording a CUDA event pair
+ * around every launch; enable = 0 stops, waits for the events and returns the
+ * summed kernel milliseconds, the algorithmic FP32 flops (sweeps x n(n-1)/2
+ * pair visits x 12 n per launch, the sweep count read from the launch's
+ * status word) and the number of launches. */
+SGT_API int sgt_eig_profile(int enable, double* ms, double* flops, long long* launches);
+
 /* Symmetric PSD eigen-decomposition in FP32 (the Gram-form bond solve):
  * Z (n x n, overwritten) -> Vt rows = eigenvectors, lam descending.
  * method 0: two-sided block Jacobi in one thread-block cluster (used when it

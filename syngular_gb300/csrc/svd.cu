@@ -16,6 +16,7 @@
 #include <float.h>
 
 #include <cstdlib>
+#include <vector>
 
 #include "common.cuh"
 
@@ -1598,6 +1599,17 @@ size_t sym_eig_rows_ws_bytes(int64_t n) {
   return a.used + jacobi_rows_ws_bytes_t<float>(n, n);
 }
 
+// Optional event timing of the cluster eigensolver's launches (benchmarks):
+// a CUDA event pair around every gjacobi_kernel<1> launch, on its stream,
+// and the status word that receives its sweep count.
+struct EigProfRec {
+  cudaEvent_t a, b;
+  const int* status;
+  int64_t n;
+};
+bool g_eig_prof_on = false;
+std::vector<EigProfRec> g_eig_prof;
+
 int sym_eig_rows_f32(cudaStream_t st, float* Z, int64_t n, float* Vt, float* lam, int* status, Arena& ar,
                      int method) {
   if (method < 1 || method > 3 || n < 64 || n > 16 * GJ_W)
@@ -1614,7 +1626,30 @@ int sym_eig_rows_f32(cudaStream_t st, float* Z, int64_t n, float* Vt, float* lam
     int* perm = ar.take<int>((size_t)n);
     SGT_REQUIRE(ar.ok(), SGT_ERR_WORKSPACE, "sym_eig: workspace too small");
     bool launched = false;
+    // timing (benchmarks only) never fails the solve: a record whose events
+    // cannot be made is dropped, and its error cleared
+    EigProfRec rec{nullptr, nullptr, status, n};
+    bool prof = false;
+    if (g_eig_prof_on) {
+      prof = cudaEventCreate(&rec.a) == cudaSuccess;
+      if (prof && cudaEventCreate(&rec.b) != cudaSuccess) {
+        cudaEventDestroy(rec.a);
+        rec.a = nullptr;
+        prof = false;
+      }
+      if (prof && cudaEventRecord(rec.a, st) != cudaSuccess) prof = false;
+      if (!prof) cudaGetLastError();
+    }
     SGT_TRY(launch_gjacobi<1>(st, Z, n, Vt, n, n, n, norms, status, nullptr, &launched, qlog, blog));
+    if (rec.b) {
+      if (prof && launched && cudaEventRecord(rec.b, st) == cudaSuccess) {
+        g_eig_prof.push_back(rec);
+      } else {
+        if (prof && launched) cudaGetLastError();
+        cudaEventDestroy(rec.a);
+        cudaEventDestroy(rec.b);
+      }
+    }
     if (!launched) return jacobi_rows_f32(st, Z, n, n, n, Vt, n, lam, status, ar0);
     const int cs = gj_cluster(n);
     const int bsz = (int)cdiv(n, 2 * cs);
@@ -1655,3 +1690,40 @@ int sym_eig_rows_f32(cudaStream_t st, float* Z, int64_t n, float* Vt, float* lam
 }
 
 }  // namespace sgt
+
+// enable = 1: start recording the cluster eigensolver's launches; 0: stop, wait
+// for the recorded events and return the summed kernel milliseconds, the
+// algorithmic FP32 flops (sweeps x n(n-1)/2 pair visits x 12 n: three dot
+// products and the rotation of two rows of length n per visit) and the number
+// of launches.
+extern "C" SGT_API int sgt_eig_profile(int enable, double* ms, double* flops, long long* launches) {
+  using namespace sgt;
+  if (enable) {
+    g_eig_prof_on = true;
+    return SGT_OK;
+  }
+  g_eig_prof_on = false;
+  std::vector<EigProfRec> recs;
+  recs.swap(g_eig_prof);
+  double tot = 0.0, fl = 0.0;
+  int rc = SGT_OK;
+  for (auto& r : recs) {
+    float t = 0.f;
+    int sw = 0;
+    if (rc == SGT_OK && cudaEventSynchronize(r.b) == cudaSuccess &&
+        cudaEventElapsedTime(&t, r.a, r.b) == cudaSuccess &&
+        (!r.status || cudaMemcpy(&sw, r.status, sizeof(int), cudaMemcpyDeviceToHost) == cudaSuccess)) {
+      tot += t;
+      const double sweeps = sw > 0 ? sw : (sw < 0 ? JAC_MAX_SWEEPS : 0);
+      fl += sweeps * 0.5 * (double)r.n * (double)(r.n - 1) * 12.0 * (double)r.n;
+    } else if (rc == SGT_OK) {
+      rc = SGT_ERR_CUDA;
+    }
+    cudaEventDestroy(r.a);
+    cudaEventDestroy(r.b);
+  }
+  if (ms) *ms = tot;
+  if (flops) *flops = fl;
+  if (launches) *launches = (long long)recs.size();
+  return rc;
+}

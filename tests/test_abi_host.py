@@ -65,6 +65,13 @@ def test_workspace_queries_and_shape_checks(lib):
     assert L.query("sgt_tc_gemm_f32_workspace_size", 256, 4096, 4096) == 3 * 256 * 4096 * 4
     assert L.query("sgt_tc_gemm_f32_workspace_size", 4096, 4096, 4096) == 0
     assert L.query("sgt_tc_gemm_f32_workspace_size", 128, 128, 64) == 0
+    # event profiles: stopping with nothing recorded needs no device
+    import ctypes
+
+    for name in ("sgt_tc_profile", "sgt_eig_profile"):
+        ms, fl, n = ctypes.c_double(1.0), ctypes.c_double(1.0), ctypes.c_longlong(1)
+        assert getattr(lib, name)(0, ctypes.byref(ms), ctypes.byref(fl), ctypes.byref(n)) == 0
+        assert (ms.value, fl.value, n.value) == (0.0, 0.0, 0)
 
 
 def test_svd_round_shapes_match_oracle(lib):
