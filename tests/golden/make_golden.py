@@ -451,6 +451,22 @@ def mul_cases(st: Store):
     st.put("mul", "WV", cores(wv))
     st.put("mul", "WV_tensor", wv.to_tensor())
 
+    # test/test_syn.py:10-26 test_mul: arange operands, both argument orders and MPS . MPS
+    x = np.arange(2 ** 2)
+    w = np.arange(2 ** 4).reshape((4, 4))
+    with quiet():
+        X = MPS(x.reshape((2, 2)), bond_shape=(2,)).decompose()
+        W = MPO(w.reshape((2, 2, 2, 2)), bond_shape=(2,)).decompose()
+        wx = mul(W, X, mode="standard")
+        xw = mul(X, W, mode="standard")
+        xx = mul(X, X, mode="standard")
+    st.put("syn", "X", cores(X))
+    st.put("syn", "W", cores(W))
+    st.put("syn", "WX_tensor", wx.to_tensor())
+    st.put("syn", "XW_tensor", xw.to_tensor())
+    st.put("syn", "XX", float(xx))
+    st.put("syn", "exact_xw", np.matmul(x, w).astype(np.float64))
+
 
 GROUPS = {
     "readme_flow": readme_flow,

@@ -473,3 +473,8 @@ def test_mul(golden):
     assert rel(wv.to_tensor(), g("mul", "WV_tensor")) < TOL
     with pytest.raises(Exception, match="same number of sites"):
         syn.mul(X, mpo(g("mul", "W")[:2]))
+    # test/test_syn.py:10-26: arange operands (exact at this size)
+    X, W = mps(g("syn", "X")), mpo(g("syn", "W"))
+    assert rel(syn.mul(W, X, mode="standard").to_tensor(), g("syn", "WX_tensor")) < TOL
+    assert rel(syn.mul(X, W, mode="standard").to_tensor(), g("syn", "XW_tensor")) < TOL
+    assert abs(float(syn.mul(X, X, mode="standard")) - float(g("syn", "XX"))) <= TOL * 14.0

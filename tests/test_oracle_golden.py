@@ -233,3 +233,12 @@ def test_mul(golden):
     assert rel(O.mpo_to_tensor(wv), g("mul", "WV_tensor")) < TOL
     with pytest.raises(Exception, match="same number of sites"):
         O.mul("mps", X, "mpo", W[:2])
+    # test/test_syn.py:10-26: arange operands, exact at this size
+    X, W = g("syn", "X"), g("syn", "W")
+    _, wx = O.mul("mpo", W, "mps", X)
+    assert rel(O.to_tensor(wx), g("syn", "WX_tensor")) < TOL
+    _, xw = O.mul("mps", X, "mpo", W)
+    assert rel(O.to_tensor(xw), g("syn", "XW_tensor")) < TOL
+    np.testing.assert_allclose(O.to_tensor(xw).reshape(-1), g("syn", "exact_xw"), rtol=1e-12)
+    _, xx = O.mul("mps", X, "mps", X)
+    assert abs(xx - float(g("syn", "XX"))) <= TOL * abs(xx)
