@@ -272,7 +272,9 @@ SGT_API int sgt_tc_profile(int enable, double* ms, double* flops, long long* lau
  * around every launch; enable = 0 stops, waits for the events and returns the
  * summed kernel milliseconds, the algorithmic FP32 flops (sweeps x n(n-1)/2
  * pair visits x 12 n per launch, the sweep count read from the launch's
- * status word) and the number of launches. */
+ * status word) and the number of launches.  Like sgt_tc_profile, a process-wide
+ * switch for single-threaded benchmarks: not for use while other threads launch
+ * work or while a stream is being captured into a graph. */
 SGT_API int sgt_eig_profile(int enable, double* ms, double* flops, long long* launches);
 
 /* Symmetric PSD eigen-decomposition in FP32 (the Gram-form bond solve):
