@@ -133,3 +133,20 @@ def test_batched_plan_host_only():
         assert len(oshape) == n and oshape[0][0] == 1 and oshape[-1][2] == 1
         for k in range(n - 1):
             assert oshape[k][2] == oshape[k + 1][0] and oshape[k][2] <= chi
+
+
+def test_bench_dominant_kernel_object(lib):
+    """The bench line's dominant_kernel object from the eigensolver's event
+    profile: well-formed figures, and an error string instead of a failure."""
+    import bench
+
+    assert bench._eig_profile(True) is True
+    stats = bench._eig_profile(False)
+    assert stats == (0.0, 0.0, 0)
+    assert bench._eig_summary(stats, 600.0) == {"kernel": "gjacobi_kernel<1>", "launches": 0}
+    flops = 14 * 0.5 * 512 * 511 * 12 * 512 * 55
+    d = bench._eig_summary((437.5, flops, 55), 600.0)
+    assert d["launches"] == 55 and abs(d["ms_per_launch"] - 437.5 / 55) < 1e-12
+    assert 0 < d["frac"] < d["frac_of_cluster_sms"] < 1
+    assert abs(d["share_of_step"] - 437.5 / 600.0) < 1e-12
+    assert bench._eig_summary("RuntimeError: x", 600.0)["error"] == "RuntimeError: x"
