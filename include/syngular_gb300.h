@@ -50,8 +50,10 @@ extern "C" {
 /* Arithmetic of the rounding / contraction entry points that take a `precision`. */
 #define SGT_PREC_F64 0     /* plain FP64 everywhere */
 #define SGT_PREC_TF32 1    /* GEMM-shaped work on tcgen05 kind::tf32, FP32 accumulate */
-#define SGT_PREC_BF16 2    /* GEMM-shaped work on tcgen05 kind::f16 with bf16 inputs */
-#define SGT_PREC_BF16X3 3  /* split bf16 (hi*hi + hi*lo + lo*hi) on tcgen05, FP32 accumulate */
+#define SGT_PREC_BF16 2    /* reserved, rejected with SGT_ERR_INVALID (see SGT_PREC_BF16X3) */
+#define SGT_PREC_BF16X3 3  /* reserved, rejected with SGT_ERR_INVALID: a split bf16 product keeps
+                              ~16 mantissa bits (~1.5e-5), short of the ~1e-7 that the Gram form's
+                              squared spectrum needs; the split-tf32 form below keeps ~22 bits */
 #define SGT_PREC_TF32X3 4  /* split tf32 (hi*hi + hi*lo + lo*hi) on tcgen05, FP32 accumulate */
 
 SGT_API int sgt_version(void);
