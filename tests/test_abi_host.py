@@ -65,6 +65,10 @@ def test_workspace_queries_and_shape_checks(lib):
     assert L.query("sgt_tc_gemm_f32_workspace_size", 256, 4096, 4096) == 3 * 256 * 4096 * 4
     assert L.query("sgt_tc_gemm_f32_workspace_size", 4096, 4096, 4096) == 0
     assert L.query("sgt_tc_gemm_f32_workspace_size", 128, 128, 64) == 0
+    # the reserved bf16 precision codes are rejected by the size queries already
+    for prec in (L.PREC_BF16, L.PREC_BF16X3):
+        assert L.query("sgt_svd_round_workspace_size", 3, sh, 2, prec) == 0
+        assert b"precision" in lib.sgt_last_error()
     # event profiles: stopping with nothing recorded needs no device
     import ctypes
 
