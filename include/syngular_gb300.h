@@ -100,8 +100,9 @@ SGT_API size_t sgt_bond_concat_chain_workspace_size(int n);
 /* ----------------------------------------------------------------------
  * Overlap <X|Y> without conjugation -- MatrixProductState.__or__ (mps:116-127).
  * Transfer sweep E_{k+1} = sum_p X_k[:,p,:]^T E_k Y_k[:,p,:] with per-site
- * rescaling.  `result` (device, 2 doubles) receives (mantissa, log_scale):
- * <X|Y> = mantissa * exp(log_scale).
+ * rescaling by exact powers of two.  `result` (device, 2 doubles) receives
+ * (mantissa, exponent) with the exponent an integer held in a double:
+ * <X|Y> = mantissa * 2^exponent, i.e. ldexp(mantissa, (int)exponent) in C.
  * -------------------------------------------------------------------- */
 SGT_API size_t sgt_overlap_workspace_size(int n, const int64_t* xshape, const int64_t* yshape);
 SGT_API int sgt_overlap_sweep(int n, const double* const* X, const int64_t* xshape,
@@ -119,7 +120,7 @@ SGT_API int sgt_overlap_sweep(int n, const double* const* X, const int64_t* xsha
  * up that array's device address (make it before any stream capture).  All
  * calls share the array: calls that overlap on the GPU (other streams or host
  * threads) race and must be serialised by the caller.  Result as for
- * sgt_overlap_sweep. */
+ * sgt_overlap_sweep: (mantissa, exponent), <X|Y> = ldexp(mantissa, exponent). */
 SGT_API int sgt_overlap_sweep_noalloc(int n, const double* const* X, const int64_t* xshape,
                                       const double* const* Y, const int64_t* yshape,
                                       double* result, void* stream);

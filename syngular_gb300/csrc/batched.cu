@@ -13,6 +13,7 @@
 // released by sgt_batched_plan_destroy.
 #include <algorithm>
 #include <mutex>
+#include <string>
 #include <vector>
 
 #include "common.cuh"
@@ -167,22 +168,36 @@ SGT_API int sgt_batched_launch(sgt_batched_plan_s* plan, const double* const* co
   SGT_TRY(create_streams(plan));
   cudaStream_t caller = as_stream(stream);
   SGT_CUDA(cudaEventRecord(plan->fork, caller));
+  // A failure part-way still joins every lane forked so far back into the
+  // caller's stream (an unjoined lane would invalidate a stream capture and
+  // hide the real error); the first error code is returned, with its message.
+  int first = SGT_OK;
+  std::string msg;
   for (size_t l = 0; l < plan->lanes.size(); ++l) {
     cudaStream_t s = plan->streams[l];
-    SGT_CUDA(cudaStreamWaitEvent(s, plan->fork, 0));
+    if (cudaStreamWaitEvent(s, plan->fork, 0) != cudaSuccess) {
+      if (first == SGT_OK) first = SGT_ERR_CUDA, msg = "batched_launch: cudaStreamWaitEvent failed";
+      break;
+    }
     char* base = static_cast<char*>(ws) + plan->lane_off[l];
     for (int i : plan->lanes[l]) {
+      if (first != SGT_OK) break;
       const auto& in = plan->inst[i];
-      SGT_TRY(sgt_mpo_mps_round(in.n, W[i], in.wshape.data(), X[i], in.xshape.data(), in.chi, plan->precision,
-                                out[i], spectra ? spectra[i] : nullptr, discarded ? discarded[i] : nullptr,
-                                status ? status[i] : nullptr, base, plan->lane_bytes[l], s));
-      SGT_TRY(sgt_overlap_sweep(in.n, X[i], in.xshape.data(), out[i], in.oshape.data(), overlap[i], base,
-                                plan->lane_bytes[l], s));
+      int rc = sgt_mpo_mps_round(in.n, W[i], in.wshape.data(), X[i], in.xshape.data(), in.chi, plan->precision,
+                                 out[i], spectra ? spectra[i] : nullptr, discarded ? discarded[i] : nullptr,
+                                 status ? status[i] : nullptr, base, plan->lane_bytes[l], s);
+      if (rc == SGT_OK)
+        rc = sgt_overlap_sweep(in.n, X[i], in.xshape.data(), out[i], in.oshape.data(), overlap[i], base,
+                               plan->lane_bytes[l], s);
+      if (rc != SGT_OK) first = rc, msg = get_error();
     }
-    SGT_CUDA(cudaEventRecord(plan->done[l], s));
-    SGT_CUDA(cudaStreamWaitEvent(caller, plan->done[l], 0));
+    const bool joined = cudaEventRecord(plan->done[l], s) == cudaSuccess &&
+                        cudaStreamWaitEvent(caller, plan->done[l], 0) == cudaSuccess;
+    if (!joined && first == SGT_OK) first = SGT_ERR_CUDA, msg = "batched_launch: joining a lane failed";
+    if (first != SGT_OK) break;
   }
-  return SGT_OK;
+  if (first != SGT_OK) set_error("%s", msg.c_str());
+  return first;
 }
 
 SGT_API void sgt_batched_plan_destroy(sgt_batched_plan_s* plan) {

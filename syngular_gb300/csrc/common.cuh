@@ -30,6 +30,12 @@ const char* get_error();
 // (sgt_launch_count), which benchmarks read around their timed region.
 void note_launch();
 
+// cudaFuncSetAttribute acts on the current device only.  Raise `attr` of
+// `func` to at least `value` on the current device, remembering per device
+// what was already set, so that a process using several GPUs opts every one
+// of them in.  Returns the CUDA status of the set (cudaSuccess when cached).
+cudaError_t func_attr_at_least(const void* func, cudaFuncAttribute attr, int value);
+
 #define SGT_LAUNCHED()                                                                     \
   do {                                                                                     \
     ::sgt::note_launch();                                                                  \

@@ -348,20 +348,12 @@ int sym_eig_f32(cudaStream_t st, const float* Z, int64_t ldz, int64_t n, float* 
   float* lraw = ar.take<float>((size_t)n);
   int* perm = ar.take<int>((size_t)n);
   SGT_REQUIRE(ar.ok(), SGT_ERR_WORKSPACE, "sym_eig: workspace too small");
-  static bool attr = false;
-  static size_t smem_set = 0;
-  if (!attr) {
-    SGT_CUDA(cudaFuncSetAttribute(sjacobi_kernel, cudaFuncAttributeNonPortableClusterSizeAllowed, 1));
-    attr = true;
-  }
-  if (smem > smem_set) {
-    // dynamic + static shared memory must stay within the per-block opt-in limit
-    if (cudaFuncSetAttribute(sjacobi_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) !=
-        cudaSuccess) {
-      cudaGetLastError();
-      return SGT_OK;  // does not fit here: the caller uses the one-sided kernel
-    }
-    smem_set = smem;
+  SGT_CUDA(func_attr_at_least((const void*)sjacobi_kernel, cudaFuncAttributeNonPortableClusterSizeAllowed, 1));
+  // dynamic + static shared memory must stay within the per-block opt-in limit
+  if (func_attr_at_least((const void*)sjacobi_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) !=
+      cudaSuccess) {
+    cudaGetLastError();
+    return SGT_OK;  // does not fit here: the caller uses the one-sided kernel
   }
   cudaLaunchConfig_t cfg = {};
   cfg.gridDim = dim3(cs, 1, 1);

@@ -298,7 +298,7 @@ int gram_step_structured(cudaStream_t st, int passes, const float* Gh, const flo
     dim3 gt((unsigned)cdiv(chi, GT_TA), (unsigned)cdiv(chi2, GT_TC));
     auto run = [&](auto kern, size_t smem) -> int {
       if (smem > 200 * 1024) return SGT_OK;  // the generic kernel below takes it
-      SGT_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+      SGT_CUDA(func_attr_at_least((const void*)kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
       kern<<<gt, GT_THREADS, smem, st>>>(T1, W, T3h, T3l, (int)chi, (int)chi2);
       SGT_LAUNCHED();
       done = true;
@@ -319,11 +319,7 @@ int gram_step_structured(cudaStream_t st, int passes, const float* Gh, const flo
   int TC = 8;
   while (TC > 1 && mid_smem_bytes((int)D, (int)d, (int)dout, (int)D2, TC) > 160 * 1024) TC /= 2;
   const size_t smem = mid_smem_bytes((int)D, (int)d, (int)dout, (int)D2, TC);
-  static size_t smem_set = 0;
-  if (smem > smem_set) {
-    SGT_CUDA(cudaFuncSetAttribute(gram_mid_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    smem_set = smem;
-  }
+  SGT_CUDA(func_attr_at_least((const void*)gram_mid_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
   dim3 g((unsigned)cdiv(chi, GM_TA), (unsigned)cdiv(chi2, TC));
   gram_mid_kernel<<<g, 256, smem, st>>>(T1, W, T3h, T3l, (int)chi, (int)D, (int)d, (int)dout, (int)D2, (int)chi2,
                                         TC);

@@ -1388,13 +1388,9 @@ static int launch_gjacobi(cudaStream_t st, float* G, int64_t ldg, float* Vt, int
   if (MODE == 1 && rlen % 8 == 0) rlen += 4;  // the kernel's row padding
   const int64_t slot_bytes = bsz * rlen * (int64_t)sizeof(float);
   if (bsz > GJ_W / 2 || slot_bytes > BJ_MAX_SLOT_BYTES || slot_bytes % 16 != 0) return SGT_OK;
-  static bool attr_done = false;
   auto kern = gjacobi_kernel<MODE>;
-  if (!attr_done) {
-    SGT_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeNonPortableClusterSizeAllowed, 1));
-    SGT_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, 3 * GJ_SLOT_CAP));
-    attr_done = true;
-  }
+  SGT_CUDA(func_attr_at_least((const void*)kern, cudaFuncAttributeNonPortableClusterSizeAllowed, 1));
+  SGT_CUDA(func_attr_at_least((const void*)kern, cudaFuncAttributeMaxDynamicSharedMemorySize, 3 * GJ_SLOT_CAP));
   const int64_t gram_bytes = ((bsz * bsz + 3) & ~int64_t(3)) * (int64_t)sizeof(float);
   const int64_t dyn = (MODE == 1 ? 4 : 3) * (slot_bytes + gram_bytes);
   if (dyn > 3 * GJ_SLOT_CAP) return SGT_OK;
@@ -1470,14 +1466,10 @@ int jacobi_rows_t(cudaStream_t st, T* G, int64_t ldg, int64_t n, int64_t m, T* V
       const int64_t bsz = cdiv(n, 2 * csb);
       const int64_t slot_bytes = bsz * (m + (vt_smem ? n : 0)) * (int64_t)sizeof(T);
       if (slot_bytes > BJ_MAX_SLOT_BYTES || slot_bytes % 16 != 0) continue;
-      static bool attr_done[2] = {false, false};
       auto kern = bjacobi_kernel<T>;
-      if (!attr_done[sizeof(T) == 8]) {
-        SGT_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeNonPortableClusterSizeAllowed, 1));
-        SGT_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                      3 * BJ_MAX_SLOT_BYTES));
-        attr_done[sizeof(T) == 8] = true;
-      }
+      SGT_CUDA(func_attr_at_least((const void*)kern, cudaFuncAttributeNonPortableClusterSizeAllowed, 1));
+      SGT_CUDA(func_attr_at_least((const void*)kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                  3 * BJ_MAX_SLOT_BYTES));
       const double tolb = jacobi_tol<T>(m);
       cudaLaunchConfig_t cfg = {};
       cfg.gridDim = dim3(csb, 1, 1);
@@ -1512,12 +1504,8 @@ int jacobi_rows_t(cudaStream_t st, T* G, int64_t ldg, int64_t n, int64_t m, T* V
   else if (pairs >= 8 * JAC_WARPS) cs = 8;
   else if (pairs >= 4 * JAC_WARPS) cs = 4;
   else if (pairs >= 2 * JAC_WARPS) cs = 2;
-  static bool nonportable = false;
-  if (!nonportable) {
-    SGT_CUDA(cudaFuncSetAttribute(jacobi_kernel<double>, cudaFuncAttributeNonPortableClusterSizeAllowed, 1));
-    SGT_CUDA(cudaFuncSetAttribute(jacobi_kernel<float>, cudaFuncAttributeNonPortableClusterSizeAllowed, 1));
-    nonportable = true;
-  }
+  SGT_CUDA(func_attr_at_least((const void*)jacobi_kernel<double>, cudaFuncAttributeNonPortableClusterSizeAllowed, 1));
+  SGT_CUDA(func_attr_at_least((const void*)jacobi_kernel<float>, cudaFuncAttributeNonPortableClusterSizeAllowed, 1));
   const double tol = jacobi_tol<T>(m);
   cudaLaunchConfig_t cfg = {};
   cfg.gridDim = dim3(cs, 1, 1);
@@ -1656,14 +1644,12 @@ int sym_eig_rows_f32(cudaStream_t st, float* Z, int64_t n, float* Vt, float* lam
     // 8-column slices unless that leaves most SMs idle
     const int cols = cdiv(n, 8) >= 128 ? 8 : 4;
     const size_t smem = sizeof(float) * ((size_t)2 * cs * bsz * cols + (size_t)2 * cs * GJ_W * RP_QS);
-    static bool rp_attr = false;
-    if (!rp_attr) {
+    {
       const size_t qb = sizeof(float) * (size_t)2 * 16 * GJ_W * RP_QS;
-      SGT_CUDA(cudaFuncSetAttribute(gj_replay_kernel<8>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                    (int)(sizeof(float) * (size_t)2 * 16 * (GJ_W / 2) * 8 + qb)));
-      SGT_CUDA(cudaFuncSetAttribute(gj_replay_kernel<4>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                    (int)(sizeof(float) * (size_t)2 * 16 * (GJ_W / 2) * 4 + qb)));
-      rp_attr = true;
+      SGT_CUDA(func_attr_at_least((const void*)gj_replay_kernel<8>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                  (int)(sizeof(float) * (size_t)2 * 16 * (GJ_W / 2) * 8 + qb)));
+      SGT_CUDA(func_attr_at_least((const void*)gj_replay_kernel<4>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                  (int)(sizeof(float) * (size_t)2 * 16 * (GJ_W / 2) * 4 + qb)));
     }
     if (cols == 8)
       gj_replay_kernel<8><<<(unsigned)cdiv(n, 8), RP_THREADS, smem, st>>>(qlog, blog, status, (int)n, cs, bsz, Vt, n);

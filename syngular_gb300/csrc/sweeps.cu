@@ -9,6 +9,9 @@
 #include <stdarg.h>
 
 #include <algorithm>
+#include <map>
+#include <mutex>
+#include <tuple>
 #include <vector>
 
 #include "common.cuh"
@@ -56,6 +59,21 @@ void set_error(const char* fmt, ...) {
   va_end(ap);
 }
 const char* get_error() { return g_err; }
+
+cudaError_t func_attr_at_least(const void* func, cudaFuncAttribute attr, int value) {
+  static std::mutex mu;
+  static std::map<std::tuple<const void*, int, int>, int> done;
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return e;
+  std::lock_guard<std::mutex> lock(mu);
+  const auto key = std::make_tuple(func, (int)attr, dev);
+  auto it = done.find(key);
+  if (it != done.end() && it->second >= value) return cudaSuccess;
+  e = cudaFuncSetAttribute(func, attr, value);
+  if (e == cudaSuccess) done[key] = value;
+  return e;
+}
 
 namespace {
 

@@ -425,12 +425,8 @@ int tc_gemm_tf32(cudaStream_t st, int passes, int64_t M, int64_t N, int64_t K, f
     mbl = mb;
   }
   const size_t smem = tc_smem_bytes(passes);
-  static bool attr_set = false;
-  if (!attr_set) {
-    SGT_CUDA(cudaFuncSetAttribute(tc_gemm_tf32_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                  (int)tc_smem_bytes(3)));
-    attr_set = true;
-  }
+  SGT_CUDA(func_attr_at_least((const void*)tc_gemm_tf32_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                              (int)tc_smem_bytes(3)));
   const int S = part ? tc_splits(M, N, K, part_floats) : 1;
   const int KTall = (int)cdiv(K, TC_BK);
   const int kps = (int)cdiv(KTall, S);

@@ -18,6 +18,7 @@ has its own workspace and stream, and the kernels read only its own data.
 """
 from __future__ import annotations
 
+import ctypes
 import queue
 import threading
 import time
@@ -102,7 +103,16 @@ class RoundServer:
             wsh, _a = L.i64_array([int(v) for w in W for v in w.shape])
             xsh, _b = L.shape_array([tuple(x.shape) for x in X])
             ws = L.query("sgt_mpo_mps_round_workspace_size", n, wsh, xsh, job.chi, job.precision)
-            out = sum(x.shape[1] * job.chi * job.chi * 8 for x in X)
+            # outputs as the library sizes them: the rounded cores carry the
+            # operator's out leg; plus the spectra, discarded weights and status
+            psh, _p = L.shape_array([(X[k].shape[0] * W[k].shape[0], W[k].shape[2], X[k].shape[2] * W[k].shape[3])
+                                     for k in range(n)])
+            out_arr = (ctypes.c_int64 * (3 * n))()
+            cnt_arr = (ctypes.c_int64 * max(1, n - 1))()
+            L.call("sgt_svd_round_shapes", n, psh, job.chi, ctypes.cast(out_arr, L._PI64),
+                   ctypes.cast(cnt_arr, L._PI64))
+            out = 8 * sum(out_arr[3 * k] * out_arr[3 * k + 1] * out_arr[3 * k + 2] for k in range(n))
+            out += 8 * (sum(cnt_arr[k] for k in range(n - 1)) + max(1, n - 1)) + 4
             return ws + out if ws else -1
         if job.kind == "add_round":
             X, Y = s["mps"], self.sessions[job.other]["mps"]
@@ -142,7 +152,14 @@ class RoundServer:
             try:
                 while True:
                     j = self.inbox.get_nowait()
-                    need = self.footprint(j)
+                    try:
+                        need = self.footprint(j)
+                    except Exception as e:  # unknown session, shape the size query rejects, ...
+                        j.error = "rejected: %s: %s" % (type(e).__name__, e)
+                        j.end = time.perf_counter()
+                        self.rejected.append(j)
+                        j.done.set()
+                        continue
                     if need < 0 or need > self.budget:
                         j.error = "rejected: footprint %d bytes exceeds the HBM budget" % need
                         j.end = time.perf_counter()

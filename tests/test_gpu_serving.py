@@ -98,3 +98,20 @@ def test_budget_admission_and_rejection():
     assert ok.error is None and big.error is not None and "budget" in big.error
     st = latency_stats([ok])
     assert st["count"] == 1 and st["p50_ms"] >= 0
+
+
+def test_bad_job_does_not_stop_the_loop():
+    """A job naming an unknown session is rejected on its own; the scheduler
+    thread keeps serving the jobs that follow it."""
+    from syngular_gb300.serving import Job
+
+    rng = np.random.default_rng(11)
+    srv = server_with_sessions(rng, 2, slots=2).start()
+    bad = Job(kind="round", session="no-such-session", chi=4, precision=0)
+    good = Job(kind="overlap", session="s0", other="s1")
+    srv.submit(bad)
+    srv.submit(good)
+    assert bad.done.wait(60) and good.done.wait(60)
+    srv.stop()
+    assert bad.error is not None and "KeyError" in bad.error
+    assert good.error is None and good.result is not None
