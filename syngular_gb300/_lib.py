@@ -29,6 +29,7 @@ PREC_TF32 = 1
 PREC_BF16 = 2
 PREC_BF16X3 = 3
 PREC_TF32X3 = 4
+PREC_BF16X5 = 5
 
 _c_i64 = ctypes.c_int64
 _c_vp = ctypes.c_void_p
@@ -71,6 +72,9 @@ SIGNATURES = {
     "sgt_tc_gemm_f32_workspace_size": (_c_size, [_c_i64, _c_i64, _c_i64]),
     "sgt_tc_gemm_f32_ws": (_c_int, [_c_int, _c_i64, _c_i64, _c_i64, ctypes.c_float, _c_vp, _c_vp, _c_i64, _c_vp, _c_vp, _c_i64, ctypes.c_float, _c_vp, _c_i64, _c_vp, _c_vp, _c_size, _c_vp]),
     "sgt_split_tf32": (_c_int, [_c_vp, _c_vp, _c_vp, _c_i64, _c_vp]),
+    "sgt_gemm_f64_sliced_workspace_size": (_c_size, [_c_i64, _c_i64, _c_i64]),
+    "sgt_gemm_f64_sliced": (_c_int, [_c_i64, _c_i64, _c_i64, _c_dbl, _c_vp, _c_i64, _c_vp, _c_i64, _c_dbl, _c_vp, _c_i64, _c_vp, _c_size, _c_vp]),
+    "sgt_sliced_profile": (_c_int, [_c_int, ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_longlong)]),
     "sgt_launch_count": (ctypes.c_ulonglong, []),
     "sgt_sym_eig_f32_workspace_size": (_c_size, [_c_i64]),
     "sgt_sym_eig_f32": (_c_int, [_c_vp, _c_i64, _c_vp, _c_vp, _c_vp, _c_int, _c_vp, _c_size, _c_vp]),

@@ -1,0 +1,839 @@
+// The accurate mixed-precision form of the metric operation
+// (sgt_mpo_mps_round / sgt_svd_round with SGT_PREC_BF16X5).
+//
+// Same algebra as the Gram form of mixed.cu (no Householder QR on the R x R
+// product unfoldings):
+//   G_0 = [1],  G_{k+1} = sum_o P_k[:,o,:]^T G_k P_k[:,o,:]      (left Gram, structured)
+//   right to left, F_N = [1]:
+//     Y_k = P_k F_{k+1},  Z_k = Y_k^T G_k Y_k = V diag(s^2) V^T,
+//     core_k = V[:, :chi]^T,  F_k = Y_k V[:, :chi],  core_0 = P_0 F_1,
+// but carried at FP64-class accuracy:
+//   * every O(R^3) product is the sliced bf16 GEMM of oz_gemm.cu (tcgen05,
+//     ~2^-35 of the operands' scale) instead of split TF32 (~2^-22);
+//   * the two small W contractions of the Gram step, the elementwise steps and
+//     the intermediate matrices are FP32 pairs ("double-float", ~48 bits):
+//     GB300's FP64 pipe is too slow for them;
+//   * the bond eigensolve keeps the FP32 cluster Jacobi (svd.cu) as its first
+//     approximation and then refines the eigenvectors and eigenvalues against
+//     the pair-accurate Z by two steps of Ogita & Aishima's iteration
+//     ("Iterative refinement for symmetric eigenvalue decomposition", Japan J.
+//     Indust. Appl. Math. 35, 2018): with X the approximate eigenvectors,
+//       R = I - X^T X,  S = X^T Z X,  l_i = S_ii / (1 - R_ii),
+//       E_ij = (S_ij + l_j R_ij) / (l_j - l_i)  (E_ii = R_ii / 2),
+//       X <- X + X E,
+//     all four products on the sliced GEMM.  Each step squares the error, so
+//     two steps take the FP32 Jacobi's ~1e-6 to the GEMMs' own accuracy.
+//     Pairs whose correction would not be small (near-equal eigenvalues)
+//     keep E_ij = R_ij / 2, as in the published method's cluster case.
+// Product cores are never stored whole: the right sweep slices P_k site by
+// site straight from X_k and W_k.
+#include <float.h>
+
+#include <algorithm>
+#include <vector>
+
+#include "common.cuh"
+#include "oz.cuh"
+
+namespace sgt {
+
+void svd_round_plan_public(int n, const int64_t* shape, int64_t chi, std::vector<int64_t>& b,
+                           std::vector<int64_t>& x, std::vector<int64_t>& cnt);
+size_t sym_eig_rows_ws_bytes(int64_t n);
+int sym_eig_rows_f32(cudaStream_t st, float* Z, int64_t n, float* Vt, float* lam, int* status, Arena& ar,
+                     int method);
+
+namespace {
+
+inline unsigned grid_for(int64_t n, int per = 256) {
+  return (unsigned)std::max<int64_t>(1, std::min<int64_t>(cdiv(n, per), 152 * 16));
+}
+
+// FP64 -> pair
+__global__ void f64_to_pair_kernel(const double* __restrict__ x, float* __restrict__ h, float* __restrict__ l,
+                                   int64_t n) {
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    const double v = x[i];
+    const float a = (float)v;
+    h[i] = a;
+    l[i] = (float)(v - (double)a);
+  }
+}
+
+// dst (rows x cols FP64, ldd) = pair src (lds)
+__global__ void pair_to_f64_kernel(const float* __restrict__ h, const float* __restrict__ l, int64_t lds,
+                                   double* __restrict__ dst, int64_t ldd, int64_t rows, int64_t cols) {
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < rows * cols;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t r = i / cols, c = i % cols;
+    dst[r * ldd + c] = (double)h[r * lds + c] + (double)l[r * lds + c];
+  }
+}
+
+// Pair transpose, batched: for every batch b, dst[b] (cols x rows, ldd) =
+// src[b]^T (rows x cols, lds); batch strides sb / db.
+__global__ void pair_transpose_kernel(float* __restrict__ dh, float* __restrict__ dl, int64_t ldd, int64_t db,
+                                      const float* __restrict__ sh, const float* __restrict__ sl, int64_t lds,
+                                      int64_t sb, int64_t rows, int64_t cols) {
+  __shared__ float th[32][33], tl[32][33];
+  const int64_t b = blockIdx.z;
+  sh += b * sb;
+  sl += b * sb;
+  dh += b * db;
+  dl += b * db;
+  const int64_t tiles_c = (cols + 31) / 32, tiles_r = (rows + 31) / 32;
+  for (int64_t t = blockIdx.x; t < tiles_r * tiles_c; t += gridDim.x) {
+    const int64_t r0 = (t / tiles_c) * 32, c0 = (t % tiles_c) * 32;
+    for (int i = threadIdx.y; i < 32; i += blockDim.y) {
+      const int64_t r = r0 + i, c = c0 + threadIdx.x;
+      const bool in = r < rows && c < cols;
+      th[i][threadIdx.x] = in ? sh[r * lds + c] : 0.f;
+      tl[i][threadIdx.x] = in ? sl[r * lds + c] : 0.f;
+    }
+    __syncthreads();
+    for (int i = threadIdx.y; i < 32; i += blockDim.y) {
+      const int64_t c = c0 + i, r = r0 + threadIdx.x;
+      if (c < cols && r < rows) {
+        dh[c * ldd + r] = th[threadIdx.x][i];
+        dl[c * ldd + r] = tl[threadIdx.x][i];
+      }
+    }
+    __syncthreads();
+  }
+}
+
+// P[(a,b,o)][(a2,b2)] = sum_i X[a,i,a2] W[b,i,o,b2] in pair arithmetic from the
+// pairs of X and W (error-free products, two-sum accumulation).
+__device__ __forceinline__ void product_elem(const float* __restrict__ Xh, const float* __restrict__ Xl,
+                                             const float* __restrict__ Wh, const float* __restrict__ Wl, int a, int b,
+                                             int o, int a2, int b2, int I, int O, int A2, int B2, int Bd, float& h,
+                                             float& l) {
+  h = 0.f;
+  l = 0.f;
+  for (int i = 0; i < I; ++i) {
+    const int64_t xi = ((int64_t)a * I + i) * A2 + a2;
+    const int64_t wi = (((int64_t)b * I + i) * O + o) * B2 + b2;
+    df_fma(h, l, Xh[xi], Xl[xi], Wh[wi], Wl[wi]);
+  }
+  (void)Bd;
+  df_norm(h, l);
+}
+
+// One block per row (a, b, o) of the product core: pass 1 finds the row's
+// exponent, pass 2 recomputes the row and writes its slices (padding zeroed).
+__global__ void product_slices_kernel(const float* __restrict__ Xh, const float* __restrict__ Xl,
+                                      const float* __restrict__ Wh, const float* __restrict__ Wl, int Bd, int I, int O,
+                                      int A2, int B2, __nv_bfloat16* __restrict__ out, int64_t ldo, int64_t sstride,
+                                      int* __restrict__ ex) {
+  __shared__ float red[32];
+  __shared__ int s_e;
+  const int r = blockIdx.x;
+  const int o = r % O, ab = r / O, b = ab % Bd, a = ab / Bd;
+  const int ncol = A2 * B2;
+  float mx = 0.f;
+  for (int c = threadIdx.x; c < ncol; c += blockDim.x) {
+    float h, l;
+    product_elem(Xh, Xl, Wh, Wl, a, b, o, c / B2, c % B2, I, O, A2, B2, Bd, h, l);
+    mx = fmaxf(mx, fabsf(h));
+  }
+  for (int s = 16; s > 0; s >>= 1) mx = fmaxf(mx, __shfl_xor_sync(0xffffffffu, mx, s));
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = mx;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    float m = 0.f;
+    for (int w = 0; w < (int)(blockDim.x >> 5); ++w) m = fmaxf(m, red[w]);
+    int e = 0;
+    if (m > 0.f && isfinite(m)) frexpf(m, &e);
+    s_e = e;
+    ex[r] = e;
+  }
+  __syncthreads();
+  const int e = s_e;
+  for (int c = threadIdx.x; c < ncol; c += blockDim.x) {
+    float h, l;
+    product_elem(Xh, Xl, Wh, Wl, a, b, o, c / B2, c % B2, I, O, A2, B2, Bd, h, l);
+    slice_store(ldexpf(h, 6 - e), ldexpf(l, 6 - e), out, sstride, (int64_t)r * ldo + c);
+  }
+  for (int64_t c = ncol + threadIdx.x; c < ldo; c += blockDim.x) slice_zero(out, sstride, (int64_t)r * ldo + c);
+}
+
+// Steps B and C of the structured Gram step (see gram.cu) in pair arithmetic,
+// for a tile of MD_TA values of a and TC values of c'.
+//   B: U [a][b][o][e'][c'] = sum_{e,j} T1[a][b][e][j][c'] W[e][j][o][e']
+//   C: T3[c'][e'][b'][a][i] = sum_{b,o} W[b][i][o][b'] U[a][b][o][e'][c']
+// T1 / T3 are pair matrices (hi, lo); W is FP64 [b][i][o][b'].
+constexpr int MD_TA = 4;
+
+size_t mid_df_smem(int D, int d, int dout, int D2, int TC) {
+  return sizeof(float) * 2 *
+         ((size_t)D * d * dout * D2 + (size_t)MD_TA * D * D * d * TC + (size_t)MD_TA * D * dout * D2 * TC);
+}
+
+__global__ void __launch_bounds__(256) gram_mid_df_kernel(const float* __restrict__ T1h, const float* __restrict__ T1l,
+                                                          const double* __restrict__ W, float* __restrict__ T3h,
+                                                          float* __restrict__ T3l, int chi, int D, int d, int dout,
+                                                          int D2, int chi2, int TC) {
+  extern __shared__ float md_smem[];
+  const int a0 = blockIdx.x * MD_TA, c0 = blockIdx.y * TC;
+  const int bej = D * D * d;
+  const int boe = D * dout * D2;
+  const int wn = D * d * dout * D2;
+  float2* sW = reinterpret_cast<float2*>(md_smem);  // [D][d][dout][D2]
+  float2* sT = sW + wn;                              // [TA][bej][TC]
+  float2* sU = sT + MD_TA * bej * TC;                // [TA][b][o][e'][TC]
+  const int tid = threadIdx.x;
+  for (int i = tid; i < wn; i += 256) {
+    const double v = W[i];
+    const float h = (float)v;
+    sW[i] = make_float2(h, (float)(v - (double)h));
+  }
+  for (int i = tid; i < MD_TA * bej * TC; i += 256) {
+    const int t = i % TC, r = (i / TC) % bej, at = i / (TC * bej);
+    const int a = a0 + at, c = c0 + t;
+    float2 v = make_float2(0.f, 0.f);
+    if (a < chi && c < chi2) {
+      const int64_t g = ((int64_t)a * bej + r) * chi2 + c;
+      v = make_float2(T1h[g], T1l[g]);
+    }
+    sT[i] = v;
+  }
+  __syncthreads();
+  for (int i = tid; i < MD_TA * boe * TC; i += 256) {
+    const int t = i % TC;
+    int r = i / TC;
+    const int e2 = r % D2;
+    r /= D2;
+    const int o = r % dout;
+    r /= dout;
+    const int b = r % D, at = r / D;
+    const float2* tcol = sT + ((int64_t)at * bej + (int64_t)b * D * d) * TC + t;
+    float h = 0.f, l = 0.f;
+    for (int e = 0; e < D; ++e)
+      for (int j = 0; j < d; ++j) {
+        const float2 x = tcol[(e * d + j) * TC];
+        const float2 w = sW[((e * d + j) * dout + o) * D2 + e2];
+        df_fma(h, l, x.x, x.y, w.x, w.y);
+      }
+    df_norm(h, l);
+    sU[i] = make_float2(h, l);
+  }
+  __syncthreads();
+  const int inner = MD_TA * d;
+  const int total = inner * D2 * D2 * TC;
+  for (int k = tid; k < total; k += 256) {
+    const int ai = k % inner;
+    int r = k / inner;
+    const int b2 = r % D2;
+    r /= D2;
+    const int e2 = r % D2;
+    const int t = r / D2;
+    const int at = ai / d, i = ai % d;
+    const int a = a0 + at, c = c0 + t;
+    if (a >= chi || c >= chi2) continue;
+    float h = 0.f, l = 0.f;
+    for (int b = 0; b < D; ++b)
+      for (int o = 0; o < dout; ++o) {
+        const float2 w = sW[((b * d + i) * dout + o) * D2 + b2];
+        const float2 u = sU[((((int64_t)at * D + b) * dout + o) * D2 + e2) * TC + t];
+        df_fma(h, l, w.x, w.y, u.x, u.y);
+      }
+    df_norm(h, l);
+    const int64_t idx = (((int64_t)c * D2 + e2) * D2 + b2) * ((int64_t)chi * d) + (int64_t)a * d + i;
+    T3h[idx] = h;
+    T3l[idx] = l;
+  }
+}
+
+// max |h| over n values as the bit pattern of a non-negative float
+__global__ void pair_absmax_kernel(const float* __restrict__ h, int64_t n, unsigned* __restrict__ out) {
+  float m = 0.f;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+    m = fmaxf(m, fabsf(h[i]));
+  for (int o = 16; o > 0; o >>= 1) m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, o));
+  if ((threadIdx.x & 31) == 0 && m > 0.f) atomicMax(out, __float_as_uint(m));
+}
+
+// (h, l) *= 2^-e (exact), e = binary exponent of the max; gexp_next = gexp_prev + e
+__global__ void pair_scale_kernel(float* __restrict__ h, float* __restrict__ l, int64_t n,
+                                  const unsigned* __restrict__ maxbits, const int* __restrict__ gexp_prev,
+                                  int* __restrict__ gexp_next) {
+  const float m = __uint_as_float(*maxbits);
+  int e = 0;
+  if (m > 0.f && isfinite(m)) frexpf(m, &e);
+  if (blockIdx.x == 0 && threadIdx.x == 0) *gexp_next = *gexp_prev + e;
+  if (e == 0) return;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    h[i] = ldexpf(h[i], -e);
+    l[i] = ldexpf(l[i], -e);
+  }
+}
+
+__global__ void pair_one_kernel(float* h, float* l) {
+  h[0] = 1.f;
+  l[0] = 0.f;
+}
+
+// Z <- (Z + Z^T) / 2 in pair arithmetic
+__global__ void pair_symmetrize_kernel(float* __restrict__ h, float* __restrict__ l, int64_t n) {
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n * n; i += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t r = i / n, c = i % n;
+    if (c <= r) continue;
+    float sh = h[r * n + c], sl = l[r * n + c];
+    df_add(sh, sl, h[c * n + r], l[c * n + r]);
+    sh *= 0.5f;
+    sl *= 0.5f;
+    h[r * n + c] = sh;
+    l[r * n + c] = sl;
+    h[c * n + r] = sh;
+    l[c * n + r] = sl;
+  }
+}
+
+// pair (a / b) for b != 0 (one Newton correction of the FP32 quotient)
+__device__ __forceinline__ void df_div(float ah, float al, float bh, float bl, float& qh, float& ql) {
+  const float q = ah / bh;
+  // r = a - q b in pair arithmetic
+  const float p = q * bh;
+  const float pe = fmaf(q, bh, -p);
+  float r = (ah - p) - pe;
+  r += al - q * bl;
+  const float q2 = r / bh;
+  qh = q + q2;
+  ql = q2 - (qh - q);
+}
+
+// Refinement step, part 1: l_i = S_ii / VV_ii (= S_ii / (1 - R_ii)), pairs.
+__global__ void oa_lambda_kernel(const float* __restrict__ Sh, const float* __restrict__ Sl,
+                                 const float* __restrict__ Vh, const float* __restrict__ Vl, int n,
+                                 float* __restrict__ lh, float* __restrict__ ll) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    const int64_t d = (int64_t)i * n + i;
+    float qh, ql;
+    df_div(Sh[d], Sl[d], Vh[d], Vl[d], qh, ql);
+    lh[i] = qh;
+    ll[i] = ql;
+  }
+}
+
+// Refinement step, part 2: Et[i][j] = E[j][i], with
+//   E_jj = R_jj / 2,  E_ji = (S_ji + l_i R_ji) / (l_i - l_j)  where that is below 1/8,
+//   else R_ji / 2;    R = I - VV.
+__global__ void oa_correction_kernel(const float* __restrict__ Sh, const float* __restrict__ Sl,
+                                     const float* __restrict__ Vh, const float* __restrict__ Vl,
+                                     const float* __restrict__ lh, const float* __restrict__ ll, int n,
+                                     float* __restrict__ Eh, float* __restrict__ El) {
+  for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < (int64_t)n * n;
+       t += (int64_t)gridDim.x * blockDim.x) {
+    const int i = (int)(t / n), j = (int)(t % n);  // output Et[i][j] = E[j][i]
+    const int64_t ji = (int64_t)j * n + i;
+    // R_ji = delta_ji - VV_ji
+    float rh = -Vh[ji], rl = -Vl[ji];
+    if (i == j) df_add(rh, rl, 1.f, 0.f);
+    float eh, el;
+    if (i == j) {
+      eh = 0.5f * rh;
+      el = 0.5f * rl;
+    } else {
+      // numerator S_ji + l_i R_ji
+      float nh = Sh[ji], nl = Sl[ji];
+      df_fma(nh, nl, lh[i], ll[i], rh, rl);
+      df_norm(nh, nl);
+      // denominator l_i - l_j
+      float dh = lh[i], dl = ll[i];
+      df_add(dh, dl, -lh[j], -ll[j]);
+      if (fabsf(dh) > 8.f * fabsf(nh) && dh != 0.f) {
+        df_div(nh, nl, dh, dl, eh, el);
+      } else {
+        eh = 0.5f * rh;
+        el = 0.5f * rl;
+      }
+    }
+    Eh[t] = eh;
+    El[t] = el;
+  }
+}
+
+// Rank sort of the eigenvalues (descending, ties by index): perm[rank] = i.
+__global__ void rank_desc_kernel(const float* __restrict__ lh, int n, int* __restrict__ perm) {
+  for (int i = threadIdx.x; i < n; i += blockDim.x) {
+    const float v = lh[i];
+    int rank = 0;
+    for (int j = 0; j < n; ++j) {
+      const float w = lh[j];
+      rank += (w > v) || (w == v && j < i);
+    }
+    perm[rank] = i;
+  }
+}
+
+// rows perm[0..keep) of the refined Vt: FP64 core (keep x n) and its pair copy
+__global__ void gather_rows_kernel(const float* __restrict__ Vh, const float* __restrict__ Vl, int n,
+                                   const int* __restrict__ perm, int keep, double* __restrict__ core,
+                                   float* __restrict__ Kh, float* __restrict__ Kl) {
+  for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < (int64_t)keep * n;
+       t += (int64_t)gridDim.x * blockDim.x) {
+    const int r = (int)(t / n), c = (int)(t % n);
+    const int64_t s = (int64_t)perm[r] * n + c;
+    const float h = Vh[s], l = Vl[s];
+    core[t] = (double)h + (double)l;
+    Kh[t] = h;
+    Kl[t] = l;
+  }
+}
+
+// spectra (descending) = sqrt(l 2^gexp), discarded = sum_{j >= keep} l_j / sum l_j
+__global__ void oz_spectrum_kernel(const float* __restrict__ lh, const float* __restrict__ ll,
+                                   const int* __restrict__ perm, int count, int keep, double* __restrict__ spec,
+                                   double* __restrict__ disc, const int* __restrict__ gexp) {
+  __shared__ double red[2][32];
+  double tot = 0.0, drop = 0.0;
+  const int ge = gexp ? *gexp : 0;
+  for (int j = threadIdx.x; j < count; j += blockDim.x) {
+    const int i = perm[j];
+    const double v = fmax((double)lh[i] + (double)ll[i], 0.0);
+    if (spec) spec[j] = sqrt(ldexp(v, ge));
+    tot += v;
+    if (j >= keep) drop += v;
+  }
+  for (int o = 16; o > 0; o >>= 1) {
+    tot += __shfl_xor_sync(0xffffffffu, tot, o);
+    drop += __shfl_xor_sync(0xffffffffu, drop, o);
+  }
+  if ((threadIdx.x & 31) == 0) red[0][threadIdx.x >> 5] = tot, red[1][threadIdx.x >> 5] = drop;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double t = 0.0, d = 0.0;
+    for (int w = 0; w < (int)(blockDim.x >> 5); ++w) t += red[0][w], d += red[1][w];
+    if (disc) *disc = (t > 0.0) ? d / t : 0.0;
+  }
+}
+
+__global__ void oz_status_kernel(const int* __restrict__ st, int n, int* __restrict__ out, const int* __restrict__ err) {
+  if (threadIdx.x != 0) return;
+  int r = 0;
+  for (int k = 1; k < n; ++k) {
+    if (st[k] < 0) {
+      r = -1;
+      break;
+    }
+    r = max(r, st[k]);
+  }
+  if (err && *err) r = -2;
+  *out = r;
+}
+
+__global__ void identity_cores_f64_kernel(double* __restrict__ eye, const int* __restrict__ dims, int n, int stride) {
+  for (int k = blockIdx.x; k < n; k += gridDim.x) {
+    const int d = dims[k];
+    for (int i = threadIdx.x; i < d * d; i += blockDim.x) eye[(int64_t)k * stride + i] = (i / d == i % d) ? 1.0 : 0.0;
+  }
+}
+
+// C = alpha (h + l) + beta C in FP64 (beta == 0 does not read C)
+__global__ void axpby_pair_f64_kernel(const float* __restrict__ h, const float* __restrict__ l, int64_t lds,
+                                      double alpha, double beta, double* __restrict__ C, int64_t ldc, int64_t rows,
+                                      int64_t cols) {
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < rows * cols;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t r = i / cols, c = i % cols;
+    const double v = alpha * ((double)h[r * lds + c] + (double)l[r * lds + c]);
+    double* dst = C + r * ldc + c;
+    *dst = (beta == 0.0) ? v : fma(beta, *dst, v);
+  }
+}
+
+struct Site4 {
+  int64_t b, i, o, b2;
+};
+
+// Pair matrix buffers (hi, lo) carved from the arena.
+struct Pair {
+  float* h = nullptr;
+  float* l = nullptr;
+};
+Pair take_pair(Arena& ar, int64_t count) {
+  Pair p;
+  p.h = ar.take<float>((size_t)count);
+  p.l = ar.take<float>((size_t)count);
+  return p;
+}
+
+// Slices + per-row exponents of a rows x cols operand.
+struct Sliced {
+  __nv_bfloat16* s = nullptr;
+  int* e = nullptr;
+  int64_t rows = 0, cols = 0;
+  OzMat mat() const { return oz_mat(s, rows, cols, e); }
+};
+Sliced take_sliced(Arena& ar, int64_t rows, int64_t cols) {
+  Sliced q;
+  q.s = ar.take<__nv_bfloat16>(oz_slice_elems(rows, cols));
+  q.e = ar.take<int>((size_t)rows);
+  q.rows = rows;
+  q.cols = cols;
+  return q;
+}
+
+int split_pair(cudaStream_t st, const Pair& p, int64_t ld, Sliced& q, int64_t rows, int64_t cols) {
+  q.rows = rows;
+  q.cols = cols;
+  return oz_split_pair(st, p.h, p.l, ld, rows, cols, q.s, q.e, 1);
+}
+
+int pair_transpose(cudaStream_t st, Pair dst, int64_t ldd, int64_t db, Pair src, int64_t lds, int64_t sb, int64_t rows,
+                   int64_t cols, int64_t batch) {
+  if (rows <= 0 || cols <= 0 || batch <= 0) return SGT_OK;
+  const int64_t tiles = cdiv(rows, 32) * cdiv(cols, 32);
+  dim3 g((unsigned)std::min<int64_t>(tiles, 1024), 1, (unsigned)batch);
+  pair_transpose_kernel<<<g, dim3(32, 8), 0, st>>>(dst.h, dst.l, ldd, db, src.h, src.l, lds, sb, rows, cols);
+  SGT_LAUNCHED();
+  return SGT_OK;
+}
+
+int mid_tc(int64_t D, int64_t d, int64_t dout, int64_t D2) {
+  int TC = 8;
+  while (TC > 1 && mid_df_smem((int)D, (int)d, (int)dout, (int)D2, TC) > 200 * 1024) TC /= 2;
+  return mid_df_smem((int)D, (int)d, (int)dout, (int)D2, TC) <= 200 * 1024 ? TC : 0;
+}
+
+}  // namespace
+
+bool oz_round_supported(int n, const int64_t* ws4) {
+  for (int k = 0; k + 1 < n; ++k)
+    if (mid_tc(ws4[4 * k], ws4[4 * k + 1], ws4[4 * k + 2], ws4[4 * k + 3]) == 0) return false;
+  return true;
+}
+
+// ---------------------------------------------------------------------------
+int oz_round_impl(cudaStream_t st, int n, const double* const* W, const int64_t* ws4, const double* const* X,
+                  const int64_t* xs, int64_t chi, double* const* out, double* spectra, double* discarded, int* status,
+                  Arena& ar) {
+  std::vector<Site4> w(n);
+  std::vector<int64_t> R(n + 1), Pd(n), shp(3 * n);
+  for (int k = 0; k < n; ++k) {
+    w[k] = {ws4[4 * k], ws4[4 * k + 1], ws4[4 * k + 2], ws4[4 * k + 3]};
+    SGT_REQUIRE(xs[3 * k + 1] == w[k].i, SGT_ERR_INVALID, "mpo_mps_round: leg mismatch at site %d", k);
+    R[k] = xs[3 * k] * w[k].b;
+    Pd[k] = w[k].o;
+  }
+  R[n] = xs[3 * (n - 1) + 2] * w[n - 1].b2;
+  SGT_REQUIRE(R[0] == 1 && R[n] == 1, SGT_ERR_INVALID, "mpo_mps_round: boundary bonds must be 1");
+  SGT_REQUIRE(oz_round_supported(n, ws4), SGT_ERR_INVALID,
+              "mpo_mps_round: operator bonds too large for the pair-precision Gram step");
+  for (int k = 0; k < n; ++k) shp[3 * k] = R[k], shp[3 * k + 1] = Pd[k], shp[3 * k + 2] = R[k + 1];
+  std::vector<int64_t> bb, x, cnt;
+  svd_round_plan_public(n, shp.data(), chi, bb, x, cnt);
+
+  // ---- workspace ----
+  int64_t rmax = 1, cmax = 1, xmax = 1, wmax = 1, t1max = 1, t3max = 1, pmax = 1, pemax = 1;
+  size_t gsmax = 1, xtmax = 1, x2max = 1, t3smax = 1;
+  int64_t gcrows = 1, xtrows = 1, x2rows = 1, t3rows = 1;
+  for (int k = 0; k < n; ++k) {
+    rmax = std::max(rmax, std::max(R[k], R[k + 1]));
+    cmax = std::max(cmax, Pd[k] * x[k + 1]);
+    xmax = std::max<int64_t>(xmax, xs[3 * k] * xs[3 * k + 1] * xs[3 * k + 2]);
+    wmax = std::max<int64_t>(wmax, w[k].b * w[k].i * w[k].o * w[k].b2);
+    pmax = std::max<int64_t>(pmax, (int64_t)oz_slice_elems(R[k] * Pd[k], R[k + 1]));
+    pemax = std::max<int64_t>(pemax, R[k] * Pd[k]);
+    if (k + 1 < n) {
+      const int64_t chi_k = xs[3 * k], d = xs[3 * k + 1], chi2 = xs[3 * k + 2];
+      t1max = std::max<int64_t>(t1max, chi_k * w[k].b * w[k].b * d * chi2);
+      t3max = std::max<int64_t>(t3max, chi2 * w[k].b2 * w[k].b2 * chi_k * d);
+      gsmax = std::max(gsmax, oz_slice_elems(R[k] * R[k] / chi_k, chi_k));
+      gcrows = std::max(gcrows, R[k] * R[k] / chi_k);
+      xtmax = std::max(xtmax, oz_slice_elems(d * chi2, chi_k));
+      xtrows = std::max(xtrows, d * chi2);
+      x2max = std::max(x2max, oz_slice_elems(chi2, chi_k * d));
+      x2rows = std::max(x2rows, chi2);
+      t3smax = std::max(t3smax, oz_slice_elems(chi2 * w[k].b2 * w[k].b2, chi_k * d));
+      t3rows = std::max(t3rows, chi2 * w[k].b2 * w[k].b2);
+    }
+  }
+  auto take_raw = [&](size_t elems, int64_t rows) {
+    Sliced q;
+    q.s = ar.take<__nv_bfloat16>(elems);
+    q.e = ar.take<int>((size_t)rows);
+    return q;
+  };
+  // G_k slices with rows of R_k (kept for the right sweep)
+  std::vector<Sliced> GsR(n);
+  for (int k = 0; k < n; ++k) GsR[k] = take_sliced(ar, R[k], R[k]);
+  Sliced Gchi = take_raw(gsmax, gcrows);  // G_k with rows of chi_k (next Gram step), reused
+  Pair G = take_pair(ar, rmax * rmax);
+  Pair T1 = take_pair(ar, t1max);
+  Pair T3 = take_pair(ar, t3max);
+  Sliced T3s = take_raw(t3smax, t3rows);
+  Sliced Xt = take_raw(xtmax, xtrows), X2 = take_raw(x2max, x2rows);
+  Pair pX = take_pair(ar, xmax), pW = take_pair(ar, wmax);
+  __nv_bfloat16* Ps = ar.take<__nv_bfloat16>((size_t)pmax);
+  int* Pe_all = ar.take<int>((size_t)pemax);
+  Pair Ft = take_pair(ar, chi * rmax + 1);
+  Sliced Fts = take_sliced(ar, chi, rmax);
+  Pair Yt = take_pair(ar, cmax * rmax), Ytp = take_pair(ar, cmax * rmax), GY = take_pair(ar, cmax * rmax);
+  Sliced Yts = take_sliced(ar, cmax, rmax), Ytps = take_sliced(ar, cmax, rmax), GYs = take_sliced(ar, cmax, rmax);
+  Sliced Ys = take_sliced(ar, rmax, cmax);
+  Pair Z = take_pair(ar, cmax * cmax);
+  float* Z32 = ar.take<float>((size_t)(cmax * cmax));
+  float* Vt32 = ar.take<float>((size_t)(cmax * cmax));
+  float* lam32 = ar.take<float>((size_t)cmax);
+  Pair Vt = take_pair(ar, cmax * cmax), Xv = take_pair(ar, cmax * cmax), VV = take_pair(ar, cmax * cmax);
+  Pair T = take_pair(ar, cmax * cmax), S = take_pair(ar, cmax * cmax), Et = take_pair(ar, cmax * cmax);
+  Pair lamp = take_pair(ar, cmax);
+  Sliced Vts = take_sliced(ar, cmax, cmax), Xvs = take_sliced(ar, cmax, cmax), Zs = take_sliced(ar, cmax, cmax);
+  Sliced Ts = take_sliced(ar, cmax, cmax), Ets = take_sliced(ar, cmax, cmax);
+  Pair Vk = take_pair(ar, chi * cmax);
+  Sliced Vks = take_sliced(ar, chi, cmax);
+  int* perm = ar.take<int>((size_t)cmax);
+  // split-K partials: the largest requirement of the products below
+  size_t part_bytes = 0;
+  for (int k = 0; k < n; ++k) {
+    const int64_t r = R[k], r2 = R[k + 1], c = Pd[k] * x[k + 1];
+    part_bytes = std::max(part_bytes, oz_gemm_ws_bytes(x[k + 1], r, r2));
+    part_bytes = std::max(part_bytes, oz_gemm_ws_bytes(c, r, r));
+    part_bytes = std::max(part_bytes, oz_gemm_ws_bytes(c, c, r));
+    part_bytes = std::max(part_bytes, oz_gemm_ws_bytes(c, c, c));
+    part_bytes = std::max(part_bytes, oz_gemm_ws_bytes(x[k], r, c));
+    if (k + 1 < n) {
+      const int64_t chi_k = xs[3 * k], d = xs[3 * k + 1], chi2 = xs[3 * k + 2];
+      part_bytes = std::max(part_bytes, oz_gemm_ws_bytes(chi_k * w[k].b * w[k].b, d * chi2, chi_k));
+      part_bytes = std::max(part_bytes, oz_gemm_ws_bytes(chi2 * w[k].b2 * w[k].b2, chi2, chi_k * d));
+    }
+  }
+  float* part = ar.take<float>(part_bytes / sizeof(float) + 1);
+  const int64_t part_floats = (int64_t)(part_bytes / sizeof(float));
+  int* stat = ar.take<int>((size_t)n + 1);
+  int* err = ar.take<int>(1);
+  int* gexp = ar.take<int>((size_t)n + 1);
+  unsigned* gmax = ar.take<unsigned>(1);
+  const size_t jbytes = sym_eig_rows_ws_bytes(cmax);
+  char* jscratch = ar.take<char>(jbytes);
+  if (ar.measure) return SGT_OK;
+  SGT_REQUIRE(ar.ok(), SGT_ERR_WORKSPACE, "mpo_mps_round: workspace too small");
+  SGT_CUDA(cudaMemsetAsync(stat, 0, sizeof(int) * (n + 1), st));
+  SGT_CUDA(cudaMemsetAsync(err, 0, sizeof(int), st));
+  SGT_CUDA(cudaMemsetAsync(gexp, 0, sizeof(int) * (n + 1), st));
+
+  auto gemm = [&](int64_t M, int64_t N, int64_t K, float alpha, const OzMat& A, const OzMat& B, float beta,
+                  Pair C, int64_t ldc) -> int {
+    return oz_gemm(st, M, N, K, alpha, A, B, beta, C.h, C.l, ldc, part, part_floats, err);
+  };
+
+  // ---- left Gram recursion (structured: X and W contractions, no product) ----
+  pair_one_kernel<<<1, 1, 0, st>>>(G.h, G.l);
+  SGT_LAUNCHED();
+  SGT_TRY(split_pair(st, G, 1, GsR[0], 1, 1));
+  for (int k = 0; k + 1 < n; ++k) {
+    const int64_t chi_k = xs[3 * k], d = xs[3 * k + 1], chi2 = xs[3 * k + 2];
+    const int64_t D = w[k].b, dout = w[k].o, D2 = w[k].b2;
+    // G_k as rows of chi_k (its columns are in (b, a) order, so a row of chi_k is one b)
+    if (k == 0) {
+      SGT_TRY(split_pair(st, G, 1, Gchi, 1, 1));
+    } else {
+      SGT_TRY(split_pair(st, G, chi_k, Gchi, R[k] * R[k] / chi_k, chi_k));
+    }
+    // Xt[(j,c')][c] = X[c][j][c'],  X2[a'][(a,i)] = X[a][i][a']
+    SGT_TRY(oz_split_f64(st, X[k], 1, d * chi2, d * chi2, chi_k, Xt.s, Xt.e, 1));
+    Xt.rows = d * chi2;
+    Xt.cols = chi_k;
+    SGT_TRY(oz_split_f64(st, X[k], 1, chi2, chi2, chi_k * d, X2.s, X2.e, 1));
+    X2.rows = chi2;
+    X2.cols = chi_k * d;
+    // A: T1 ((chi D D) x (d chi2)) = G_k (rows of chi) Xt^T
+    SGT_TRY(gemm(chi_k * D * D, d * chi2, chi_k, 1.f, Gchi.mat(), Xt.mat(), 0.f, T1, d * chi2));
+    // B + C in pair arithmetic
+    const int TC = mid_tc(D, d, dout, D2);
+    const size_t smem = mid_df_smem((int)D, (int)d, (int)dout, (int)D2, TC);
+    SGT_CUDA(func_attr_at_least((const void*)gram_mid_df_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                (int)smem));
+    dim3 g((unsigned)cdiv(chi_k, MD_TA), (unsigned)cdiv(chi2, TC));
+    gram_mid_df_kernel<<<g, 256, smem, st>>>(T1.h, T1.l, W[k], T3.h, T3.l, (int)chi_k, (int)D, (int)d, (int)dout,
+                                             (int)D2, (int)chi2, TC);
+    SGT_LAUNCHED();
+    // D: G_{k+1} ((chi2 D2 D2) x chi2) = T3 X2^T
+    SGT_TRY(split_pair(st, T3, chi_k * d, T3s, chi2 * D2 * D2, chi_k * d));
+    SGT_TRY(gemm(chi2 * D2 * D2, chi2, chi_k * d, 1.f, T3s.mat(), X2.mat(), 0.f, G, chi2));
+    // exact power-of-two scaling against range loss over long chains
+    const int64_t gn = R[k + 1] * R[k + 1];
+    SGT_CUDA(cudaMemsetAsync(gmax, 0, sizeof(unsigned), st));
+    pair_absmax_kernel<<<grid_for(gn), 256, 0, st>>>(G.h, gn, gmax);
+    SGT_LAUNCHED();
+    pair_scale_kernel<<<grid_for(gn), 256, 0, st>>>(G.h, G.l, gn, gmax, gexp + k, gexp + k + 1);
+    SGT_LAUNCHED();
+    SGT_TRY(split_pair(st, G, R[k + 1], GsR[k + 1], R[k + 1], R[k + 1]));
+  }
+
+  // ---- right-to-left projections, bond eigensolves, refinement ----
+  pair_one_kernel<<<1, 1, 0, st>>>(Ft.h, Ft.l);
+  SGT_LAUNCHED();
+  for (int k = n - 1; k >= 0; --k) {
+    const int64_t r = R[k], r2 = R[k + 1], p = Pd[k], xc = x[k + 1], c = p * xc;
+    const int64_t xsz = xs[3 * k] * xs[3 * k + 1] * xs[3 * k + 2], wsz = w[k].b * w[k].i * w[k].o * w[k].b2;
+    // product core P_k sliced by rows (a, b, o), straight from X_k and W_k
+    f64_to_pair_kernel<<<grid_for(xsz), 256, 0, st>>>(X[k], pX.h, pX.l, xsz);
+    SGT_LAUNCHED();
+    f64_to_pair_kernel<<<grid_for(wsz), 256, 0, st>>>(W[k], pW.h, pW.l, wsz);
+    SGT_LAUNCHED();
+    const int64_t prow = r * p, pld = oz_ld(r2), pss = prow * pld;
+    SGT_REQUIRE(prow < (1ll << 31), SGT_ERR_INVALID, "mpo_mps_round: product core too tall");
+    product_slices_kernel<<<(unsigned)prow, 256, 0, st>>>(pX.h, pX.l, pW.h, pW.l, (int)w[k].b, (int)w[k].i,
+                                                          (int)w[k].o, (int)xs[3 * k + 2], (int)w[k].b2, Ps, pld, pss,
+                                                          Pe_all);
+    SGT_LAUNCHED();
+    // Yt (c x r): rows o*xc..: Ft (xc x r2) P[:, o, :]^T
+    SGT_TRY(split_pair(st, Ft, r2, Fts, xc, r2));
+    for (int64_t o = 0; o < p; ++o) {
+      OzMat Po{Ps + o * pld, pld * p, pss, Pe_all + o, p};
+      Pair dst{Yt.h + o * xc * r, Yt.l + o * xc * r};
+      SGT_TRY(gemm(xc, r, r2, 1.f, Fts.mat(), Po, 0.f, dst, r));
+    }
+    if (k == 0) {
+      // core_0[0][o][j] = Yt[o*xc + j][0]
+      pair_to_f64_kernel<<<grid_for(c), 256, 0, st>>>(Yt.h, Yt.l, 1, out[0], 1, c, 1);
+      SGT_LAUNCHED();
+      break;
+    }
+    const int64_t keep = x[k];
+    // GY (c x r) = Ytp G_k^T, with Ytp = Yt's columns in G_k's (b, a) column order
+    const int64_t chik = xs[3 * k], Dk = w[k].b;
+    SGT_TRY(pair_transpose(st, Ytp, chik, r, Yt, Dk, r, chik, Dk, c));
+    SGT_TRY(split_pair(st, Ytp, r, Ytps, c, r));
+    SGT_TRY(gemm(c, r, r, 1.f, Ytps.mat(), GsR[k].mat(), 0.f, GY, r));
+    // Z (c x c) = Yt GY^T
+    SGT_TRY(split_pair(st, Yt, r, Yts, c, r));
+    SGT_TRY(split_pair(st, GY, r, GYs, c, r));
+    SGT_TRY(gemm(c, c, r, 1.f, Yts.mat(), GYs.mat(), 0.f, Z, c));
+    pair_symmetrize_kernel<<<grid_for(c * c), 256, 0, st>>>(Z.h, Z.l, c);
+    SGT_LAUNCHED();
+    // FP32 Jacobi on the leading part of Z: first approximation
+    SGT_CUDA(cudaMemcpyAsync(Z32, Z.h, sizeof(float) * c * c, cudaMemcpyDeviceToDevice, st));
+    {
+      Arena ja(jscratch, jbytes);
+      SGT_TRY(sym_eig_rows_f32(st, Z32, c, Vt32, lam32, stat + k, ja, 1));
+    }
+    SGT_CUDA(cudaMemcpyAsync(Vt.h, Vt32, sizeof(float) * c * c, cudaMemcpyDeviceToDevice, st));
+    SGT_CUDA(cudaMemsetAsync(Vt.l, 0, sizeof(float) * c * c, st));
+    // refinement against the pair-accurate Z
+    SGT_TRY(split_pair(st, Z, c, Zs, c, c));
+    for (int it = 0; it < 2; ++it) {
+      SGT_TRY(split_pair(st, Vt, c, Vts, c, c));
+      SGT_TRY(gemm(c, c, c, 1.f, Vts.mat(), Vts.mat(), 0.f, VV, c));   // VV = Vt Vt^T
+      SGT_TRY(gemm(c, c, c, 1.f, Vts.mat(), Zs.mat(), 0.f, T, c));     // T = Vt Z
+      SGT_TRY(split_pair(st, T, c, Ts, c, c));
+      SGT_TRY(gemm(c, c, c, 1.f, Ts.mat(), Vts.mat(), 0.f, S, c));     // S = Vt Z Vt^T
+      oa_lambda_kernel<<<grid_for(c), 256, 0, st>>>(S.h, S.l, VV.h, VV.l, (int)c, lamp.h, lamp.l);
+      SGT_LAUNCHED();
+      oa_correction_kernel<<<grid_for(c * c), 256, 0, st>>>(S.h, S.l, VV.h, VV.l, lamp.h, lamp.l, (int)c, Et.h, Et.l);
+      SGT_LAUNCHED();
+      SGT_TRY(split_pair(st, Et, c, Ets, c, c));
+      SGT_TRY(pair_transpose(st, Xv, c, 0, Vt, c, 0, c, c, 1));             // Xv = Vt^T
+      SGT_TRY(split_pair(st, Xv, c, Xvs, c, c));
+      SGT_TRY(gemm(c, c, c, 1.f, Ets.mat(), Xvs.mat(), 1.f, Vt, c));   // Vt += E^T Vt
+    }
+    // final eigenvalues of the refined vectors
+    SGT_TRY(split_pair(st, Vt, c, Vts, c, c));
+    SGT_TRY(gemm(c, c, c, 1.f, Vts.mat(), Vts.mat(), 0.f, VV, c));
+    SGT_TRY(gemm(c, c, c, 1.f, Vts.mat(), Zs.mat(), 0.f, T, c));
+    SGT_TRY(split_pair(st, T, c, Ts, c, c));
+    SGT_TRY(gemm(c, c, c, 1.f, Ts.mat(), Vts.mat(), 0.f, S, c));
+    oa_lambda_kernel<<<grid_for(c), 256, 0, st>>>(S.h, S.l, VV.h, VV.l, (int)c, lamp.h, lamp.l);
+    SGT_LAUNCHED();
+    rank_desc_kernel<<<1, 1024, 0, st>>>(lamp.h, (int)c, perm);
+    SGT_LAUNCHED();
+    gather_rows_kernel<<<grid_for(keep * c), 256, 0, st>>>(Vt.h, Vt.l, (int)c, perm, (int)keep, out[k], Vk.h, Vk.l);
+    SGT_LAUNCHED();
+    double* spec_k = nullptr;
+    if (spectra) {
+      int64_t off = 0;
+      for (int j = 1; j < k; ++j) off += cnt[j];
+      spec_k = spectra + off;
+    }
+    oz_spectrum_kernel<<<1, 256, 0, st>>>(lamp.h, lamp.l, perm, (int)cnt[k], (int)keep, spec_k,
+                                          discarded ? discarded + (k - 1) : nullptr, gexp + k);
+    SGT_LAUNCHED();
+    // Ft_k (keep x r) = Vk Y^T with Y = Yt^T (r x c)
+    Pair Y = Ytp;  // Ytp is free again
+    SGT_TRY(pair_transpose(st, Y, c, 0, Yt, r, 0, c, r, 1));
+    SGT_TRY(split_pair(st, Y, c, Ys, r, c));
+    SGT_TRY(split_pair(st, Vk, c, Vks, keep, c));
+    SGT_TRY(gemm(keep, r, c, 1.f, Vks.mat(), Ys.mat(), 0.f, Ft, r));
+  }
+  if (status) {
+    oz_status_kernel<<<1, 32, 0, st>>>(stat, n, status, err);
+    SGT_LAUNCHED();
+  }
+  return SGT_OK;
+}
+
+// TT-SVD rounding of a plain chain in this form: the chain is the product of
+// a bond-1 identity MPO with itself (one d x d identity core per site).
+int oz_round_chain(cudaStream_t st, int n, const double* const* X, const int64_t* xs, int64_t chi, double* const* out,
+                   double* spectra, double* discarded, int* status, Arena& ar) {
+  std::vector<int64_t> w4(4 * (size_t)n);
+  std::vector<int> dims(n);
+  int64_t dmax = 1;
+  for (int k = 0; k < n; ++k) {
+    const int64_t d = xs[3 * k + 1];
+    w4[4 * k] = 1;
+    w4[4 * k + 1] = d;
+    w4[4 * k + 2] = d;
+    w4[4 * k + 3] = 1;
+    dims[k] = (int)d;
+    dmax = std::max(dmax, d);
+  }
+  double* eye = ar.take<double>((size_t)n * dmax * dmax);
+  int* ddims = ar.take<int>((size_t)n);
+  std::vector<const double*> W(n, nullptr);
+  if (!ar.measure) {
+    SGT_REQUIRE(ar.ok(), SGT_ERR_WORKSPACE, "round: workspace too small");
+    SGT_CUDA(cudaMemcpyAsync(ddims, dims.data(), sizeof(int) * n, cudaMemcpyHostToDevice, st));
+    identity_cores_f64_kernel<<<(unsigned)std::min(n, 1024), 128, 0, st>>>(eye, ddims, n, (int)(dmax * dmax));
+    SGT_LAUNCHED();
+    for (int k = 0; k < n; ++k) W[k] = eye + (int64_t)k * dmax * dmax;
+  }
+  return oz_round_impl(st, n, W.data(), w4.data(), X, xs, chi, out, spectra, discarded, status, ar);
+}
+
+// FP64 in / FP64 out through the sliced GEMM (exported for tests and callers):
+// C = alpha A B^T + beta C, A (M x K, lda), B (N x K, ldb), C (M x N, ldc).
+static int gemm_f64_sliced_impl(cudaStream_t st, int64_t M, int64_t N, int64_t K, double alpha, const double* A,
+                                int64_t lda, const double* B, int64_t ldb, double beta, double* C, int64_t ldc,
+                                Arena& ar) {
+  SGT_REQUIRE(M > 0 && N > 0 && K > 0, SGT_ERR_INVALID, "gemm_f64_sliced: empty problem");
+  Sliced As = take_sliced(ar, M, K), Bs = take_sliced(ar, N, K);
+  Pair Cp = take_pair(ar, M * N);
+  const size_t pb = oz_gemm_ws_bytes(M, N, K);
+  float* part = ar.take<float>(pb / sizeof(float) + 1);
+  int* err = ar.take<int>(1);
+  if (ar.measure) return SGT_OK;
+  SGT_REQUIRE(ar.ok(), SGT_ERR_WORKSPACE, "gemm_f64_sliced: workspace too small");
+  SGT_TRY(oz_split_f64(st, A, lda, 1, M, K, As.s, As.e, 1));
+  SGT_TRY(oz_split_f64(st, B, ldb, 1, N, K, Bs.s, Bs.e, 1));
+  SGT_CUDA(cudaMemsetAsync(err, 0, sizeof(int), st));
+  SGT_TRY(oz_gemm(st, M, N, K, 1.f, As.mat(), Bs.mat(), 0.f, Cp.h, Cp.l, N, part, (int64_t)(pb / sizeof(float)), err));
+  // C = alpha * (Ch + Cl) + beta * C in FP64 (alpha / beta stay FP64)
+  axpby_pair_f64_kernel<<<grid_for(M * N), 256, 0, st>>>(Cp.h, Cp.l, N, alpha, beta, C, ldc, M, N);
+  SGT_LAUNCHED();
+  return SGT_OK;
+}
+
+}  // namespace sgt
+
+using namespace sgt;
+
+extern "C" SGT_API size_t sgt_gemm_f64_sliced_workspace_size(int64_t M, int64_t N, int64_t K) {
+  Arena a = Arena::measuring();
+  if (gemm_f64_sliced_impl(nullptr, M, N, K, 1.0, nullptr, K, nullptr, K, 0.0, nullptr, N, a) != SGT_OK) return 0;
+  return a.used;
+}
+
+extern "C" SGT_API int sgt_gemm_f64_sliced(int64_t M, int64_t N, int64_t K, double alpha, const double* A, int64_t lda,
+                                           const double* B, int64_t ldb, double beta, double* C, int64_t ldc, void* ws,
+                                           size_t ws_bytes, void* stream) {
+  SGT_REQUIRE(A && B && C && ws, SGT_ERR_INVALID, "gemm_f64_sliced: null argument");
+  Arena a(ws, ws_bytes);
+  return gemm_f64_sliced_impl(as_stream(stream), M, N, K, alpha, A, lda, B, ldb, beta, C, ldc, a);
+}
+
+extern "C" SGT_API int sgt_sliced_profile(int enable, double* ms, double* flops, long long* launches) {
+  return sgt::oz_profile(enable, ms, flops, launches);
+}

@@ -1,0 +1,147 @@
+"""FP64-class sliced bf16 GEMM (tcgen05 kind::f16) and the SGT_PREC_BF16X5
+rounding form built on it, against numpy FP64 and the FP64 oracle.
+
+Tolerances: the GEMM keeps ~2^-35 of sum_k |a_ik||b_jk| (tested at 2^-32 of
+that bound elementwise, and exactly for small-integer operands, where every
+slice product and every accumulation is exact); the rounding form is held to
+a plain relative 1e-6 on <X|Z> and <Z|Z> (the accuracy bound of the
+mixed-precision target), with its measured error far below that."""
+import ctypes
+
+import numpy as np
+import pytest
+import torch
+
+from oracle import tt_fp64 as O
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module", autouse=True)
+def built():
+    import __graft_entry__ as g
+
+    g.build()
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+
+
+def sliced_gemm(A, B, alpha=1.0, beta=0.0, C=None):
+    from syngular_gb300 import _lib as L
+
+    M, K = A.shape
+    N = B.shape[0]
+    a = torch.as_tensor(A, dtype=torch.float64, device="cuda").contiguous()
+    b = torch.as_tensor(B, dtype=torch.float64, device="cuda").contiguous()
+    c = (torch.zeros((M, N), dtype=torch.float64, device="cuda") if C is None
+         else torch.as_tensor(C, dtype=torch.float64, device="cuda").clone())
+    nb = L.query("sgt_gemm_f64_sliced_workspace_size", M, N, K)
+    assert nb > 0
+    ws = L.workspace(nb)
+    L.call("sgt_gemm_f64_sliced", M, N, K, ctypes.c_double(alpha), L.ptr(a), K, L.ptr(b), K, ctypes.c_double(beta),
+           L.ptr(c), N, L.ptr(ws), ws.numel(), L.stream_ptr())
+    torch.cuda.synchronize()
+    return c.cpu().numpy()
+
+
+@pytest.mark.parametrize("M,N,K", [(200, 300, 1500), (128, 128, 64), (257, 129, 4096), (33, 517, 999)])
+def test_exact_on_small_integers(M, N, K):
+    """Integer operands of at most 7 bits fit the first slice exactly, so the
+    tensor-core result must equal the exact integer product (also across the
+    split-K partials when K > 1024)."""
+    rng = np.random.default_rng(M + N + K)
+    A = rng.integers(-64, 65, size=(M, K)).astype(np.float64)
+    B = rng.integers(-64, 65, size=(N, K)).astype(np.float64)
+    C = sliced_gemm(A, B)
+    np.testing.assert_array_equal(C, A @ B.T)
+
+
+@pytest.mark.parametrize("M,N,K", [(512, 4096, 4096), (1000, 256, 512), (512, 512, 512), (7, 9, 3), (4096, 64, 256)])
+def test_accuracy_bound(M, N, K):
+    rng = np.random.default_rng(7 * M + N)
+    A = rng.standard_normal((M, K)) * np.exp(rng.uniform(-3, 3, size=(M, 1)))
+    B = rng.standard_normal((N, K))
+    C = sliced_gemm(A, B)
+    ref = A @ B.T
+    err = np.abs(C - ref)
+    # slicing keeps every entry to 2^-35 of its row's (column's) largest entry
+    scale = np.max(np.abs(A), axis=1)[:, None] * np.max(np.abs(B), axis=1)[None, :]
+    assert np.all(err <= 2.0 ** -33 * K * scale), float(np.max(err / (K * scale)))
+    # independent truncation errors: ~2^-35 sqrt(K) of that scale in the median
+    assert float(np.median(err / (np.sqrt(K) * scale))) < 2.0 ** -33
+    # and far below split TF32 (2^-22) relative to sum_k |a_ik| |b_jk|
+    bound = np.abs(A) @ np.abs(B).T
+    assert float(np.max(err / bound)) < 2.0 ** -28
+
+
+def test_alpha_beta():
+    rng = np.random.default_rng(3)
+    A = rng.standard_normal((130, 70))
+    B = rng.standard_normal((90, 70))
+    C0 = rng.standard_normal((130, 90))
+    C = sliced_gemm(A, B, alpha=-0.75, beta=2.0, C=C0)
+    np.testing.assert_allclose(C, -0.75 * (A @ B.T) + 2.0 * C0, rtol=0, atol=1e-9)
+
+
+def dev(cores):
+    from syngular_gb300 import _lib
+
+    return [_lib.as_device(c) for c in cores]
+
+
+def rel_overlaps(X, Z, Zr):
+    from syngular_gb300.tensor import _ops
+
+    Xd = dev(X)
+    ov, ovr = _ops.overlap(Xd, Z), O.overlap(X, Zr)
+    zz, zzr = _ops.overlap(Z, Z), O.overlap(Zr, Zr)
+    return abs(ov - ovr) / abs(ovr), abs(zz - zzr) / abs(zzr)
+
+
+CASES = [(6, 2, 8, 3, 5), (10, 2, 32, 4, 24), (8, 3, 16, 4, 20), (12, 2, 64, 8, 64), (8, 2, 32, 16, 48),
+         (7, 3, 16, 8, 30), (14, 2, 64, 16, 40)]
+
+
+@pytest.mark.parametrize("n,d,chi,D,cut", CASES)
+def test_bf16x5_round_matches_oracle(n, d, chi, D, cut):
+    from syngular_gb300 import _lib as L
+    from syngular_gb300.tensor import _ops
+
+    rng = np.random.default_rng(1000 * n + chi)
+    X = O.random_mps_cores(rng, n, d, chi)
+    W = O.random_mpo_cores(rng, n, d, D)
+    Zr, spec_r, disc_r = O.tt_svd_round(O.mpo_mps_product(W, X), cut)
+    Z, spec, counts, disc, status = _ops.mpo_mps_round(dev(W), dev(X), cut, L.PREC_BF16X5)
+    torch.cuda.synchronize()
+    assert int(status.item()) >= 0
+    assert [tuple(z.shape) for z in Z] == [z.shape for z in Zr]
+    e_ov, e_zz = rel_overlaps(X, Z, Zr)
+    assert e_ov < 1e-6 and e_zz < 1e-6, (e_ov, e_zz)
+    assert e_ov < 1e-8 and e_zz < 1e-9, (e_ov, e_zz)  # the form's own accuracy, well inside the bound
+    s = spec.cpu().numpy()
+    off = 0
+    for k in range(n - 1):
+        m = min(counts[k], len(spec_r[k]))
+        np.testing.assert_allclose(s[off:off + m], spec_r[k][:m], rtol=0, atol=1e-8 * spec_r[k][0])
+        off += counts[k]
+    np.testing.assert_allclose(disc.cpu().numpy()[: n - 1], disc_r, rtol=1e-6, atol=1e-12)
+
+
+def test_bf16x5_svd_round_chain():
+    """sgt_svd_round in the BF16X5 form on a plain chain (a direct sum, so the
+    bond matrices are rank-deficient), against the oracle."""
+    from syngular_gb300 import _lib as L
+    from syngular_gb300.tensor import _ops
+
+    rng = np.random.default_rng(21)
+    A = O.random_mps_cores(rng, 10, 2, 24)
+    B = O.random_mps_cores(rng, 10, 2, 24)
+    S = O.direct_sum(A, B)
+    Zr, spec_r, _ = O.tt_svd_round(S, 20)
+    Z, spec, counts, disc, status = _ops.svd_round(dev(S), 20, L.PREC_BF16X5)
+    torch.cuda.synchronize()
+    assert int(status.item()) >= 0
+    ov, ovr = _ops.overlap(dev(A), Z), O.overlap(A, Zr)
+    assert abs(ov - ovr) / abs(ovr) < 1e-8
+    zz, zzr = _ops.overlap(Z, Z), O.overlap(Zr, Zr)
+    assert abs(zz - zzr) / zzr < 1e-9
