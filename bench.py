@@ -43,6 +43,10 @@ sys.path.insert(0, ROOT)
 N_SITES, D_PHYS, CHI, D_MPO = 64, 2, 256, 16
 SEED = 2024
 METRIC = "MPO·MPS+SVD-round sweeps/s at χ=256 vs plain FP64 GPU; p50/p99 job latency"
+# precision form -> library code (include/syngular_gb300.h SGT_PREC_*) and the arithmetic it computes in
+PRECISIONS = {"f64": 0, "tf32": 1, "tf32x3": 4, "bf16x6": 5}
+DTYPES = {"f64": "f64", "tf32": "tf32/f32", "tf32x3": "tf32x3/f32",
+          "bf16x6": "bf16x6 slices (tcgen05) / f32 pairs / f32 Jacobi + refinement"}
 
 
 def _eig_profile(enable):
@@ -282,7 +286,7 @@ def run_gpu(args, rank, world, local_rank):
 
     torch.cuda.set_device(local_rank)
     dev = torch.device("cuda", local_rank)
-    prec = {"tf32x3": L.PREC_TF32X3, "tf32": L.PREC_TF32, "f64": L.PREC_F64}[args.precision]
+    prec = PRECISIONS[args.precision]
 
     Xh, Wh = make_inputs()
     Xd = [torch.from_numpy(c).to(dev) for c in Xh]
@@ -320,6 +324,7 @@ def run_gpu(args, rank, world, local_rank):
     clocks.start()
     time.sleep(0.3)
     L.call("sgt_tc_profile", 1, None, None, None)
+    L.call("sgt_sliced_profile", 1, None, None, None)
     eig_prof = _eig_profile(True)
     launches0 = L.load().sgt_launch_count()
     barrier()
@@ -334,6 +339,8 @@ def run_gpu(args, rank, world, local_rank):
     launches = L.load().sgt_launch_count() - launches0
     tc_ms, tc_flops, tc_n = ctypes.c_double(), ctypes.c_double(), ctypes.c_longlong()
     L.call("sgt_tc_profile", 0, ctypes.byref(tc_ms), ctypes.byref(tc_flops), ctypes.byref(tc_n))
+    oz_ms, oz_flops, oz_n = ctypes.c_double(), ctypes.c_double(), ctypes.c_longlong()
+    L.call("sgt_sliced_profile", 0, ctypes.byref(oz_ms), ctypes.byref(oz_flops), ctypes.byref(oz_n))
     eig_stats = _eig_profile(False) if eig_prof is True else eig_prof
     clk = clocks.stop()
     ms_total = max_over_ranks(e0.elapsed_time(e1))
@@ -358,7 +365,7 @@ def run_gpu(args, rank, world, local_rank):
     out = {
         "metric": METRIC, "value": value, "unit": "sweeps/s", "n_gpus": world, "steps": args.steps,
         "warmup": max(args.warmup, 3), "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak",
-        "vs_baseline": None, "dtype": {"tf32x3": "tf32x3/f32", "tf32": "tf32/f32", "f64": "f64"}[args.precision],
+        "vs_baseline": None, "dtype": DTYPES[args.precision],
         "data": "synthetic (seeded N(0,1)/sqrt(chi*d) cores)",
         "config": {"workload": workload_name(), "form": args.precision, "l2": "inputs larger than L2 (split product cores %.1f GB)" % (N_SITES * 4096 * 2 * 4096 * 8 / 1e9),
                    "parallelism": "replicas" if world > 1 else "single GPU"},
@@ -379,6 +386,19 @@ def run_gpu(args, rank, world, local_rank):
         pass
     peak = peaks.get("bf16_tflops") or 1900.0
     passes = 3 if args.precision == "tf32x3" else 1
+    if oz_n.value > 0:
+        # sliced bf16 GEMM: 21 slice-pair MMAs of 2MNK each per FP64-class product
+        per_launch_s = oz_ms.value / 1e3 / oz_n.value
+        alg_flops = oz_flops.value / oz_n.value
+        achieved = alg_flops * 21 / per_launch_s / 1e12
+        out["roofline"] = {
+            "bound": "tensor", "kernel": "oz_gemm_kernel", "achieved": achieved, "peak": peak,
+            "unit": "TFLOP/s", "frac": achieved / peak, "traffic": None,
+            "note": "bf16 tensor-pipe flops (21 slice products x 2MNK) per launch / mean CUDA-event launch time "
+                    "over the timed region (split-K reduction included); peak = measured dense bf16 (burst)",
+            "share_of_step": oz_ms.value / ms_total if ms_total > 0 else None,
+            "launches": oz_n.value, "fp64_equivalent_tflops": alg_flops / per_launch_s / 1e12,
+        }
     if tc_n.value > 0:
         per_launch_s = tc_ms.value / 1e3 / tc_n.value
         alg_flops = tc_flops.value / tc_n.value
@@ -565,7 +585,7 @@ def run_config4(args):
     Bd = [torch.from_numpy(c).cuda() for c in B]
     log("inputs resident")
     S = _ops.concat(Ad, Bd)
-    prec = {"tf32x3": L.PREC_TF32X3, "tf32": L.PREC_TF32, "f64": L.PREC_F64}[args.precision]
+    prec = PRECISIONS[args.precision]
     for _ in range(args.warmup):
         Z, spec, counts, disc, status = _ops.svd_round(S, 1024, prec)
     torch.cuda.synchronize()
@@ -586,7 +606,7 @@ def run_config4(args):
     out = {
         "metric": "config4 round(A + B) to chi=1024 per second", "value": 1e3 / ms, "unit": "rounds/s",
         "n_gpus": 1, "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True,
-        "dtype": {"tf32x3": "tf32x3/f32", "tf32": "tf32/f32", "f64": "f64"}[args.precision],
+        "dtype": DTYPES[args.precision],
         "data": "synthetic seeded: geometric spectra 0.98^k, random orthogonal factors",
         "config": {"workload": "config4: two MPS N=32 d=2 chi=1024 -> direct sum (bond 2048) -> TT-SVD round "
                                "to 1024", "form": args.precision},
@@ -676,7 +696,7 @@ def main():
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="syngular", choices=["syngular", "reference"])
-    ap.add_argument("--precision", default="tf32x3", choices=["tf32x3", "tf32", "f64"])
+    ap.add_argument("--precision", default="bf16x6", choices=sorted(PRECISIONS))
     ap.add_argument("--no-plain", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--workload", default="config2", choices=["config2", "batched", "serving", "config4"])

@@ -55,9 +55,9 @@ extern "C" {
                               ~16 mantissa bits (~1.5e-5), short of the ~1e-7 that the Gram form's
                               squared spectrum needs; the split-tf32 form below keeps ~22 bits */
 #define SGT_PREC_TF32X3 4  /* split tf32 (hi*hi + hi*lo + lo*hi) on tcgen05, FP32 accumulate */
-#define SGT_PREC_BF16X5 5  /* FP64-class: every operand row cut exactly into five 7-bit bf16 slices,
-                              the 15 leading slice products on tcgen05 kind::f16 accumulated exactly
-                              in TMEM (~2^-35 of the operands' scale); elementwise work in FP32 pairs;
+#define SGT_PREC_BF16X6 5  /* FP64-class: every operand row cut exactly into six 7-bit bf16 slices,
+                              the 21 leading slice products on tcgen05 kind::f16 accumulated exactly
+                              in TMEM (~2^-41 of the operands' scale); elementwise work in FP32 pairs;
                               FP32 Jacobi eigenvectors refined against the pair-accurate bond matrix */
 
 SGT_API int sgt_version(void);
@@ -206,7 +206,7 @@ SGT_API int sgt_svd_round(int n, const double* const* cores, const int64_t* shap
  * SGT_PREC_TF32 / SGT_PREC_TF32X3: Gram form on tcgen05 -- product cores and
  * left Gram matrices in FP32, every O(R^3) step a TF32 (one pass) or split
  * 3xTF32 GEMM, eigen-solves by one-sided Jacobi (FP32 columns, FP64 angles).
- * SGT_PREC_BF16X5: the same Gram-form algebra at FP64-class accuracy -- every
+ * SGT_PREC_BF16X6: the same Gram-form algebra at FP64-class accuracy -- every
  * O(R^3) step the sliced bf16 GEMM below (sgt_gemm_f64_sliced), Gram matrices
  * and intermediates in FP32 pairs, each bond's FP32 Jacobi eigenvectors
  * refined by two Ogita-Aishima steps against the pair-accurate bond matrix;
@@ -339,13 +339,13 @@ SGT_API void sgt_batched_plan_destroy(sgt_batched_plan plan);
 
 /* FP64-class GEMM on the bf16 tensor cores: C = alpha A B^T + beta C with A
  * (M x K, lda) and B (N x K, ldb) row-major FP64, C (M x N, ldc) FP64.  Every
- * row of A and of B is scaled by a power of two and cut exactly into five
- * 7-bit slices held in bf16; the 15 slice products with slice levels
- * s + t <= 4 run as tcgen05 kind::f16 MMAs whose FP32 accumulation is exact
+ * row of A and of B is scaled by a power of two and cut exactly into six
+ * 7-bit slices held in bf16; the 21 slice products with slice levels
+ * s + t <= 5 run as tcgen05 kind::f16 MMAs whose FP32 accumulation is exact
  * over K ranges of 1024 (longer K is split and the partials added in a fixed
- * order).  Error ~2^-35 of sum_k |a_ik| |b_jk| (FP64: 2^-52; split TF32:
- * 2^-22).  The GEMM kind of the SGT_PREC_BF16X5 forms, exported for
- * composition and tests. */
+ * order).  Error ~2^-41 of the row-max times column-max scale per term
+ * (FP64: 2^-52; split TF32: 2^-22).  The GEMM kind of the SGT_PREC_BF16X6
+ * forms, exported for composition and tests. */
 SGT_API size_t sgt_gemm_f64_sliced_workspace_size(int64_t M, int64_t N, int64_t K);
 SGT_API int sgt_gemm_f64_sliced(int64_t M, int64_t N, int64_t K, double alpha, const double* A, int64_t lda,
                                 const double* B, int64_t ldb, double beta, double* C, int64_t ldc, void* ws,

@@ -29,7 +29,7 @@ PREC_TF32 = 1
 PREC_BF16 = 2
 PREC_BF16X3 = 3
 PREC_TF32X3 = 4
-PREC_BF16X5 = 5
+PREC_BF16X6 = 5
 
 _c_i64 = ctypes.c_int64
 _c_vp = ctypes.c_void_p

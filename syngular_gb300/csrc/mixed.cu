@@ -600,7 +600,7 @@ __global__ void identity_cores_kernel(double* __restrict__ eye, const int* __res
 int mixed_round_chain(cudaStream_t st, int n, const double* const* X, const int64_t* xs, int64_t chi,
                       int precision, double* const* out, double* spectra, double* discarded, int* status,
                       Arena& ar) {
-  if (precision == SGT_PREC_BF16X5) return oz_round_chain(st, n, X, xs, chi, out, spectra, discarded, status, ar);
+  if (precision == SGT_PREC_BF16X6) return oz_round_chain(st, n, X, xs, chi, out, spectra, discarded, status, ar);
   SGT_REQUIRE(precision == SGT_PREC_TF32 || precision == SGT_PREC_TF32X3, SGT_ERR_INVALID,
               "round: precision %d has no Gram form", precision);
   std::vector<int64_t> w4(4 * (size_t)n);
@@ -642,7 +642,7 @@ static int mpo_mps_round_impl(cudaStream_t st, int n, const double* const* W, co
   if (precision == SGT_PREC_TF32 || precision == SGT_PREC_TF32X3)
     return mixed_round_impl(st, n, W, ws4, X, xs, chi, precision == SGT_PREC_TF32 ? 1 : 3, out, spectra,
                             discarded, status, ar);
-  if (precision == SGT_PREC_BF16X5)
+  if (precision == SGT_PREC_BF16X6)
     return oz_round_impl(st, n, W, ws4, X, xs, chi, out, spectra, discarded, status, ar);
   SGT_REQUIRE(precision == SGT_PREC_F64, SGT_ERR_INVALID, "mpo_mps_round: unsupported precision %d",
               precision);

@@ -1,5 +1,5 @@
 // The accurate mixed-precision form of the metric operation
-// (sgt_mpo_mps_round / sgt_svd_round with SGT_PREC_BF16X5).
+// (sgt_mpo_mps_round / sgt_svd_round with SGT_PREC_BF16X6).
 //
 // Same algebra as the Gram form of mixed.cu (no Householder QR on the R x R
 // product unfoldings):

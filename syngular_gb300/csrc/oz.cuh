@@ -9,7 +9,7 @@
 
 namespace sgt {
 
-constexpr int OZ_SLICES = 5;   // bf16 slices per operand row (6 + 4 * 7 = 34 bits, 2^-35 truncation)
+constexpr int OZ_SLICES = 6;   // bf16 slices per operand row (6 + 5 * 7 = 41 bits, 2^-42 truncation)
 constexpr int OZ_KC = 1024;    // longest K range accumulated exactly by one CTA
 
 // ---------------------------------------------------------------------------
@@ -63,7 +63,7 @@ struct OzMat {
 };
 
 // x (a pair, scaled so that |x| < 64) -> OZ_SLICES integers m_s with
-// x = sum_s m_s 2^(-7 s) + r, |m_s| <= 64, |r| <= 2^-29; slice s stored as the
+// x = sum_s m_s 2^(-7 s) + r, |m_s| <= 64, |r| <= 2^-36; slice s stored as the
 // bf16 value m_s 2^(-7 s) (exact).
 __device__ __forceinline__ void slice_store(float h, float l, __nv_bfloat16* out, int64_t sstride, int64_t idx) {
   float m = rintf(h);

@@ -10,29 +10,33 @@
 // Slicing (Ozaki's error-free splitting, with a fixed slice width): row i of
 // an operand is scaled by 2^(6 - e_i), e_i the binary exponent of the row's
 // largest entry (|x| < 2^e_i), and cut by round-to-nearest into
-//   x 2^(6 - e_i) = sum_{s<5} m_s 2^(-7 s) + r,   m_s integers, |m_s| <= 64,
-//   |r| <= 2^-29 (so x is kept to 2^-35 of the row's largest entry).
+//   x 2^(6 - e_i) = sum_{s<6} m_s 2^(-7 s) + r,   m_s integers, |m_s| <= 64,
+//   |r| <= 2^-36 (so x is kept to 2^-42 of the row's largest entry).
 // Slice s is stored in bf16 as m_s 2^(-7 s), which bf16 holds exactly.
 //
 // The product of slices s of A and t of B is an integer times 2^(-7(s+t)),
-// at most 2^12 in magnitude.  The pairs with s + t <= 4 (15 of them)
-// accumulate in four TMEM accumulators by level c = min(s + t, 3).  Over a K
-// range of at most OZ_KC = 1024, the level-c accumulator (c <= 2) is an
-// integer times 2^(-7c) of magnitude below (c + 1) * 1024 * 2^12 <= 2^23.6,
+// at most 2^12 in magnitude.  The pairs with s + t <= 5 (21 of them)
+// accumulate in five TMEM accumulators by level c = min(s + t, 4).  Over a K
+// range of at most OZ_KC = 1024, the level-c accumulator (c <= 3) is an
+// integer times 2^(-7c) of magnitude at most (c + 1) * 1024 * 2^12 <= 2^24,
 // so its FP32 accumulation is exact whatever the tensor core's rounding;
-// level 3 gathers the s + t = 3, 4 terms, which carry 2^-21 of the leading
-// level's weight, so its FP32 rounding stays near 2^-37 of the result's scale.
+// level 4 gathers the s + t = 4, 5 terms, which carry 2^-28 of the leading
+// level's weight, so its FP32 rounding stays near 2^-40 of the result's scale
+// (one shared accumulator for levels 3..5 measured 2^-33: its rounding, not
+// the slicing, limited the accuracy).
 // The epilogue adds the four levels in pair arithmetic and scales by
 // 2^(e_i + f_j - 12).  Longer K is split over CTAs (grid z) whose pair
 // partials a second kernel adds in a fixed order (deterministic).
 //
-// Accuracy: about 2^-35 of sum_k |a_ik| |b_jk| (of row-max times column-max
-// scale), against 2^-22 for split TF32 and 2^-52 for FP64.
+// Accuracy: about 2^-40 of the row-max times column-max scale per product
+// term (level 4's rounding, the dropped s + t = 6 terms and the slice
+// remainders), against 2^-22 for split TF32 and 2^-52 for FP64.
 //
-// CTA: 6 warps.  Warp 0 lane 0 issues the TMA loads (a 3D map per operand,
-// the slice index is the third coordinate) into a 2-stage ring; warp 1 owns
-// TMEM (4 x 128 columns) and lane 0 issues the MMAs; warps 2..5 drain the four
-// accumulators once at the end (warp w reads TMEM lanes 32 (w % 4)..+31).
+// CTA: 128 x 96 output tile, 6 warps.  Warp 0 lane 0 issues the TMA loads (a
+// 3D map per operand, the slice index is the third coordinate) into a 2-stage
+// ring; warp 1 owns TMEM (5 x 96 columns) and lane 0 issues the MMAs; warps
+// 2..5 drain the five accumulators once at the end (warp w reads TMEM lanes
+// 32 (w % 4)..+31).
 // Every mbarrier wait has an iteration limit: on expiry the kernel records
 // an error, skips the remaining work, frees TMEM and returns.
 #include <cuda.h>
@@ -50,15 +54,17 @@ namespace sgt {
 namespace {
 
 constexpr int OZ_BM = 128;
-constexpr int OZ_BN = 128;
+constexpr int OZ_BN = 96;  // five accumulators of 96 columns fill 480 of TMEM's 512
 constexpr int OZ_BK = 32;  // bf16 elements per stage along K = 64 bytes = one 64B-swizzle row
 constexpr int OZ_STAGES = 2;
-constexpr int OZ_LEVELS = 4;
+constexpr int OZ_LEVELS = 5;
 constexpr int OZ_EPI_WARPS = 4;
 constexpr int OZ_THREADS = 64 + 32 * OZ_EPI_WARPS;
-constexpr int OZ_TMEM_COLS = OZ_LEVELS * OZ_BN;  // 512: the whole TMEM of the SM
-constexpr int OZ_TILE_BYTES = OZ_BM * OZ_BK * 2;  // 8 KB per slice tile (A and B tiles alike)
-constexpr int OZ_STAGE_BYTES = 2 * OZ_SLICES * OZ_TILE_BYTES;
+constexpr int OZ_TMEM_COLS = 512;  // allocation (a power of two): the whole TMEM of the SM
+constexpr int OZ_TILE_A = OZ_BM * OZ_BK * 2;  // 8 KB per A slice tile
+constexpr int OZ_TILE_B = OZ_BN * OZ_BK * 2;  // 6 KB per B slice tile
+constexpr int OZ_STAGE_BYTES = OZ_SLICES * (OZ_TILE_A + OZ_TILE_B);
+static_assert(OZ_LEVELS * OZ_BN <= OZ_TMEM_COLS, "accumulators exceed TMEM");
 constexpr uint32_t OZ_WAIT_LIMIT = 1u << 24;
 
 __device__ __forceinline__ uint32_t smem_u32(const void* p) {
@@ -213,10 +219,10 @@ __global__ void __launch_bounds__(OZ_THREADS, 1)
   const uint32_t tmem = *tmem_slot;
 
   auto tileA = [&](int stage, int s) -> unsigned char* {
-    return ring + (size_t)stage * OZ_STAGE_BYTES + (size_t)s * OZ_TILE_BYTES;
+    return ring + (size_t)stage * OZ_STAGE_BYTES + (size_t)s * OZ_TILE_A;
   };
   auto tileB = [&](int stage, int s) -> unsigned char* {
-    return ring + (size_t)stage * OZ_STAGE_BYTES + (size_t)(OZ_SLICES + s) * OZ_TILE_BYTES;
+    return ring + (size_t)stage * OZ_STAGE_BYTES + (size_t)OZ_SLICES * OZ_TILE_A + (size_t)s * OZ_TILE_B;
   };
 
   if (warp == 0) {
@@ -242,7 +248,7 @@ __global__ void __launch_bounds__(OZ_THREADS, 1)
     __syncwarp();
   } else if (warp == 1) {
     if (lane == 0) {
-      // ---- MMA issuer: the 15 slice pairs of every 16-wide K step ----
+      // ---- MMA issuer: the 21 slice pairs of every 16-wide K step ----
       constexpr uint32_t idesc = idesc_bf16(OZ_BM, OZ_BN);
       bool ok = true;
       for (int kt = 0; kt < KT; ++kt) {
@@ -257,7 +263,7 @@ __global__ void __launch_bounds__(OZ_THREADS, 1)
 #pragma unroll
         for (int kk = 0; kk < OZ_BK / 16; ++kk) {  // bf16 MMA consumes K = 16 (32 bytes)
           const uint32_t off = kk * 32;
-          // small terms first within each accumulator (level 3 holds s + t = 3, 4)
+          // small terms first within each accumulator (level 3 holds s + t = 3, 4, 5)
 #pragma unroll
           for (int lv = OZ_SLICES - 1; lv >= 0; --lv) {
 #pragma unroll
@@ -298,27 +304,29 @@ __global__ void __launch_bounds__(OZ_THREADS, 1)
     float* clo = args.Clo + (int64_t)blockIdx.z * args.pstride;
 #pragma unroll 1
     for (int c0 = 0; c0 < OZ_BN; c0 += 32) {
-      float v0[32], v1[32], v2[32], v3[32];
+      float v0[32], v1[32], v2[32], v3[32], v4[32];
       const uint32_t ta = tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)c0;
       if (ok) {
         tmem_ld32(ta, v0);
         tmem_ld32(ta + OZ_BN, v1);
         tmem_ld32(ta + 2 * OZ_BN, v2);
         tmem_ld32(ta + 3 * OZ_BN, v3);
+        tmem_ld32(ta + 4 * OZ_BN, v4);
       } else {
 #pragma unroll
-        for (int i = 0; i < 32; ++i) v0[i] = v1[i] = v2[i] = v3[i] = 0.f;
+        for (int i = 0; i < 32; ++i) v0[i] = v1[i] = v2[i] = v3[i] = v4[i] = 0.f;
       }
       if (!ok || *(volatile int*)&s_fail || row >= args.M) continue;
 #pragma unroll
       for (int i = 0; i < 32; ++i) {
         const int col = n0 + c0 + i;
         if (col >= args.N) continue;
-        // exact: v0 + v1 (integers on grids 1 and 2^-7 below 2^24), then v2, v3
+        // exact: v0 + v1 (integers on grids 1 and 2^-7 up to 2^24), then v2, v3, v4
         float h = v0[i], l = 0.f;
         pair_add(h, l, v1[i]);
         pair_add(h, l, v2[i]);
-        l += v3[i];
+        pair_add(h, l, v3[i]);
+        l += v4[i];
         const float hs = h + l;
         l = l - (hs - h);
         h = hs;
@@ -437,14 +445,14 @@ int get_enc() {
 }
 
 // rows x K bf16 slices (row stride ld, slice stride sstride, in elements), box 32 x 128 x 1.
-int make_slice_map(CUtensorMap* map, const OzMat& m, int64_t rows, int64_t K) {
+int make_slice_map(CUtensorMap* map, const OzMat& m, int64_t rows, int64_t K, int box_rows) {
   SGT_REQUIRE((reinterpret_cast<uintptr_t>(m.s) & 15) == 0, SGT_ERR_INVALID, "oz_gemm: slices not 16-byte aligned");
   SGT_REQUIRE((m.ld * 2) % 16 == 0 && (m.sstride * 2) % 16 == 0 && m.ld >= oz_ld(K), SGT_ERR_INVALID,
               "oz_gemm: row and slice strides must be multiples of 8 elements, rows padded to oz_ld(K)");
   // the padded width: slice rows hold zeros in [K, oz_ld(K)), so the last K-tile reads zeros
   cuuint64_t dims[3] = {(cuuint64_t)oz_ld(K), (cuuint64_t)rows, (cuuint64_t)OZ_SLICES};
   cuuint64_t strides[2] = {(cuuint64_t)(m.ld * 2), (cuuint64_t)(m.sstride * 2)};
-  cuuint32_t box[3] = {(cuuint32_t)OZ_BK, (cuuint32_t)OZ_BM, 1};
+  cuuint32_t box[3] = {(cuuint32_t)OZ_BK, (cuuint32_t)box_rows, 1};
   cuuint32_t estr[3] = {1, 1, 1};
   CUresult r = g_enc(map, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 3, const_cast<__nv_bfloat16*>(m.s), dims, strides, box,
                      estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_64B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
@@ -490,8 +498,8 @@ int oz_gemm(cudaStream_t st, int64_t M, int64_t N, int64_t K, float alpha, const
   SGT_REQUIRE(M < (1ll << 31) && N < (1ll << 31) && K < (1ll << 31), SGT_ERR_INVALID, "oz_gemm: too large");
   SGT_TRY(get_enc());
   CUtensorMap ma, mb;
-  SGT_TRY(make_slice_map(&ma, A, M, K));
-  SGT_TRY(make_slice_map(&mb, B, N, K));
+  SGT_TRY(make_slice_map(&ma, A, M, K, OZ_BM));
+  SGT_TRY(make_slice_map(&mb, B, N, K, OZ_BN));
   SGT_CUDA(func_attr_at_least((const void*)oz_gemm_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                               (int)oz_smem_bytes()));
   const int S = oz_splits(M, N, K, part ? part_floats : 0);

@@ -549,7 +549,7 @@ static int svd_round_impl(cudaStream_t st, int n, const double* const* cores, co
   auto s = shapes_of(n, shp);
   SGT_TRY(check_chain(n, s, "svd_round"));
   SGT_REQUIRE(chi >= 1, SGT_ERR_INVALID, "svd_round: chi must be >= 1");
-  if (precision == SGT_PREC_TF32 || precision == SGT_PREC_TF32X3 || precision == SGT_PREC_BF16X5)
+  if (precision == SGT_PREC_TF32 || precision == SGT_PREC_TF32X3 || precision == SGT_PREC_BF16X6)
     return mixed_round_chain(st, n, cores, shp, chi, precision, out, spectra, discarded, status, ar);
   SGT_REQUIRE(precision == SGT_PREC_F64, SGT_ERR_INVALID, "svd_round: unsupported precision %d", precision);
   SGT_REQUIRE(s[0].l == 1 && s[n - 1].r == 1, SGT_ERR_INVALID, "svd_round: boundary bonds must be 1");
