@@ -161,7 +161,10 @@ __global__ void product_slices_kernel(const float* __restrict__ Xh, const float*
 // for a tile of MD_TA values of a and TC values of c'.
 //   B: U [a][b][o][e'][c'] = sum_{e,j} T1[a][b][e][j][c'] W[e][j][o][e']
 //   C: T3[c'][e'][b'][a][i] = sum_{b,o} W[b][i][o][b'] U[a][b][o][e'][c']
-// T1 / T3 are pair matrices (hi, lo); W is FP64 [b][i][o][b'].
+// T1 / T3 are pair matrices (hi, lo); W is FP64 [b][i][o][b'].  T1 comes from
+// step A as T1t[(j, c')][(a, b, e)] (c' outer, so that a tile of a values
+// reads contiguous runs of (b, e)).  This generic form serves the edge sites;
+// gram_mid_df_tiled below the middle ones.
 constexpr int MD_TA = 4;
 
 size_t mid_df_smem(int D, int d, int dout, int D2, int TC) {
@@ -192,7 +195,9 @@ __global__ void __launch_bounds__(256) gram_mid_df_kernel(const float* __restric
     const int a = a0 + at, c = c0 + t;
     float2 v = make_float2(0.f, 0.f);
     if (a < chi && c < chi2) {
-      const int64_t g = ((int64_t)a * bej + r) * chi2 + c;
+      // r = (b D + e) d + j
+      const int b = r / (D * d), e = (r / d) % D, j = r % d;
+      const int64_t g = ((int64_t)j * chi2 + c) * ((int64_t)chi * D * D) + ((int64_t)a * D + b) * D + e;
       v = make_float2(T1h[g], T1l[g]);
     }
     sT[i] = v;
@@ -241,6 +246,121 @@ __global__ void __launch_bounds__(256) gram_mid_df_kernel(const float* __restric
     const int64_t idx = (((int64_t)c * D2 + e2) * D2 + b2) * ((int64_t)chi * d) + (int64_t)a * d + i;
     T3h[idx] = h;
     T3l[idx] = l;
+  }
+}
+
+
+// Middle sites (D2 = D, dout = d), compile-time sizes: one block per (8 values
+// of a, one c').  Step B: a thread owns one (a, b) row and 16 of the 32
+// (o, e') columns, step C one (a, e') row and 16 of the (i, b') columns, so
+// every shared-memory value feeds 16 independent pair multiply-adds.  The W
+// pairs sit in shared memory in both column orders; rows of T and U are
+// padded by one pair against bank conflicts; the T3 tile is staged in shared
+// memory and stored as runs of (a, i).
+constexpr int MT_TA = 8;
+
+template <int D, int d>
+constexpr size_t mid_tiled_smem() {
+  return sizeof(float2) * (2 * (size_t)(D * d) * (d * D) + 2 * (size_t)MT_TA * D * (D * d + 1));
+}
+
+template <int D, int d>
+__global__ void __launch_bounds__(256, 2) gram_mid_df_tiled(const float* __restrict__ T1h, const float* __restrict__ T1l,
+                                                           const double* __restrict__ W, float* __restrict__ T3h,
+                                                           float* __restrict__ T3l, int chi, int chi2) {
+  constexpr int K = D * d;       // (e, j) and (b, o) extents
+  constexpr int NB = d * D;      // (o, e') and (i, b') extents
+  constexpr int KP = K + 1;      // padded row of T / U
+  constexpr int HALF = NB / 2;   // columns per thread
+  extern __shared__ float2 mt_smem[];
+  float2* sWB = mt_smem;               // [(e, j)][(o, e')]
+  float2* sWC = sWB + K * NB;          // [(b, o)][(i, b')]
+  float2* sT = sWC + K * NB;           // [a][b][(e, j)] (padded), later the T3 stage
+  float2* sU = sT + MT_TA * D * KP;    // [a][e'][(b, o)] (padded)
+  const int a0 = blockIdx.x * MT_TA, c = blockIdx.y;
+  const int tid = threadIdx.x;
+  const int64_t RR = (int64_t)chi * D * D;
+  for (int idx = tid; idx < K * NB; idx += 256) {
+    // idx = ((b d + i) d + o) D + b2 in W's own order
+    const int b2 = idx % D, o = (idx / D) % d, i = (idx / (D * d)) % d, b = idx / (D * d * d);
+    const double v = W[idx];
+    const float h = (float)v;
+    const float2 w = make_float2(h, (float)(v - (double)h));
+    sWB[idx] = w;                                   // [(b, i)][(o, b2)]
+    sWC[(b * d + o) * NB + i * D + b2] = w;         // [(b, o)][(i, b2)]
+  }
+  for (int idx = tid; idx < MT_TA * d * D * D; idx += 256) {
+    const int be = idx % (D * D), j = (idx / (D * D)) % d, at = idx / (D * D * d);
+    const int b = be / D, e = be % D, a = a0 + at;
+    float2 v = make_float2(0.f, 0.f);
+    if (a < chi) {
+      const int64_t g = ((int64_t)j * chi2 + c) * RR + (int64_t)a * D * D + be;
+      v = make_float2(T1h[g], T1l[g]);
+    }
+    sT[(at * D + b) * KP + e * d + j] = v;
+  }
+  __syncthreads();
+  // ---- B: U[a][e'][(b, o)] = sum_(e,j) T[a][b][(e,j)] W[(e,j)][(o,e')] ----
+  for (int task = tid; task < MT_TA * D * 2; task += 256) {
+    const int half = task & 1, b = (task >> 1) % D, at = (task >> 1) / D;
+    float h[HALF], l[HALF];
+#pragma unroll
+    for (int n = 0; n < HALF; ++n) h[n] = l[n] = 0.f;
+    const float2* trow = sT + (at * D + b) * KP;
+    const float2* wcol = sWB + half * HALF;
+#pragma unroll 4
+    for (int k = 0; k < K; ++k) {
+      const float2 t = trow[k];
+#pragma unroll
+      for (int n = 0; n < HALF; ++n) {
+        const float2 w = wcol[k * NB + n];
+        df_fma(h[n], l[n], t.x, t.y, w.x, w.y);
+      }
+    }
+#pragma unroll
+    for (int n = 0; n < HALF; ++n) {
+      const int col = half * HALF + n, o = col / D, e2 = col % D;
+      df_norm(h[n], l[n]);
+      sU[(at * D + e2) * KP + b * d + o] = make_float2(h[n], l[n]);
+    }
+  }
+  __syncthreads();
+  // ---- C: stage[e'][b'][a][i] = sum_(b,o) U[a][e'][(b,o)] W[(b,o)][(i,b')] ----
+  float2* stage = sT;
+  for (int task = tid; task < MT_TA * D * 2; task += 256) {
+    const int half = task & 1, e2 = (task >> 1) % D, at = (task >> 1) / D;
+    float h[HALF], l[HALF];
+#pragma unroll
+    for (int n = 0; n < HALF; ++n) h[n] = l[n] = 0.f;
+    const float2* urow = sU + (at * D + e2) * KP;
+    const float2* wcol = sWC + half * HALF;
+#pragma unroll 4
+    for (int k = 0; k < K; ++k) {
+      const float2 u = urow[k];
+#pragma unroll
+      for (int n = 0; n < HALF; ++n) {
+        const float2 w = wcol[k * NB + n];
+        df_fma(h[n], l[n], u.x, u.y, w.x, w.y);
+      }
+    }
+#pragma unroll
+    for (int n = 0; n < HALF; ++n) {
+      const int col = half * HALF + n, i = col / D, b2 = col % D;
+      df_norm(h[n], l[n]);
+      stage[((e2 * D + b2) * MT_TA + at) * d + i] = make_float2(h[n], l[n]);
+    }
+  }
+  __syncthreads();
+  // ---- store: T3[c][e'][b'][(a, i)], runs of MT_TA * d values ----
+  constexpr int RUN = MT_TA * d;
+  for (int idx = tid; idx < D * D * RUN; idx += 256) {
+    const int r = idx % RUN, eb = idx / RUN;
+    const int a = a0 + r / d;
+    if (a >= chi) continue;
+    const int64_t g = ((int64_t)c * D * D + eb) * ((int64_t)chi * d) + (int64_t)a0 * d + r;
+    const float2 v = stage[idx];
+    T3h[g] = v.x;
+    T3l[g] = v.y;
   }
 }
 
@@ -638,17 +758,39 @@ int oz_round_impl(cudaStream_t st, int n, const double* const* W, const int64_t*
     SGT_TRY(oz_split_f64(st, X[k], 1, chi2, chi2, chi_k * d, X2.s, X2.e, 1));
     X2.rows = chi2;
     X2.cols = chi_k * d;
-    // A: T1 ((chi D D) x (d chi2)) = G_k (rows of chi) Xt^T
-    SGT_TRY(gemm(chi_k * D * D, d * chi2, chi_k, 1.f, Gchi.mat(), Xt.mat(), 0.f, T1, d * chi2));
+    // A: T1t ((d chi2) x (chi D D)) = Xt G_k^T, G_k taken as rows of chi
+    SGT_TRY(gemm(d * chi2, chi_k * D * D, chi_k, 1.f, Xt.mat(), Gchi.mat(), 0.f, T1, chi_k * D * D));
     // B + C in pair arithmetic
-    const int TC = mid_tc(D, d, dout, D2);
-    const size_t smem = mid_df_smem((int)D, (int)d, (int)dout, (int)D2, TC);
-    SGT_CUDA(func_attr_at_least((const void*)gram_mid_df_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                (int)smem));
-    dim3 g((unsigned)cdiv(chi_k, MD_TA), (unsigned)cdiv(chi2, TC));
-    gram_mid_df_kernel<<<g, 256, smem, st>>>(T1.h, T1.l, W[k], T3.h, T3.l, (int)chi_k, (int)D, (int)d, (int)dout,
-                                             (int)D2, (int)chi2, TC);
-    SGT_LAUNCHED();
+    bool tiled_done = false;
+    if (D2 == D && dout == d && chi2 <= 65535) {
+      auto run = [&](auto kern, size_t smem) -> int {
+        SGT_CUDA(func_attr_at_least((const void*)kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+        dim3 gt((unsigned)cdiv(chi_k, MT_TA), (unsigned)chi2);
+        kern<<<gt, 256, smem, st>>>(T1.h, T1.l, W[k], T3.h, T3.l, (int)chi_k, (int)chi2);
+        SGT_LAUNCHED();
+        tiled_done = true;
+        return SGT_OK;
+      };
+      if (D == 16 && d == 2) SGT_TRY(run(gram_mid_df_tiled<16, 2>, mid_tiled_smem<16, 2>()));
+      else if (D == 16 && d == 4) SGT_TRY(run(gram_mid_df_tiled<16, 4>, mid_tiled_smem<16, 4>()));
+      else if (D == 8 && d == 2) SGT_TRY(run(gram_mid_df_tiled<8, 2>, mid_tiled_smem<8, 2>()));
+      else if (D == 8 && d == 3) SGT_TRY(run(gram_mid_df_tiled<8, 3>, mid_tiled_smem<8, 3>()));
+      else if (D == 8 && d == 4) SGT_TRY(run(gram_mid_df_tiled<8, 4>, mid_tiled_smem<8, 4>()));
+      else if (D == 16 && d == 3) SGT_TRY(run(gram_mid_df_tiled<16, 3>, mid_tiled_smem<16, 3>()));
+      else if (D == 4 && d == 2) SGT_TRY(run(gram_mid_df_tiled<4, 2>, mid_tiled_smem<4, 2>()));
+      else if (D == 4 && d == 3) SGT_TRY(run(gram_mid_df_tiled<4, 3>, mid_tiled_smem<4, 3>()));
+      else if (D == 4 && d == 4) SGT_TRY(run(gram_mid_df_tiled<4, 4>, mid_tiled_smem<4, 4>()));
+    }
+    if (!tiled_done) {
+      const int TC = mid_tc(D, d, dout, D2);
+      const size_t smem = mid_df_smem((int)D, (int)d, (int)dout, (int)D2, TC);
+      SGT_CUDA(func_attr_at_least((const void*)gram_mid_df_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                  (int)smem));
+      dim3 g((unsigned)cdiv(chi_k, MD_TA), (unsigned)cdiv(chi2, TC));
+      gram_mid_df_kernel<<<g, 256, smem, st>>>(T1.h, T1.l, W[k], T3.h, T3.l, (int)chi_k, (int)D, (int)d, (int)dout,
+                                               (int)D2, (int)chi2, TC);
+      SGT_LAUNCHED();
+    }
     // D: G_{k+1} ((chi2 D2 D2) x chi2) = T3 X2^T
     SGT_TRY(split_pair(st, T3, chi_k * d, T3s, chi2 * D2 * D2, chi_k * d));
     SGT_TRY(gemm(chi2 * D2 * D2, chi2, chi_k * d, 1.f, T3s.mat(), X2.mat(), 0.f, G, chi2));
