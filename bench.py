@@ -232,36 +232,122 @@ def cpu_site_sample(rng_seed=7):
     return t1 - t0
 
 
+def cpu_info():
+    """CPU model, core count and the BLAS build numpy uses (printed with every
+    CPU figure)."""
+    import numpy as np
+
+    model = None
+    try:
+        with open("/proc/cpuinfo") as f:
+            for ln in f:
+                key = ln.split(":")[0].strip().lower()
+                if key in ("model name", "cpu part", "hardware") and model is None:
+                    model = ln.split(":", 1)[1].strip()
+    except OSError:
+        pass
+    try:
+        out = subprocess.run(["lscpu"], capture_output=True, text=True, timeout=10).stdout
+        for ln in out.splitlines():
+            if ln.lower().startswith("model name"):
+                model = ln.split(":", 1)[1].strip()
+    except (OSError, subprocess.SubprocessError):
+        pass
+    blas = None
+    try:
+        b = np.show_config(mode="dicts")["Build Dependencies"]["blas"]
+        blas = "%s %s (%s)" % (b.get("name"), b.get("version"), b.get("openblas configuration", ""))
+    except Exception:  # noqa: BLE001 - informational only
+        pass
+    return {"cpu_model": model, "cores": os.cpu_count(), "blas": blas, "numpy": np.__version__}
+
+
+_CPU_SWEEP = """
+import json, sys, time
+sys.path.insert(0, %r)
+import bench
+bench.N_SITES = %d
+from oracle import tt_fp64 as O
+X, W = bench.make_inputs()
+t0 = time.perf_counter()
+Z, ov, spectra, disc = O.sweep_fp64(W, X, bench.CHI)
+print(json.dumps({"seconds": time.perf_counter() - t0, "overlap": ov}))
+"""
+
+_CPU_SITE = """
+import json, sys
+sys.path.insert(0, %r)
+import bench
+print(json.dumps({"seconds": bench.cpu_site_sample()}))
+"""
+
+
+def _cpu_subprocess(code, threads):
+    """Run a CPU measurement in a fresh interpreter whose BLAS uses `threads`
+    threads (the thread count is fixed when numpy loads its BLAS)."""
+    env = dict(os.environ)
+    for var in ("OPENBLAS_NUM_THREADS", "OMP_NUM_THREADS", "MKL_NUM_THREADS"):
+        env[var] = str(threads)
+    r = subprocess.run([sys.executable, "-c", code], capture_output=True, text=True, env=env)
+    if r.returncode != 0:
+        raise RuntimeError("CPU measurement failed: %s" % r.stderr[-2000:])
+    return json.loads(r.stdout.strip().splitlines()[-1])
+
+
+def cpu_full_sweep(threads, sites=None):
+    """One whole sweep of the numpy FP64 port (the oracle: raw product, left QR
+    sweep, right-to-left SVDs, overlap) on the host cores; returns seconds."""
+    return _cpu_subprocess(_CPU_SWEEP % (ROOT, sites or N_SITES), threads)
+
+
 def cpu_baseline_measure():
+    """The numpy FP64 port on the host cores: one measured full sweep with all
+    cores, plus a 1-thread figure (one full-size middle site at one thread,
+    scaled to the sweep by per-site flops: a full 1-thread sweep takes ~40 min)."""
+    cores = os.cpu_count() or 1
+    full = cpu_full_sweep(cores)
+    t_sweep = full["seconds"]
     fl, mid = site_flops_model()
-    t_site = cpu_site_sample()
-    t_sweep = t_site * sum(fl) / fl[mid]
-    return {"value": 1.0 / t_sweep, "unit": "sweeps/s", "cores": os.cpu_count(), "kind": "port",
-            "sample": "one full-size middle site of the numpy FP64 sweep (%.2f s), scaled to 64 sites by "
-                      "per-site flops (x%.1f)" % (t_site, sum(fl) / fl[mid]),
-            "seconds_per_sweep": t_sweep}
+    scale = sum(fl) / fl[mid]
+    one = _cpu_subprocess(_CPU_SITE % ROOT, 1)["seconds"] * scale
+    info = cpu_info()
+    return {"value": 1.0 / t_sweep, "unit": "sweeps/s", "cores": cores, "kind": "port",
+            "sample": "one whole %d-site sweep of the numpy FP64 port (measured, %.1f s, all %d host threads)"
+                      % (N_SITES, t_sweep, cores),
+            "seconds_per_sweep": t_sweep, "overlap": full["overlap"],
+            "one_thread": {"value": 1.0 / one, "unit": "sweeps/s", "cores": 1,
+                           "sample": "one full-size middle site at 1 thread, scaled to the sweep by per-site "
+                                     "flops (x%.1f)" % scale, "seconds_per_sweep": one},
+            **info}
 
 
 def run_reference(args, rank, world):
+    """The reference arm: the numpy FP64 port of the sweep (the reference's own
+    MPS / MPO code cannot run this workload), whole sweeps on all host cores.
+    A sweep takes minutes, so the arm runs one untimed sweep of a 3-site chain
+    of the same core shapes and then exactly one timed full sweep, and reports
+    the steps it ran (1)."""
     if rank != 0:
         return 0
-    import numpy as np  # noqa: F401
-
-    fl, mid = site_flops_model()
-    scale = sum(fl) / fl[mid]
-    for _ in range(args.warmup):
-        cpu_site_sample()
-    ts = [cpu_site_sample() for _ in range(args.steps)]
-    t_sweep = statistics.mean(ts) * scale
+    cores = os.cpu_count() or 1
+    cpu_full_sweep(cores, sites=3)  # warm-up (BLAS threads, page-in)
+    full = cpu_full_sweep(cores)
+    t_sweep = full["seconds"]
     v = 1.0 / t_sweep
+    info = cpu_info()
     line = {
         "impl": "reference", "metric": METRIC, "value": v, "unit": "sweeps/s", "n_gpus": world,
-        "steps": args.steps, "warmup": args.warmup, "ms_per_step": t_sweep * 1e3, "higher_is_better": True,
+        "steps": 1, "warmup": 1, "ms_per_step": t_sweep * 1e3, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded, config-2 shapes)",
-        "config": {"workload": workload_name(), "cpu": "numpy FP64 port of the sweep (Householder QR + LAPACK SVD)"},
-        "cpu_baseline": {"value": v, "unit": "sweeps/s", "cores": os.cpu_count(), "kind": "port",
-                         "sample": "each step = one full-size middle site, scaled to 64 sites by flops (x%.1f)" % scale},
+        "config": {"workload": workload_name(), "cpu": "numpy FP64 port of the sweep (Householder QR + LAPACK SVD)",
+                   "steps_note": "one whole sweep timed (about %.0f s); the --steps / --warmup values asked "
+                                 "for (%d / %d) are not run: each would be a further whole sweep"
+                                 % (t_sweep, args.steps, args.warmup)},
+        "cpu_baseline": {"value": v, "unit": "sweeps/s", "cores": cores, "kind": "port",
+                         "sample": "one whole %d-site sweep (measured), after a 3-site warm-up sweep" % N_SITES,
+                         **info},
         "e2e": {"value": v, "unit": "sweeps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "overlap": full["overlap"],
     }
     print(json.dumps(line))
     return 0
@@ -348,18 +434,29 @@ def run_gpu(args, rank, world, local_rank):
     value = world * args.steps / (ms_total / 1e3)
     ov_fast = _ops.decode_overlap(res.cpu().tolist())
 
-    # ---- e2e: host buffers in, scalar out ----
-    torch.cuda.synchronize()
-    barrier()
-    t0 = time.perf_counter()
-    for _ in range(args.steps):
-        Xe = [c.to(dev, non_blocking=True) for c in Xp]
-        We = [c.to(dev, non_blocking=True) for c in Wp]
-        Z, res, status = step(Xe, We)
-        _ = res.cpu().tolist()
-    torch.cuda.synchronize()
-    barrier()
-    e2e_s = max_over_ranks(time.perf_counter() - t0)
+    # ---- e2e: host buffers in, scalar out, through the drop-in API ----
+    # (W @ X) >> chi with the raw product left unformed (AUTO_ROUND off) and the
+    # TT-SVD rounding in the benchmark's precision, then X | Z back on the host
+    from syngular_gb300.tensor import MatrixProductOperator, MatrixProductState
+
+    saved = (MatrixProductOperator.AUTO_ROUND, MatrixProductOperator.PRECISION, MatrixProductState.ROUNDING)
+    MatrixProductOperator.AUTO_ROUND = False
+    MatrixProductOperator.PRECISION = args.precision
+    MatrixProductState.ROUNDING = "svd"
+    try:
+        torch.cuda.synchronize()
+        barrier()
+        t0 = time.perf_counter()
+        for _ in range(args.steps):
+            Xm = MatrixProductState.from_sites([c.to(dev, non_blocking=True) for c in Xp])
+            Wm = MatrixProductOperator.from_sites([c.to(dev, non_blocking=True) for c in Wp])
+            Zm = (Wm @ Xm) >> CHI
+            ov_api = float(Xm | Zm)
+        torch.cuda.synchronize()
+        barrier()
+        e2e_s = max_over_ranks(time.perf_counter() - t0)
+    finally:
+        MatrixProductOperator.AUTO_ROUND, MatrixProductOperator.PRECISION, MatrixProductState.ROUNDING = saved
     e2e_value = world * args.steps / e2e_s
 
     out = {
@@ -369,7 +466,9 @@ def run_gpu(args, rank, world, local_rank):
         "data": "synthetic (seeded N(0,1)/sqrt(chi*d) cores)",
         "config": {"workload": workload_name(), "form": args.precision, "l2": "inputs larger than L2 (split product cores %.1f GB)" % (N_SITES * 4096 * 2 * 4096 * 8 / 1e9),
                    "parallelism": "replicas" if world > 1 else "single GPU"},
-        "e2e": {"value": e2e_value, "unit": "sweeps/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": 16},
+        "e2e": {"value": e2e_value, "unit": "sweeps/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": 16,
+                "api": "(MatrixProductOperator @ MatrixProductState) >> chi with AUTO_ROUND=False, ROUNDING='svd', "
+                       "PRECISION='%s'; then X | Z" % args.precision, "overlap": ov_api},
         "gpu_launches": int(launches),
         "clocks": clk,
         "overlap": ov_fast,
@@ -428,18 +527,23 @@ def run_gpu(args, rank, world, local_rank):
         Ws = [Wd[0], Wd[1], Wd[-1]]
         _ops.mpo_mps_round(Ws, Xs, CHI, L.PREC_F64)
         torch.cuda.synchronize()
-        p0, p1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        p0.record()
-        Zp, spec_p, counts_p, disc_p, status_p = _ops.mpo_mps_round(Wd, Xd, CHI, L.PREC_F64)
-        resp = _ops.overlap_device(Xd, Zp)
-        p1.record()
-        torch.cuda.synchronize()
-        plain_ms = max_over_ranks(p0.elapsed_time(p1))
+        plain_runs = []
+        for _ in range(max(1, args.plain_steps)):
+            p0, p1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            p0.record()
+            Zp, spec_p, counts_p, disc_p, status_p = _ops.mpo_mps_round(Wd, Xd, CHI, L.PREC_F64)
+            resp = _ops.overlap_device(Xd, Zp)
+            p1.record()
+            torch.cuda.synchronize()
+            plain_runs.append(max_over_ranks(p0.elapsed_time(p1)))
+        plain_ms = statistics.mean(plain_runs)
         ov_plain = _ops.decode_overlap(resp.cpu().tolist())
         nx = math.sqrt(_ops.overlap(Xd, Xd))
         nz = math.sqrt(abs(_ops.overlap(Zp, Zp)))
-        out["plain_fp64"] = {"sweeps_per_s": world * 1e3 / plain_ms, "ms_per_sweep": plain_ms, "steps": 1,
-                             "warmup": 1, "status": int(status_p.item())}
+        out["plain_fp64"] = {"sweeps_per_s": world * 1e3 / plain_ms, "ms_per_sweep": plain_ms,
+                             "steps": len(plain_runs), "ms_each": plain_runs,
+                             "spread_rel": (max(plain_runs) - min(plain_runs)) / plain_ms,
+                             "warmup": "one 3-site chain of the same core shapes", "status": int(status_p.item())}
         out["speedup_vs_plain_fp64"] = value / (world * 1e3 / plain_ms)
         # 1 - |<Z|Z_fp64>| / (|Z| |Z_fp64|): how far the rounded state of the
         # fast form is from the FP64 one (gauge-invariant)
@@ -698,6 +802,7 @@ def main():
     ap.add_argument("--impl", default="syngular", choices=["syngular", "reference"])
     ap.add_argument("--precision", default="bf16x6", choices=sorted(PRECISIONS))
     ap.add_argument("--no-plain", action="store_true")
+    ap.add_argument("--plain-steps", type=int, default=2, help="timed sweeps of the plain FP64 form (~62 s each)")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--workload", default="config2", choices=["config2", "batched", "serving", "config4"])
     ap.add_argument("--instances", type=int, default=512)

@@ -25,7 +25,7 @@ import torch
 
 from .. import _lib as L
 from . import _ops
-from .matrix_product_state import MatrixProductState, _is_dev
+from .matrix_product_state import MatrixProductState, _is_dev, precision_code
 
 
 class MatrixProductOperator:
@@ -34,8 +34,14 @@ class MatrixProductOperator:
     MATMUL_MODE = "standard"
     # "qr": reference QR-column truncation; "svd": TT-SVD rounding
     ROUNDING = "qr"
-    # False: `@` and `+` return the raw (unrounded) product / sum
+    # False: `@` and `+` return the raw (unrounded) product / sum; an MPO x MPS
+    # product is then formed lazily, and `>>` on it with ROUNDING = "svd" runs
+    # the fused product + TT-SVD round in PRECISION without storing the product
     AUTO_ROUND = True
+    # Arithmetic of the "svd" rounding of `@` / `+` / `>>`: "f64" (plain FP64),
+    # "bf16x6" (FP64-class sliced bf16 tensor-core products, FP32-pair
+    # elementwise work, refined FP32 Jacobi), "tf32x3" / "tf32" (split / plain TF32)
+    PRECISION = "f64"
 
     def __init__(self, tensor=None, bond_shape: Union[Tuple, List] = (), verbose=0) -> None:
         """mpo:25-64."""
@@ -88,7 +94,14 @@ class MatrixProductOperator:
         auto = type(self).AUTO_ROUND
         if isinstance(mp, MatrixProductState):
             if MatrixProductOperator.MATMUL_MODE == "standard":
-                s = MatrixProductState.from_sites(_ops.contract_mpo_mps(self.sites, mp.sites))
+                s = MatrixProductState.lazy_product(self.sites, mp.sites, type(self).PRECISION)
+                if auto and type(self).ROUNDING == "svd":
+                    # fused product + round (the rounding this operator class asks for)
+                    if min_bond >= min(s.bond_shape):
+                        return s
+                    out, _sp, _c, _d, _st = _ops.mpo_mps_round(self.sites, mp.sites, min_bond,
+                                                               precision_code(type(self).PRECISION))
+                    return MatrixProductState.from_sites(out)
                 return s >> min_bond if auto else s
             return None
         if isinstance(mp, MatrixProductOperator):
@@ -232,7 +245,7 @@ class MatrixProductOperator:
     def _round(self, cores, dim):
         flat = [c.reshape(c.shape[0], c.shape[1] * c.shape[2], c.shape[3]) for c in cores]
         if type(self).ROUNDING == "svd":
-            out, _spec, _cnt, _disc, _st = _ops.svd_round(flat, dim)
+            out, _spec, _cnt, _disc, _st = _ops.svd_round(flat, dim, precision_code(type(self).PRECISION))
         else:
             out = _ops.qr_truncate(flat, dim)
         return [o.reshape(o.shape[0], c.shape[1], c.shape[2], o.shape[2]) for o, c in zip(out, cores)]

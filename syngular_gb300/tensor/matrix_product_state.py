@@ -23,12 +23,27 @@ from .. import _lib as L
 from . import _ops
 
 
+PRECISIONS = {"f64": L.PREC_F64, "tf32": L.PREC_TF32, "tf32x3": L.PREC_TF32X3, "bf16x6": L.PREC_BF16X6}
+
+
+def precision_code(name: str) -> int:
+    """Library code of a precision policy name ("f64", "tf32", "tf32x3",
+    "bf16x6"; see include/syngular_gb300.h SGT_PREC_*)."""
+    try:
+        return PRECISIONS[name]
+    except KeyError:
+        raise ValueError("unknown precision %r (one of %s)" % (name, ", ".join(sorted(PRECISIONS)))) from None
+
+
 class MatrixProductState:
     """Matrix product state ``sum prod_k X_k[a_k, i_k, a_{k+1}]``."""
 
     # Rounding used by ``>>``: "qr" is the reference's QR-column truncation
     # (mps:432-468); "svd" the TT-SVD rounding to the same bond.
     ROUNDING = "qr"
+    # Arithmetic of the "svd" rounding: "f64" (plain FP64), "bf16x6" (FP64-class
+    # sliced bf16 tensor-core products), "tf32x3" / "tf32" (split / plain TF32).
+    PRECISION = "f64"
 
     def __init__(self, tensor=None, bond_shape: Union[Tuple, List] = (), verbose=0) -> None:
         """mps:30-61."""
@@ -57,6 +72,42 @@ class MatrixProductState:
                 self.shape = [(1, self.tensor_shape[0], 1)]
         self.verbose = verbose
         self.decomposed = False
+
+    # A raw MPO x MPS product (``W @ X`` with AUTO_ROUND off) keeps its two
+    # factors and forms its cores only when they are read: ``>>`` with the
+    # "svd" rounding sends the factors to the fused product-and-round call
+    # instead, which never stores the product (17 GB in FP64 at chi=256, D=16,
+    # 64 sites).
+    _lazy = None
+    _sites = None
+
+    @property
+    def sites(self):
+        if self._sites is None and self._lazy is not None:
+            W, X, _prec = self._lazy
+            self._sites = _ops.contract_mpo_mps(W, X)
+        return self._sites
+
+    @sites.setter
+    def sites(self, value):
+        self._sites = value
+
+    @staticmethod
+    def lazy_product(W_sites, X_sites, precision: str):
+        """The raw product ``W @ X`` as a state whose cores are formed on first
+        read (shapes and bonds as the product's: fused bond a*b)."""
+        mp = MatrixProductState()
+        mp._lazy = (list(W_sites), list(X_sites), precision)
+        mp.sites_number = len(X_sites)
+        mp.decomposed = True
+        mp.orthonormalized = None
+        mp.real_parameters_number = None
+        mp.shape = [(int(x.shape[0]) * int(w.shape[0]), int(w.shape[2]), int(x.shape[2]) * int(w.shape[3]))
+                    for w, x in zip(W_sites, X_sites)]
+        mp.parameters_number = int(sum(a * b * c for a, b, c in mp.shape))
+        mp.input_shape = tuple(s[1] for s in mp.shape)
+        mp.bond_shape = tuple(s[2] for s in mp.shape[:-1])
+        return mp
 
     # ------------------------------------------------------------------ ops
     def __add__(self, mps):
@@ -187,6 +238,12 @@ class MatrixProductState:
             if mode == "right":
                 raise NotImplementedError("compress(mode='right', strict=False) is not provided")
             return None
+        if (self._lazy is not None and self._sites is None and mode == "left"
+                and type(self).ROUNDING == "svd"):
+            # fused raw product + TT-SVD round: the product is never stored
+            W, X, prec = self._lazy
+            out, _spec, _cnt, _disc, _st = _ops.mpo_mps_round(W, X, dim, precision_code(prec))
+            return MatrixProductState.from_sites(out)
         that = self.copy()
         if mode == "left":
             new = self._round(that.sites, dim)
@@ -197,7 +254,7 @@ class MatrixProductState:
 
     def _round(self, cores, dim):
         if type(self).ROUNDING == "svd":
-            out, _spec, _cnt, _disc, _st = _ops.svd_round(cores, dim)
+            out, _spec, _cnt, _disc, _st = _ops.svd_round(cores, dim, precision_code(type(self).PRECISION))
             return out
         return _ops.qr_truncate(cores, dim)
 

@@ -154,3 +154,15 @@ def test_bench_dominant_kernel_object(lib):
     assert 0 < d["frac"] < d["frac_of_cluster_sms"] < 1
     assert abs(d["share_of_step"] - 437.5 / 600.0) < 1e-12
     assert bench._eig_summary("RuntimeError: x", 600.0)["error"] == "RuntimeError: x"
+
+
+def test_bench_cpu_port_machinery():
+    """The CPU arm's machinery on a 3-site chain of the benchmark's core shapes:
+    a whole sweep of the numpy FP64 port in a fresh interpreter with a fixed
+    BLAS thread count, and the CPU / BLAS description printed beside it."""
+    import bench
+
+    r = bench.cpu_full_sweep(1, sites=3)
+    assert r["seconds"] > 0 and r["overlap"] == r["overlap"]
+    info = bench.cpu_info()
+    assert info["cores"] >= 1 and info["numpy"]
