@@ -464,7 +464,9 @@ def run_gpu(args, rank, world, local_rank):
         "warmup": max(args.warmup, 3), "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": DTYPES[args.precision],
         "data": "synthetic (seeded N(0,1)/sqrt(chi*d) cores)",
-        "config": {"workload": workload_name(), "form": args.precision, "l2": "inputs larger than L2 (split product cores %.1f GB)" % (N_SITES * 4096 * 2 * 4096 * 8 / 1e9),
+        "config": {"workload": workload_name(), "form": args.precision, "l2": "working set larger than L2 every step (bf16x6: %.1f GB of Gram-matrix slices written and "
+                   "read per sweep; tf32 forms: %.1f GB of split product cores)"
+                   % (N_SITES * 4096 * 4096 * 12 / 1e9, N_SITES * 4096 * 2 * 4096 * 8 / 1e9),
                    "parallelism": "replicas" if world > 1 else "single GPU"},
         "e2e": {"value": e2e_value, "unit": "sweeps/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": 16,
                 "api": "(MatrixProductOperator @ MatrixProductState) >> chi with AUTO_ROUND=False, ROUNDING='svd', "
@@ -585,39 +587,71 @@ def config3_instances(count=512, seed=3):
 
 
 def run_batched(args):
+    """Config 3: independent instances through one batched plan per GPU,
+    replayed as a captured CUDA graph.  Under torchrun the instances are dealt
+    across ranks (shard: no data exchange, every instance is independent); each
+    rank times its own share between barriers and the line reports all
+    instances over the slowest rank's time."""
     import torch
+    import torch.distributed as dist
 
     import __graft_entry__ as g
 
     g.build()
     from syngular_gb300 import _lib as L
-    from syngular_gb300.batched import BatchedRound, Instance, autotune
+    from syngular_gb300.batched import BatchedRound, Instance, autotune, shard
+
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local_rank = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local_rank)
+    dev = torch.device("cuda", local_rank)
+    if world > 1:
+        dist.init_process_group("nccl")
+
+    def barrier():
+        if world > 1:
+            dist.barrier()
+
+    def reduce(v, op):
+        if world == 1:
+            return v
+        t = torch.tensor([float(v)], dtype=torch.float64, device=dev)
+        dist.all_reduce(t, op=op)
+        return float(t.item())
 
     t_start = time.perf_counter()
 
     def log(msg):
-        print("[batched %7.1f s] %s" % (time.perf_counter() - t_start, msg), file=sys.stderr, flush=True)
+        if rank == 0:
+            print("[batched %7.1f s] %s" % (time.perf_counter() - t_start, msg), file=sys.stderr, flush=True)
 
+    prec = PRECISIONS[args.precision]
     data = config3_instances(args.instances)
-    insts = [Instance(W, X, chi) for W, X, chi in data]
-    log("%d instances resident" % len(insts))
-    tune = autotune(insts, precision=L.PREC_TF32X3, candidates=(4, 8), reps=1)
+    mine = shard(list(range(len(data))), rank, world)
+    insts = [Instance(*data[i]) for i in mine]
+    log("%d instances, %d on this rank" % (len(data), len(insts)))
+    tune = autotune(insts, precision=prec, candidates=(4, 8), reps=1)
     log("autotune: %s" % json.dumps(tune))
-    b = BatchedRound(insts, precision=L.PREC_TF32X3, streams=tune["streams"])
+    b = BatchedRound(insts, precision=prec, streams=tune["streams"])
     b.capture()
     log("graph captured")
     for _ in range(max(args.warmup, 3)):
         b.replay()
     torch.cuda.synchronize()
     log("warm-up replays done")
+    barrier()
+    torch.cuda.synchronize()
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     e0.record()
     for _ in range(args.steps):
         b.replay()
     e1.record()
     torch.cuda.synchronize()
-    ms = e0.elapsed_time(e1) / args.steps
+    barrier()
+    ms = reduce(e0.elapsed_time(e1) / args.steps, dist.ReduceOp.MAX if world > 1 else None)
     st = b.statuses()
+    converged = int(reduce(sum(1 for x in st if x >= 0), dist.ReduceOp.SUM if world > 1 else None))
     log("timed replays: %.1f ms per batch" % ms)
     # plain FP64 per-instance form on a sample, scaled to the batch by instance count
     sample = insts[: args.plain_sample]
@@ -630,18 +664,31 @@ def run_batched(args):
     p1.record()
     torch.cuda.synchronize()
     plain_ms_per_inst = p0.elapsed_time(p1) / len(sample)
+    # error of the batched form against the plain FP64 form on the sample
+    from syngular_gb300.tensor._ops import decode_overlap
+
+    errs = []
+    for fast, plain in zip(b.instances[: len(sample)], bp.instances):
+        a = decode_overlap(fast.ovl.cpu().tolist())
+        r = decode_overlap(plain.ovl.cpu().tolist())
+        errs.append(abs(a - r) / abs(r) if r != 0 else abs(a))
     log("plain FP64 sample: %.1f ms per instance" % plain_ms_per_inst)
     out = {
-        "metric": "batched MPO.MPS+TT-SVD-round+overlap instances/s", "value": len(insts) / (ms / 1e3),
-        "unit": "instances/s", "n_gpus": 1, "steps": args.steps, "warmup": max(args.warmup, 3),
-        "ms_per_step": ms, "higher_is_better": True, "dtype": "tf32x3/f32", "data": "synthetic (seeded)",
+        "metric": "batched MPO.MPS+TT-SVD-round+overlap instances/s", "value": len(data) / (ms / 1e3),
+        "unit": "instances/s", "n_gpus": world, "steps": args.steps, "warmup": max(args.warmup, 3),
+        "ms_per_step": ms, "higher_is_better": True, "scaling": "strong" if world > 1 else "weak",
+        "dtype": DTYPES[args.precision], "data": "synthetic (seeded)",
         "config": {"workload": "config3: %d instances, N~U[8,64], d in {2,3,4}, chi~U[16,128], D in {4,8,16}"
-                   % len(insts), "streams": tune["streams"], "graph": "one captured CUDA graph per batch",
-                   "autotune": tune},
-        "converged": sum(1 for x in st if x >= 0), "plain_fp64_instances_per_s": 1e3 / plain_ms_per_inst,
+                   % len(data), "streams": tune["streams"], "graph": "one captured CUDA graph per batch and rank",
+                   "autotune": tune, "parallelism": "instances sharded over %d rank(s)" % world},
+        "converged": converged, "instances": len(data), "plain_fp64_instances_per_s": 1e3 / plain_ms_per_inst,
         "plain_fp64_sample": len(sample),
+        "overlap_error_vs_fp64_on_sample": {"max_rel": max(errs), "median_rel": statistics.median(errs)},
     }
-    print(json.dumps(out))
+    if rank == 0:
+        print(json.dumps(out))
+    if world > 1:
+        dist.destroy_process_group()
     return 0
 
 

@@ -319,6 +319,13 @@ int eig_method() {
   return m;
 }
 
+}  // namespace
+
+// The eigensolver method chosen for the bond problems (see sgt_eig_method).
+int eig_method_current() { return eig_method(); }
+
+namespace {
+
 inline unsigned gs(int64_t n) {
   return (unsigned)std::max<int64_t>(1, std::min<int64_t>(cdiv(n, 256), 152 * 16));
 }

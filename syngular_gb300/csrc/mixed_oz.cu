@@ -42,6 +42,7 @@ void svd_round_plan_public(int n, const int64_t* shape, int64_t chi, std::vector
 size_t sym_eig_rows_ws_bytes(int64_t n);
 int sym_eig_rows_f32(cudaStream_t st, float* Z, int64_t n, float* Vt, float* lam, int* status, Arena& ar,
                      int method);
+int eig_method_current();
 
 namespace {
 
@@ -850,7 +851,7 @@ int oz_round_impl(cudaStream_t st, int n, const double* const* W, const int64_t*
     SGT_CUDA(cudaMemcpyAsync(Z32, Z.h, sizeof(float) * c * c, cudaMemcpyDeviceToDevice, st));
     {
       Arena ja(jscratch, jbytes);
-      SGT_TRY(sym_eig_rows_f32(st, Z32, c, Vt32, lam32, stat + k, ja, 1));
+      SGT_TRY(sym_eig_rows_f32(st, Z32, c, Vt32, lam32, stat + k, ja, eig_method_current()));
     }
     SGT_CUDA(cudaMemcpyAsync(Vt.h, Vt32, sizeof(float) * c * c, cudaMemcpyDeviceToDevice, st));
     SGT_CUDA(cudaMemsetAsync(Vt.l, 0, sizeof(float) * c * c, st));
