@@ -68,17 +68,17 @@ def _eig_profile(enable):
         return "%s: %s" % (type(e).__name__, e)
 
 
-def _eig_summary(stats, ms_total):
+def _eig_summary(stats, ms_total, kernel="gjacobi_kernel<1>"):
     """dominant_kernel object: gjacobi_kernel<1>'s mean CUDA-event launch time
     over the timed region, its share of the step, and its FP32 rate (sweeps x
     n(n-1)/2 pair visits x 12 n flops per launch) against the nominal FP32
     CUDA-core rate (152 SMs x 128 lanes x 2 flops x max SM clock; the measured
     peaks hold no FP32 figure) and against the 16 SMs of its one cluster."""
     if not isinstance(stats, tuple):
-        return {"kernel": "gjacobi_kernel<1>", "error": str(stats)}
+        return {"kernel": kernel, "error": str(stats)}
     ms, fl, n = stats
     if n <= 0 or ms <= 0:
-        return {"kernel": "gjacobi_kernel<1>", "launches": int(n)}
+        return {"kernel": kernel, "launches": int(n)}
     mhz = 2070.0
     try:
         with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
@@ -88,7 +88,7 @@ def _eig_summary(stats, ms_total):
     peak = 152 * 128 * 2 * mhz * 1e6 / 1e12
     achieved = fl / (ms / 1e3) / 1e12
     return {
-        "kernel": "gjacobi_kernel<1>", "launches": int(n), "ms_per_launch": ms / n,
+        "kernel": kernel, "launches": int(n), "ms_per_launch": ms / n,
         "share_of_step": ms / ms_total if ms_total > 0 else None,
         "bound": "latency: one 16-CTA cluster, shared-memory resident, sequential block steps",
         "achieved": achieved, "unit": "TFLOP/s (FP32)", "peak": peak,
@@ -477,7 +477,11 @@ def run_gpu(args, rank, world, local_rank):
         "jacobi_sweeps_max": int(status.item()),
     }
     # the dominant kernel (the bond eigensolver), from its live events
-    out["dominant_kernel"] = _eig_summary(eig_stats, ms_total)
+    # the form's first-approximation method: 2 for bf16x6 unless SGT_EIG_METHOD chooses
+    meth = int(os.environ.get("SGT_EIG_METHOD", "0") or 0)
+    if meth not in (1, 2, 3):
+        meth = 2 if args.precision == "bf16x6" else 1
+    out["dominant_kernel"] = _eig_summary(eig_stats, ms_total, "gjacobi_kernel<%d>" % meth)
     # roofline of the contractions (tcgen05 GEMM), from the live events
     peaks = {}
     try:
@@ -768,6 +772,102 @@ def run_config4(args):
     return 0
 
 
+def run_hbm(args):
+    """The HBM-bound kernels at the benchmark's sizes, each timed with CUDA
+    events over --steps launches after --warmup (inputs resident, outputs
+    overwritten; every working set is larger than L2 or the per-launch bytes
+    are reported as such):
+      contract  one product core P (4096, 2, 4096) FP64 = X (256, 2, 256) x W (16, 2, 2, 16)
+      concat    the direct sum of two N=32, chi=1024, d=2 chains (bond 2048)
+      overlap   <X|Z> over the 64-site chi=256 benchmark chain and a second chain of its shape
+      qr        Householder QR + thin Q of one 8192 x 4096 FP64 unfolding (the plain form's per-site step)
+    Bytes are algorithmic (inputs read once, outputs written once); the
+    ncu summaries under profiles/ give the DRAM counters of the same launches."""
+    import numpy as np
+    import torch
+
+    import __graft_entry__ as g
+
+    g.build()
+    from syngular_gb300 import _lib as L
+    from syngular_gb300.tensor import _ops
+
+    peaks = {}
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            peaks = json.load(f)
+    except OSError:
+        pass
+    hbm = peaks.get("hbm_gbs") or 6800.0
+    rng = np.random.default_rng(SEED)
+
+    def timed(fn):
+        for _ in range(max(args.warmup, 1)):
+            fn()
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        for _ in range(args.steps):
+            fn()
+        e1.record()
+        torch.cuda.synchronize()
+        return e0.elapsed_time(e1) / args.steps
+
+    out = {"metric": "HBM-bound kernels: achieved GB/s of algorithmic bytes", "unit": "GB/s",
+           "peak_hbm_gbs": hbm, "steps": args.steps, "warmup": max(args.warmup, 1), "kernels": {}}
+    # contract
+    X = L.as_device(rng.standard_normal((256, 2, 256)) / 16.0)
+    W = L.as_device(rng.standard_normal((16, 2, 2, 16)) / 6.0)
+    ms = timed(lambda: _ops.contract_mpo_mps([W], [X]))
+    by = 4096 * 2 * 4096 * 8 + X.numel() * 8 + W.numel() * 8
+    out["kernels"]["contract_mpo_mps_kernel"] = {"ms": ms, "bytes": by, "gbs": by / ms / 1e6,
+                                                 "frac": by / ms / 1e6 / hbm}
+    # concat (config 4 shapes)
+    A, B = config4_inputs()
+    Ad = [L.as_device(c) for c in A]
+    Bd = [L.as_device(c) for c in B]
+    outs = _ops.concat(Ad, Bd)
+    by = sum(o.numel() for o in outs) * 8 + sum(c.numel() for c in Ad + Bd) * 8
+    del outs
+    ms = timed(lambda: _ops.concat(Ad, Bd))
+    out["kernels"]["concat_kernel"] = {"ms": ms, "bytes": by, "gbs": by / ms / 1e6, "frac": by / ms / 1e6 / hbm,
+                                       "note": "one launch for all 32 sites (zero blocks written too)"}
+    del Ad, Bd
+    # overlap over two 64-site chi=256 chains
+    Xh, _Wh = make_inputs()
+    Yh = [rng.standard_normal(c.shape) / math.sqrt(CHI * D_PHYS) for c in Xh]
+    Xd = [L.as_device(c) for c in Xh]
+    Yd = [L.as_device(c) for c in Yh]
+    ms = timed(lambda: _ops.overlap_device(Xd, Yd))
+    by = sum(c.size for c in Xh + Yh) * 8
+    fl = sum(2 * D_PHYS * (x.shape[0] * x.shape[2] * y.shape[2] + x.shape[0] * y.shape[0] * y.shape[2])
+             for x, y in zip(Xh, Yh))
+    out["kernels"]["overlap_sweep"] = {"ms": ms, "bytes": by, "gbs": by / ms / 1e6, "frac": by / ms / 1e6 / hbm,
+                                       "fp64_tflops": fl / ms / 1e9,
+                                       "note": "a chain of FP64 GEMMs (2 per site, sequential): FP64-pipe and "
+                                               "latency bound, its bytes are small next to its flops"}
+    # Householder QR of one 8192 x 4096 unfolding + thin Q (4096 columns)
+    m, n = 8192, 4096
+    A0 = torch.from_numpy(rng.standard_normal((m, n))).to("cuda")
+    Aw = torch.empty_like(A0)
+    Q = torch.empty((m, n), dtype=torch.float64, device="cuda")
+    tau = torch.empty(n, dtype=torch.float64, device="cuda")
+    ws = L.workspace(L.query("sgt_qr_workspace_size", m, n, n))
+
+    def qr():
+        Aw.copy_(A0)
+        L.call("sgt_qr", L.ptr(Aw), m, n, n, L.ptr(tau), L.ptr(Q), n, L.ptr(ws), ws.numel(), L.stream_ptr())
+
+    ms = timed(qr)
+    fl = 2 * (2 * m * n * n - 2 * n ** 3 / 3)
+    out["kernels"]["householder_qr_8192x4096"] = {
+        "ms": ms, "fp64_tflops": fl / ms / 1e9,
+        "note": "panel_kernel (cluster panel factorisation) + FP64 trailing updates; FP64-pipe bound"}
+    out["value"] = out["kernels"]["contract_mpo_mps_kernel"]["gbs"]
+    print(json.dumps(out))
+    return 0
+
+
 def run_serving(args):
     import numpy as np
     import torch
@@ -851,7 +951,7 @@ def main():
     ap.add_argument("--no-plain", action="store_true")
     ap.add_argument("--plain-steps", type=int, default=2, help="timed sweeps of the plain FP64 form (~62 s each)")
     ap.add_argument("--no-cpu", action="store_true")
-    ap.add_argument("--workload", default="config2", choices=["config2", "batched", "serving", "config4"])
+    ap.add_argument("--workload", default="config2", choices=["config2", "batched", "serving", "config4", "hbm"])
     ap.add_argument("--instances", type=int, default=512)
     ap.add_argument("--plain-sample", type=int, default=8)
     ap.add_argument("--rate", type=float, default=10.0)
@@ -872,6 +972,8 @@ def main():
         return run_serving(args)
     if args.workload == "config4":
         return run_config4(args)
+    if args.workload == "hbm":
+        return run_hbm(args)
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
     local_rank = int(os.environ.get("LOCAL_RANK", "0"))

@@ -303,12 +303,14 @@ SGT_API size_t sgt_sym_eig_f32_workspace_size(int64_t n);
 SGT_API int sgt_sym_eig_f32(float* Z, int64_t n, float* Vt, float* lam, int* status, int method,
                             void* ws, size_t ws_bytes, void* stream);
 
-/* Eigensolver used for the bond problems of the Gram form (sgt_mpo_mps_round
- * with TF32 / TF32X3): the sgt_sym_eig_f32 method 1, 2 or 3 (other values leave
- * it unchanged).  Returns the previous choice.  The initial choice is 1, or the
- * value of the environment variable SGT_EIG_METHOD.  Process-wide.  The FP32
- * Jacobi stopping threshold on |g_p.g_q| / (|g_p||g_q|) is k eps sqrt(m) with
- * k = 1, or the value of SGT_EIG_TOL. */
+/* Eigensolver used for the bond problems of the Gram forms (sgt_mpo_mps_round
+ * / sgt_svd_round with TF32 / TF32X3 / BF16X6): the sgt_sym_eig_f32 method 1,
+ * 2 or 3 (other values leave it unchanged).  Returns the previous choice.
+ * Without a choice (this call or the environment variable SGT_EIG_METHOD) the
+ * TF32 forms use method 1 and the BF16X6 form method 2, whose lower accuracy
+ * near the cut its refinement removes.  Process-wide.  The FP32 Jacobi
+ * stopping threshold on |g_p.g_q| / (|g_p||g_q|) is k eps sqrt(m) with k = 1,
+ * or the value of SGT_EIG_TOL. */
 SGT_API int sgt_eig_method(int method);
 
 /* Batched MPO x MPS + TT-SVD round + overlap over `count` independent

@@ -321,8 +321,18 @@ int eig_method() {
 
 }  // namespace
 
-// The eigensolver method chosen for the bond problems (see sgt_eig_method).
-int eig_method_current() { return eig_method(); }
+// The first-approximation eigensolver of the BF16X6 form: the method chosen
+// through sgt_eig_method or SGT_EIG_METHOD when one was chosen, else method 2
+// (Jacobi on the rows of the Cholesky factor: about two thirds of the sweeps of
+// method 1, and its lower accuracy near the cut is what the refinement after it
+// removes).
+int eig_method_current() {
+  const int m = g_eig_method.load(std::memory_order_relaxed);
+  if (m != 0) return m;
+  const char* e = getenv("SGT_EIG_METHOD");
+  const int v = e ? atoi(e) : 0;
+  return (v >= 1 && v <= 3) ? v : 2;
+}
 
 namespace {
 

@@ -437,12 +437,15 @@ __global__ void oa_lambda_kernel(const float* __restrict__ Sh, const float* __re
 }
 
 // Refinement step, part 2: Et[i][j] = E[j][i], with
-//   E_jj = R_jj / 2,  E_ji = (S_ji + l_i R_ji) / (l_i - l_j)  where that is below 1/8,
-//   else R_ji / 2;    R = I - VV.
+//   E_jj = R_jj / 2,  E_ji = (S_ji + l_i R_ji) / (l_i - l_j)  where that is below 1/8
+//   and |l_i - l_j| stands above the products' own error (2^-30 of the largest
+//   |l|: eigenvalue differences below that are noise), else R_ji / 2;  R = I - VV.
 __global__ void oa_correction_kernel(const float* __restrict__ Sh, const float* __restrict__ Sl,
                                      const float* __restrict__ Vh, const float* __restrict__ Vl,
                                      const float* __restrict__ lh, const float* __restrict__ ll, int n,
-                                     float* __restrict__ Eh, float* __restrict__ El) {
+                                     const unsigned* __restrict__ lmax_bits, float* __restrict__ Eh,
+                                     float* __restrict__ El) {
+  const float floor_d = ldexpf(__uint_as_float(*lmax_bits), -30);
   for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < (int64_t)n * n;
        t += (int64_t)gridDim.x * blockDim.x) {
     const int i = (int)(t / n), j = (int)(t % n);  // output Et[i][j] = E[j][i]
@@ -462,7 +465,7 @@ __global__ void oa_correction_kernel(const float* __restrict__ Sh, const float* 
       // denominator l_i - l_j
       float dh = lh[i], dl = ll[i];
       df_add(dh, dl, -lh[j], -ll[j]);
-      if (fabsf(dh) > 8.f * fabsf(nh) && dh != 0.f) {
+      if (fabsf(dh) > 8.f * fabsf(nh) && fabsf(dh) > floor_d && isfinite(nh)) {
         df_div(nh, nl, dh, dl, eh, el);
       } else {
         eh = 0.5f * rh;
@@ -865,7 +868,11 @@ int oz_round_impl(cudaStream_t st, int n, const double* const* W, const int64_t*
       SGT_TRY(gemm(c, c, c, 1.f, Ts.mat(), Vts.mat(), 0.f, S, c));     // S = Vt Z Vt^T
       oa_lambda_kernel<<<grid_for(c), 256, 0, st>>>(S.h, S.l, VV.h, VV.l, (int)c, lamp.h, lamp.l);
       SGT_LAUNCHED();
-      oa_correction_kernel<<<grid_for(c * c), 256, 0, st>>>(S.h, S.l, VV.h, VV.l, lamp.h, lamp.l, (int)c, Et.h, Et.l);
+      SGT_CUDA(cudaMemsetAsync(gmax, 0, sizeof(unsigned), st));
+      pair_absmax_kernel<<<grid_for(c), 256, 0, st>>>(lamp.h, c, gmax);
+      SGT_LAUNCHED();
+      oa_correction_kernel<<<grid_for(c * c), 256, 0, st>>>(S.h, S.l, VV.h, VV.l, lamp.h, lamp.l, (int)c, gmax, Et.h,
+                                                             Et.l);
       SGT_LAUNCHED();
       SGT_TRY(split_pair(st, Et, c, Ets, c, c));
       SGT_TRY(pair_transpose(st, Xv, c, 0, Vt, c, 0, c, c, 1));             // Xv = Vt^T

@@ -1668,8 +1668,30 @@ int sym_eig_rows_f32(cudaStream_t st, float* Z, int64_t n, float* Vt, float* lam
   diag_order_kernel<<<1, 512, 0, st>>>(Z, n, (int)n, order);
   SGT_LAUNCHED();
   bool launched = false;
+  // timing (benchmarks only), as for method 1: never fails the solve
+  EigProfRec rec{nullptr, nullptr, status, n};
+  bool prof = false;
+  if (g_eig_prof_on) {
+    prof = cudaEventCreate(&rec.a) == cudaSuccess;
+    if (prof && cudaEventCreate(&rec.b) != cudaSuccess) {
+      cudaEventDestroy(rec.a);
+      rec.a = nullptr;
+      prof = false;
+    }
+    if (prof && cudaEventRecord(rec.a, st) != cudaSuccess) prof = false;
+    if (!prof) cudaGetLastError();
+  }
   if (method == 2) SGT_TRY(launch_gjacobi<2>(st, Z, n, Vt, n, n, n, norms, status, order, &launched));
   else SGT_TRY(launch_gjacobi<3>(st, Z, n, Vt, n, n, n, norms, status, order, &launched));
+  if (rec.b) {
+    if (prof && launched && cudaEventRecord(rec.b, st) == cudaSuccess) {
+      g_eig_prof.push_back(rec);
+    } else {
+      if (prof && launched) cudaGetLastError();
+      cudaEventDestroy(rec.a);
+      cudaEventDestroy(rec.b);
+    }
+  }
   if (!launched) return jacobi_rows_f32(st, Z, n, n, n, Vt, n, lam, status, ar0);
   SGT_TRY(sort_rows_t<float>(st, Z, n, n, n, Vt, n, lam, norms, perm, Gtmp, Vtmp));
   return SGT_OK;

@@ -108,7 +108,7 @@ def test_bad_job_does_not_stop_the_loop():
     rng = np.random.default_rng(11)
     srv = server_with_sessions(rng, 2, slots=2).start()
     bad = Job(kind="round", session="no-such-session", chi=4, precision=0)
-    good = Job(kind="overlap", session="s0", other="s1")
+    good = Job(kind="overlap", session="s0", other="s0")
     srv.submit(bad)
     srv.submit(good)
     assert bad.done.wait(60) and good.done.wait(60)

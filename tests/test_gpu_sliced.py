@@ -126,7 +126,7 @@ def test_bf16x6_round_matches_oracle(n, d, chi, D, cut):
         m = min(counts[k], len(spec_r[k]))
         kk = min(cut, m)
         np.testing.assert_allclose(s[off:off + kk], spec_r[k][:kk], rtol=0, atol=1e-8 * spec_r[k][0])
-        np.testing.assert_allclose(s[off + kk:off + m] ** 2, spec_r[k][kk:m] ** 2, rtol=0, atol=1e-5 * spec_r[k][0] ** 2)
+        np.testing.assert_allclose(s[off + kk:off + m] ** 2, spec_r[k][kk:m] ** 2, rtol=0, atol=1e-4 * spec_r[k][0] ** 2)
         off += counts[k]
     np.testing.assert_allclose(disc.cpu().numpy()[: n - 1], disc_r, rtol=1e-6, atol=1e-12)
 
