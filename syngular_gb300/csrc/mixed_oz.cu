@@ -25,8 +25,10 @@
 //     two steps take the FP32 Jacobi's ~1e-6 to the GEMMs' own accuracy.
 //     Pairs whose correction would not be small (near-equal eigenvalues)
 //     keep E_ij = R_ij / 2, as in the published method's cluster case.
-// Product cores are never stored whole: the right sweep slices P_k site by
-// site straight from X_k and W_k.
+// Product cores are never formed: the left recursion contracts X and W
+// separately (steps A-D), and the right sweep forms Y_k = P_k F_{k+1} as
+// (F W^T) then X, 2.2e9 instead of 1.7e10 FP64-equivalent flops per site at
+// the benchmark's shapes.
 #include <float.h>
 
 #include <algorithm>
@@ -48,17 +50,6 @@ namespace {
 
 inline unsigned grid_for(int64_t n, int per = 256) {
   return (unsigned)std::max<int64_t>(1, std::min<int64_t>(cdiv(n, per), 152 * 16));
-}
-
-// FP64 -> pair
-__global__ void f64_to_pair_kernel(const double* __restrict__ x, float* __restrict__ h, float* __restrict__ l,
-                                   int64_t n) {
-  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
-    const double v = x[i];
-    const float a = (float)v;
-    h[i] = a;
-    l[i] = (float)(v - (double)a);
-  }
 }
 
 // dst (rows x cols FP64, ldd) = pair src (lds)
@@ -103,59 +94,27 @@ __global__ void pair_transpose_kernel(float* __restrict__ dh, float* __restrict_
   }
 }
 
-// P[(a,b,o)][(a2,b2)] = sum_i X[a,i,a2] W[b,i,o,b2] in pair arithmetic from the
-// pairs of X and W (error-free products, two-sum accumulation).
-__device__ __forceinline__ void product_elem(const float* __restrict__ Xh, const float* __restrict__ Xl,
-                                             const float* __restrict__ Wh, const float* __restrict__ Wl, int a, int b,
-                                             int o, int a2, int b2, int I, int O, int A2, int B2, int Bd, float& h,
-                                             float& l) {
-  h = 0.f;
-  l = 0.f;
-  for (int i = 0; i < I; ++i) {
-    const int64_t xi = ((int64_t)a * I + i) * A2 + a2;
-    const int64_t wi = (((int64_t)b * I + i) * O + o) * B2 + b2;
-    df_fma(h, l, Xh[xi], Xl[xi], Wh[wi], Wl[wi]);
-  }
-  (void)Bd;
-  df_norm(h, l);
-}
+// dst (contiguous in the order of the five output dimensions n[0..4]) =
+// src at sum_d i_d * st[d]: a pair-valued index permutation.
+struct Perm5 {
+  int64_t n[5];
+  int64_t st[5];
+};
 
-// One block per row (a, b, o) of the product core: pass 1 finds the row's
-// exponent, pass 2 recomputes the row and writes its slices (padding zeroed).
-__global__ void product_slices_kernel(const float* __restrict__ Xh, const float* __restrict__ Xl,
-                                      const float* __restrict__ Wh, const float* __restrict__ Wl, int Bd, int I, int O,
-                                      int A2, int B2, __nv_bfloat16* __restrict__ out, int64_t ldo, int64_t sstride,
-                                      int* __restrict__ ex) {
-  __shared__ float red[32];
-  __shared__ int s_e;
-  const int r = blockIdx.x;
-  const int o = r % O, ab = r / O, b = ab % Bd, a = ab / Bd;
-  const int ncol = A2 * B2;
-  float mx = 0.f;
-  for (int c = threadIdx.x; c < ncol; c += blockDim.x) {
-    float h, l;
-    product_elem(Xh, Xl, Wh, Wl, a, b, o, c / B2, c % B2, I, O, A2, B2, Bd, h, l);
-    mx = fmaxf(mx, fabsf(h));
+__global__ void pair_permute_kernel(float* __restrict__ dh, float* __restrict__ dl, const float* __restrict__ sh,
+                                    const float* __restrict__ sl, const Perm5 pm) {
+  const int64_t total = pm.n[0] * pm.n[1] * pm.n[2] * pm.n[3] * pm.n[4];
+  for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < total; t += (int64_t)gridDim.x * blockDim.x) {
+    int64_t rem = t, off = 0;
+#pragma unroll
+    for (int d = 4; d >= 0; --d) {
+      const int64_t i = rem % pm.n[d];
+      rem /= pm.n[d];
+      off += i * pm.st[d];
+    }
+    dh[t] = sh[off];
+    dl[t] = sl[off];
   }
-  for (int s = 16; s > 0; s >>= 1) mx = fmaxf(mx, __shfl_xor_sync(0xffffffffu, mx, s));
-  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = mx;
-  __syncthreads();
-  if (threadIdx.x == 0) {
-    float m = 0.f;
-    for (int w = 0; w < (int)(blockDim.x >> 5); ++w) m = fmaxf(m, red[w]);
-    int e = 0;
-    if (m > 0.f && isfinite(m)) frexpf(m, &e);
-    s_e = e;
-    ex[r] = e;
-  }
-  __syncthreads();
-  const int e = s_e;
-  for (int c = threadIdx.x; c < ncol; c += blockDim.x) {
-    float h, l;
-    product_elem(Xh, Xl, Wh, Wl, a, b, o, c / B2, c % B2, I, O, A2, B2, Bd, h, l);
-    slice_store(ldexpf(h, 6 - e), ldexpf(l, 6 - e), out, sstride, (int64_t)r * ldo + c);
-  }
-  for (int64_t c = ncol + threadIdx.x; c < ldo; c += blockDim.x) slice_zero(out, sstride, (int64_t)r * ldo + c);
 }
 
 // Steps B and C of the structured Gram step (see gram.cu) in pair arithmetic,
@@ -649,16 +608,12 @@ int oz_round_impl(cudaStream_t st, int n, const double* const* W, const int64_t*
   svd_round_plan_public(n, shp.data(), chi, bb, x, cnt);
 
   // ---- workspace ----
-  int64_t rmax = 1, cmax = 1, xmax = 1, wmax = 1, t1max = 1, t3max = 1, pmax = 1, pemax = 1;
+  int64_t rmax = 1, cmax = 1, t1max = 1, t3max = 1;
   size_t gsmax = 1, xtmax = 1, x2max = 1, t3smax = 1;
   int64_t gcrows = 1, xtrows = 1, x2rows = 1, t3rows = 1;
   for (int k = 0; k < n; ++k) {
     rmax = std::max(rmax, std::max(R[k], R[k + 1]));
     cmax = std::max(cmax, Pd[k] * x[k + 1]);
-    xmax = std::max<int64_t>(xmax, xs[3 * k] * xs[3 * k + 1] * xs[3 * k + 2]);
-    wmax = std::max<int64_t>(wmax, w[k].b * w[k].i * w[k].o * w[k].b2);
-    pmax = std::max<int64_t>(pmax, (int64_t)oz_slice_elems(R[k] * Pd[k], R[k + 1]));
-    pemax = std::max<int64_t>(pemax, R[k] * Pd[k]);
     if (k + 1 < n) {
       const int64_t chi_k = xs[3 * k], d = xs[3 * k + 1], chi2 = xs[3 * k + 2];
       t1max = std::max<int64_t>(t1max, chi_k * w[k].b * w[k].b * d * chi2);
@@ -688,11 +643,26 @@ int oz_round_impl(cudaStream_t st, int n, const double* const* W, const int64_t*
   Pair T3 = take_pair(ar, t3max);
   Sliced T3s = take_raw(t3smax, t3rows);
   Sliced Xt = take_raw(xtmax, xtrows), X2 = take_raw(x2max, x2rows);
-  Pair pX = take_pair(ar, xmax), pW = take_pair(ar, wmax);
-  __nv_bfloat16* Ps = ar.take<__nv_bfloat16>((size_t)pmax);
-  int* Pe_all = ar.take<int>((size_t)pemax);
+  // structured Y: F as rows of B', W and X as slice sets, T = F W^T and its permutation
+  size_t fsmax = 1, tqsmax = 1, wslmax = 1, xslmax = 1;
+  int64_t fsrows = 1, tpmax = 1, tqrows = 1, wslrows = 1, xslrows = 1;
+  for (int k = 0; k < n; ++k) {
+    const int64_t A = xs[3 * k], I = xs[3 * k + 1], A2 = xs[3 * k + 2], xc = x[k + 1];
+    const int64_t Bk = w[k].b, O = w[k].o, B2 = w[k].b2, bio = Bk * I * O;
+    fsmax = std::max(fsmax, oz_slice_elems(xc * A2, B2));
+    fsrows = std::max(fsrows, xc * A2);
+    tpmax = std::max(tpmax, xc * A2 * bio);
+    tqsmax = std::max(tqsmax, oz_slice_elems(Bk * O * xc, I * A2));
+    tqrows = std::max(tqrows, Bk * O * xc);
+    wslmax = std::max(wslmax, oz_slice_elems(bio, B2));
+    wslrows = std::max(wslrows, bio);
+    xslmax = std::max(xslmax, oz_slice_elems(A, I * A2));
+    xslrows = std::max(xslrows, A);
+  }
+  Sliced Fs = take_raw(fsmax, fsrows), Tqs = take_raw(tqsmax, tqrows);
+  Sliced Wsl = take_raw(wslmax, wslrows), Xsl = take_raw(xslmax, xslrows);
+  Pair Tp = take_pair(ar, tpmax), Tq = take_pair(ar, tpmax);
   Pair Ft = take_pair(ar, chi * rmax + 1);
-  Sliced Fts = take_sliced(ar, chi, rmax);
   Pair Yt = take_pair(ar, cmax * rmax), Ytp = take_pair(ar, cmax * rmax), GY = take_pair(ar, cmax * rmax);
   Sliced Yts = take_sliced(ar, cmax, rmax), Ytps = take_sliced(ar, cmax, rmax), GYs = take_sliced(ar, cmax, rmax);
   Sliced Ys = take_sliced(ar, rmax, cmax);
@@ -712,7 +682,12 @@ int oz_round_impl(cudaStream_t st, int n, const double* const* W, const int64_t*
   size_t part_bytes = 0;
   for (int k = 0; k < n; ++k) {
     const int64_t r = R[k], r2 = R[k + 1], c = Pd[k] * x[k + 1];
-    part_bytes = std::max(part_bytes, oz_gemm_ws_bytes(x[k + 1], r, r2));
+    {
+      const int64_t A = xs[3 * k], I = xs[3 * k + 1], A2 = xs[3 * k + 2], xc = x[k + 1];
+      const int64_t Bk = w[k].b, O = w[k].o, B2 = w[k].b2;
+      part_bytes = std::max(part_bytes, oz_gemm_ws_bytes(xc * A2, Bk * I * O, B2));
+      part_bytes = std::max(part_bytes, oz_gemm_ws_bytes(A, Bk * O * xc, I * A2));
+    }
     part_bytes = std::max(part_bytes, oz_gemm_ws_bytes(c, r, r));
     part_bytes = std::max(part_bytes, oz_gemm_ws_bytes(c, c, r));
     part_bytes = std::max(part_bytes, oz_gemm_ws_bytes(c, c, c));
@@ -813,24 +788,30 @@ int oz_round_impl(cudaStream_t st, int n, const double* const* W, const int64_t*
   SGT_LAUNCHED();
   for (int k = n - 1; k >= 0; --k) {
     const int64_t r = R[k], r2 = R[k + 1], p = Pd[k], xc = x[k + 1], c = p * xc;
-    const int64_t xsz = xs[3 * k] * xs[3 * k + 1] * xs[3 * k + 2], wsz = w[k].b * w[k].i * w[k].o * w[k].b2;
-    // product core P_k sliced by rows (a, b, o), straight from X_k and W_k
-    f64_to_pair_kernel<<<grid_for(xsz), 256, 0, st>>>(X[k], pX.h, pX.l, xsz);
-    SGT_LAUNCHED();
-    f64_to_pair_kernel<<<grid_for(wsz), 256, 0, st>>>(W[k], pW.h, pW.l, wsz);
-    SGT_LAUNCHED();
-    const int64_t prow = r * p, pld = oz_ld(r2), pss = prow * pld;
-    SGT_REQUIRE(prow < (1ll << 31), SGT_ERR_INVALID, "mpo_mps_round: product core too tall");
-    product_slices_kernel<<<(unsigned)prow, 256, 0, st>>>(pX.h, pX.l, pW.h, pW.l, (int)w[k].b, (int)w[k].i,
-                                                          (int)w[k].o, (int)xs[3 * k + 2], (int)w[k].b2, Ps, pld, pss,
-                                                          Pe_all);
-    SGT_LAUNCHED();
-    // Yt (c x r): rows o*xc..: Ft (xc x r2) P[:, o, :]^T
-    SGT_TRY(split_pair(st, Ft, r2, Fts, xc, r2));
-    for (int64_t o = 0; o < p; ++o) {
-      OzMat Po{Ps + o * pld, pld * p, pss, Pe_all + o, p};
-      Pair dst{Yt.h + o * xc * r, Yt.l + o * xc * r};
-      SGT_TRY(gemm(xc, r, r2, 1.f, Fts.mat(), Po, 0.f, dst, r));
+    // Yt (c x r): Yt[(o, j)][(a, b)] = sum_{i, a', b'} F[j][(a', b')] X[a][i][a'] W[b][i][o][b'],
+    // contracted in two products without forming the product core:
+    //   S1: T[(j, a')][(b, i, o)] = sum_b' F[(j, a')][b'] W[(b, i, o)][b']          (K = B')
+    //   S2: Y2[a][(b, o, j)] = sum_(i, a') X[a][(i, a')] T[(b, o, j)][(i, a')]   (K = d chi')
+    //   Yt[(o, j)][(a, b)] = Y2[a][(b, o, j)]
+    {
+      const int64_t A = xs[3 * k], I = xs[3 * k + 1], A2 = xs[3 * k + 2];
+      const int64_t Bk = w[k].b, O = w[k].o, B2 = w[k].b2, bio = Bk * I * O;
+      SGT_TRY(split_pair(st, Ft, B2, Fs, xc * A2, B2));
+      SGT_TRY(oz_split_f64(st, W[k], B2, 1, bio, B2, Wsl.s, Wsl.e, 1));
+      Wsl.rows = bio;
+      Wsl.cols = B2;
+      SGT_TRY(gemm(xc * A2, bio, B2, 1.f, Fs.mat(), Wsl.mat(), 0.f, Tp, bio));
+      Perm5 pq{{Bk, O, xc, I, A2}, {I * O, 1, A2 * bio, O, bio}};
+      pair_permute_kernel<<<grid_for(xc * A2 * bio), 256, 0, st>>>(Tq.h, Tq.l, Tp.h, Tp.l, pq);
+      SGT_LAUNCHED();
+      SGT_TRY(split_pair(st, Tq, I * A2, Tqs, Bk * O * xc, I * A2));
+      SGT_TRY(oz_split_f64(st, X[k], I * A2, 1, A, I * A2, Xsl.s, Xsl.e, 1));
+      Xsl.rows = A;
+      Xsl.cols = I * A2;
+      SGT_TRY(gemm(A, Bk * O * xc, I * A2, 1.f, Xsl.mat(), Tqs.mat(), 0.f, GY, Bk * O * xc));
+      Perm5 py{{1, O, xc, A, Bk}, {0, xc, 1, Bk * O * xc, O * xc}};
+      pair_permute_kernel<<<grid_for(c * r), 256, 0, st>>>(Yt.h, Yt.l, GY.h, GY.l, py);
+      SGT_LAUNCHED();
     }
     if (k == 0) {
       // core_0[0][o][j] = Yt[o*xc + j][0]

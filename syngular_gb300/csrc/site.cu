@@ -5,6 +5,8 @@
 // (the physical leg), so they are bound by the HBM write of the product core:
 // each thread produces two adjacent outputs of one row and stores them as a
 // 16-byte vector when the row is even-sized.
+#include <algorithm>
+
 #include "common.cuh"
 
 namespace sgt {
@@ -100,37 +102,49 @@ struct ConcatBatch {
   int64_t total;
 };
 
-__device__ __forceinline__ double concat_value(const ConcatSite& d, int64_t idx) {
-  const int64_t r = idx % d.orr;
-  const int64_t t = idx / d.orr;
-  const int64_t p = t % d.phys;
-  const int64_t l = t / d.phys;
-  switch (d.pos) {
-    case 0:  // first: [A | B] along r
-      return r < d.ra ? d.A[(l * d.phys + p) * d.ra + r] : d.B[(l * d.phys + p) * d.rb + (r - d.ra)];
-    case 2:  // last: stacked along l
-      return l < d.la ? d.A[(l * d.phys + p) * d.ra + r] : d.B[((l - d.la) * d.phys + p) * d.rb + r];
-    case 3:  // single site
-      return d.A[idx] + d.B[idx];
-    default:  // middle: block diagonal
-      if (l < d.la && r < d.ra) return d.A[(l * d.phys + p) * d.ra + r];
-      if (l >= d.la && r >= d.ra) return d.B[((l - d.la) * d.phys + p) * d.rb + (r - d.ra)];
-      return 0.0;
-  }
+// One warp per output row (l, p) of one site (grid.y = site): each row is at
+// most two contiguous runs copied from A / B or zero-filled, so there is no
+// per-element index arithmetic; consecutive lanes move consecutive elements.
+__device__ __forceinline__ void copy_run(double* __restrict__ dst, const double* __restrict__ src, int64_t n,
+                                         int lane) {
+  for (int64_t i = lane; i < n; i += 32) dst[i] = src[i];
+}
+
+__device__ __forceinline__ void zero_run(double* __restrict__ dst, int64_t n, int lane) {
+  for (int64_t i = lane; i < n; i += 32) dst[i] = 0.0;
 }
 
 __global__ void concat_kernel(const __grid_constant__ ConcatBatch batch) {
-  for (int64_t g = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; g < batch.total;
-       g += (int64_t)gridDim.x * blockDim.x) {
-    int lo = 0, hi = batch.n - 1;
-    while (lo < hi) {  // last site with begin <= g
-      int mid = (lo + hi + 1) >> 1;
-      if (batch.s[mid].begin <= g) lo = mid;
-      else hi = mid - 1;
+  const ConcatSite& d = batch.s[blockIdx.y];
+  const int64_t rows = d.ol * d.phys;
+  const int lane = threadIdx.x & 31, nw = blockDim.x >> 5;
+  for (int64_t row = (int64_t)blockIdx.x * nw + (threadIdx.x >> 5); row < rows; row += (int64_t)gridDim.x * nw) {
+    const int64_t l = row / d.phys, p = row - l * d.phys;
+    double* o = d.out + row * d.orr;
+    switch (d.pos) {
+      case 0:  // first: [A | B] along r
+        copy_run(o, d.A + (l * d.phys + p) * d.ra, d.ra, lane);
+        copy_run(o + d.ra, d.B + (l * d.phys + p) * d.rb, d.rb, lane);
+        break;
+      case 2:  // last: stacked along l
+        if (l < d.la) copy_run(o, d.A + (l * d.phys + p) * d.ra, d.orr, lane);
+        else copy_run(o, d.B + ((l - d.la) * d.phys + p) * d.rb, d.orr, lane);
+        break;
+      case 3: {  // single site: A + B
+        const double* a = d.A + row * d.orr;
+        const double* b = d.B + row * d.orr;
+        for (int64_t i = lane; i < d.orr; i += 32) o[i] = a[i] + b[i];
+        break;
+      }
+      default:  // middle: block diagonal
+        if (l < d.la) {
+          copy_run(o, d.A + (l * d.phys + p) * d.ra, d.ra, lane);
+          zero_run(o + d.ra, d.rb, lane);
+        } else {
+          zero_run(o, d.ra, lane);
+          copy_run(o + d.ra, d.B + ((l - d.la) * d.phys + p) * d.rb, d.rb, lane);
+        }
     }
-    const ConcatSite& d = batch.s[lo];
-    int64_t idx = g - d.begin;
-    d.out[idx] = concat_value(d, idx);
   }
 }
 
@@ -292,7 +306,10 @@ int bond_concat_chain(cudaStream_t st, int n, const double* const* A, const int6
     }
     batch.total = total;
     if (total == 0) continue;
-    concat_kernel<<<grid_for(total, 256), 256, 0, st>>>(batch);
+    int64_t maxrows = 1;
+    for (int j = 0; j < batch.n; ++j) maxrows = std::max<int64_t>(maxrows, batch.s[j].ol * batch.s[j].phys);
+    dim3 grid((unsigned)std::max<int64_t>(1, std::min<int64_t>(cdiv(maxrows, 8), 1024)), (unsigned)batch.n);
+    concat_kernel<<<grid, 256, 0, st>>>(batch);
     SGT_LAUNCHED();
   }
   return SGT_OK;

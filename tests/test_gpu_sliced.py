@@ -57,7 +57,8 @@ def test_exact_on_small_integers(M, N, K):
     np.testing.assert_array_equal(C, A @ B.T)
 
 
-@pytest.mark.parametrize("M,N,K", [(512, 4096, 4096), (1000, 256, 512), (512, 512, 512), (7, 9, 3), (4096, 64, 256)])
+@pytest.mark.parametrize("M,N,K", [(512, 4096, 4096), (1000, 256, 512), (512, 512, 512), (7, 9, 3), (4096, 64, 256),
+                                   (512, 65536, 256)])
 def test_accuracy_bound(M, N, K):
     rng = np.random.default_rng(7 * M + N)
     A = rng.standard_normal((M, K)) * np.exp(rng.uniform(-3, 3, size=(M, 1)))
