@@ -525,9 +525,229 @@ __global__ void axpby_pair_f64_kernel(const float* __restrict__ h, const float* 
   }
 }
 
+
+// ---------------------------------------------------------------------------
+// The kept subspace without eigenvectors (callers that do not ask for
+// spectra): trace-correcting purification (Niklasson, Phys. Rev. B 66, 155115,
+// 2002, "TC2") drives X_0 = Z / |Z|_F to the orthogonal projector onto the
+// eigenvectors of the `keep` largest eigenvalues of Z, squaring X, or taking
+// 2X - X^2, whichever moves trace(X) toward `keep`; every product on the
+// sliced GEMM, so the projector is FP64-class.  A basis of its range:
+// Q = L^T X with L the rank-keep pivoted Cholesky factor of X's FP32 part (a
+// projector's Cholesky factor has orthonormal columns, so Q starts
+// orthonormal to FP32 rounding and its rows lie in X's range to full
+// accuracy), then Newton-Schulz steps Q <- 1.5 Q - 0.5 (Q Q^T) Q in pair
+// precision.  The rounded
+// state depends on the kept subspace only (any orthonormal basis of it is a
+// gauge choice), so this replaces the eigensolve when no spectrum is wanted.
+// ---------------------------------------------------------------------------
+
+// out = sum of squares of h (double); one block
+__global__ void pair_frob_trace_kernel(const float* __restrict__ h, const float* __restrict__ l, int64_t n,
+                                       double* __restrict__ frob, double* __restrict__ trace) {
+  __shared__ double red[2][32];
+  double ss = 0.0, tr = 0.0;
+  for (int64_t i = threadIdx.x; i < n * n; i += blockDim.x) {
+    const double v = (double)h[i];
+    ss += v * v;
+    if (i / n == i % n) tr += v + (double)l[i];
+  }
+  for (int o = 16; o > 0; o >>= 1) {
+    ss += __shfl_xor_sync(0xffffffffu, ss, o);
+    tr += __shfl_xor_sync(0xffffffffu, tr, o);
+  }
+  if ((threadIdx.x & 31) == 0) red[0][threadIdx.x >> 5] = ss, red[1][threadIdx.x >> 5] = tr;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double a = 0.0, b = 0.0;
+    for (int w = 0; w < (int)(blockDim.x >> 5); ++w) a += red[0][w], b += red[1][w];
+    *frob = sqrt(a);
+    *trace = b;
+  }
+}
+
+// X = Z / |Z|_F (pair times a scalar)
+__global__ void pair_scale_by_kernel(const float* __restrict__ zh, const float* __restrict__ zl, int64_t n,
+                                     const double* __restrict__ frob, float* __restrict__ xh, float* __restrict__ xl) {
+  const double f = *frob;
+  const float inv = (f > 0.0) ? (float)(1.0 / f) : 0.f;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    const float p = zh[i] * inv;
+    const float pe = fmaf(zh[i], inv, -p) + zl[i] * inv;
+    float a = p, b = pe;
+    df_norm(a, b);
+    xh[i] = a;
+    xl[i] = b;
+  }
+}
+
+// TC2 decision from the traces of X and X^2 (one block): choice = 1 for X^2,
+// 0 for 2X - X^2.  ctl[1] (done) is set once the previous step's largest
+// |X^2 - X| (resid) fell to 2^-34: X is then a projector to the products'
+// accuracy, and every later step of the loop returns at once.
+__global__ void tc2_choose_kernel(const float* __restrict__ xh, const float* __restrict__ xl,
+                                  const float* __restrict__ x2h, const float* __restrict__ x2l, int n, int keep,
+                                  int* __restrict__ ctl, unsigned* __restrict__ resid) {
+  __shared__ double red[2][32];
+  __shared__ int s_done;
+  if (threadIdx.x == 0) {
+    s_done = ctl[1];
+    if (!s_done && __uint_as_float(*resid) <= ldexpf(1.f, -34)) s_done = ctl[1] = 1;
+  }
+  __syncthreads();
+  if (s_done) return;
+  double t = 0.0, t2 = 0.0;
+  for (int i = threadIdx.x; i < n; i += blockDim.x) {
+    const int64_t d = (int64_t)i * n + i;
+    t += (double)xh[d] + (double)xl[d];
+    t2 += (double)x2h[d] + (double)x2l[d];
+  }
+  for (int o = 16; o > 0; o >>= 1) {
+    t += __shfl_xor_sync(0xffffffffu, t, o);
+    t2 += __shfl_xor_sync(0xffffffffu, t2, o);
+  }
+  if ((threadIdx.x & 31) == 0) red[0][threadIdx.x >> 5] = t, red[1][threadIdx.x >> 5] = t2;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double a = 0.0, b = 0.0;
+    for (int w = 0; w < (int)(blockDim.x >> 5); ++w) a += red[0][w], b += red[1][w];
+    ctl[0] = fabs(b - keep) < fabs(2.0 * a - b - keep) ? 1 : 0;
+    *resid = 0u;  // this step's update records its own largest |X^2 - X|
+  }
+}
+
+// X <- X^2 or 2X - X^2 (pair), symmetrised; |X^2 - X| max into resid (bits)
+__global__ void tc2_update_kernel(float* __restrict__ xh, float* __restrict__ xl, const float* __restrict__ x2h,
+                                  const float* __restrict__ x2l, int n, const int* __restrict__ ctl,
+                                  unsigned* __restrict__ resid) {
+  if (ctl[1]) return;
+  const int ch = ctl[0];
+  float worst = 0.f;
+  for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < (int64_t)n * n;
+       t += (int64_t)gridDim.x * blockDim.x) {
+    const int i = (int)(t / n), j = (int)(t % n);
+    if (j < i) continue;
+    const int64_t a = (int64_t)i * n + j, b = (int64_t)j * n + i;
+    float vh[2], vl[2];
+    const int64_t idx[2] = {a, b};
+#pragma unroll
+    for (int q = 0; q < 2; ++q) {
+      float h2 = x2h[idx[q]], l2 = x2l[idx[q]];
+      worst = fmaxf(worst, fabsf((h2 - xh[idx[q]]) + (l2 - xl[idx[q]])));
+      if (ch) {
+        vh[q] = h2;
+        vl[q] = l2;
+      } else {  // 2X - X^2
+        float h = 2.f * xh[idx[q]], l = 2.f * xl[idx[q]];
+        df_add(h, l, -h2, -l2);
+        vh[q] = h;
+        vl[q] = l;
+      }
+    }
+    float h = vh[0], l = vl[0];
+    df_add(h, l, vh[1], vl[1]);
+    h *= 0.5f;
+    l *= 0.5f;
+    xh[a] = h;
+    xl[a] = l;
+    xh[b] = h;
+    xl[b] = l;
+  }
+  for (int o = 16; o > 0; o >>= 1) worst = fmaxf(worst, __shfl_xor_sync(0xffffffffu, worst, o));
+  if ((threadIdx.x & 31) == 0 && worst > 0.f) atomicMax(resid, __float_as_uint(worst));
+}
+
+// Pivoted Cholesky of the purified projector's FP32 part, stopped at rank
+// `keep` (one block, left-looking: O(c keep^2) work, the remaining diagonal
+// in shared memory): A (c x c) ~ L L^T, Lt (keep x c) = L^T.  A is an
+// orthogonal projector of rank keep up to rounding, so L^T L = I up to FP32
+// rounding too: L is a well-conditioned basis without any sketch.  The
+// sliced GEMM then forms L^T X, whose rows lie in the projector's range to
+// its full accuracy.  used: c ints of scratch.
+__global__ void __launch_bounds__(1024) pivoted_chol_kernel(const float* __restrict__ A, int c, int keep,
+                                                            float* __restrict__ Lt, int* __restrict__ used) {
+  extern __shared__ float pc_diag[];  // c floats
+  __shared__ float s_val[32];
+  __shared__ int s_idx[32];
+  __shared__ int s_p;
+  __shared__ float s_inv;
+  for (int i = threadIdx.x; i < c; i += blockDim.x) {
+    pc_diag[i] = A[(int64_t)i * c + i];
+    used[i] = 0;
+  }
+  __syncthreads();
+  for (int s = 0; s < keep; ++s) {
+    float best = -1.f;
+    int bi = 0;
+    for (int i = threadIdx.x; i < c; i += blockDim.x) {
+      const float v = used[i] ? -1.f : pc_diag[i];
+      if (v > best) best = v, bi = i;
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+      const float ov = __shfl_xor_sync(0xffffffffu, best, o);
+      const int oi = __shfl_xor_sync(0xffffffffu, bi, o);
+      if (ov > best || (ov == best && oi < bi)) best = ov, bi = oi;
+    }
+    if ((threadIdx.x & 31) == 0) s_val[threadIdx.x >> 5] = best, s_idx[threadIdx.x >> 5] = bi;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      float b = -1.f;
+      int p = 0;
+      for (int w = 0; w < (int)(blockDim.x >> 5); ++w)
+        if (s_val[w] > b || (s_val[w] == b && s_idx[w] < p)) b = s_val[w], p = s_idx[w];
+      s_p = p;
+      used[p] = 1;
+      s_inv = 1.f / sqrtf(fmaxf(b, 1e-30f));
+    }
+    __syncthreads();
+    const int p = s_p;
+    const float inv = s_inv;
+    for (int i = threadIdx.x; i < c; i += blockDim.x) {
+      float v = A[(int64_t)i * c + p];
+      for (int t = 0; t < s; ++t) v -= Lt[(int64_t)t * c + i] * Lt[(int64_t)t * c + p];
+      const float l = v * inv;
+      Lt[(int64_t)s * c + i] = l;
+      pc_diag[i] -= l * l;
+    }
+    __syncthreads();
+  }
+}
+
+// disc = 1 - sum_j (T[j] . Q[j]) / trace(Z)   (T = Q Z, rows of Q the kept basis)
+__global__ void kept_trace_kernel(const float* __restrict__ th, const float* __restrict__ tl,
+                                  const float* __restrict__ qh, const float* __restrict__ ql, int64_t count,
+                                  const double* __restrict__ trace_z, double* __restrict__ disc) {
+  __shared__ double red[32];
+  double s = 0.0;
+  for (int64_t i = threadIdx.x; i < count; i += blockDim.x)
+    s += ((double)th[i] + (double)tl[i]) * ((double)qh[i] + (double)ql[i]);
+  for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = s;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double a = 0.0;
+    for (int w = 0; w < (int)(blockDim.x >> 5); ++w) a += red[w];
+    const double tz = *trace_z;
+    *disc = tz > 0.0 ? fmax(0.0, 1.0 - a / tz) : 0.0;
+  }
+}
+
+// status word of a projector bond: 0 when X converged to a projector
+// (the loop stopped, or its last |X^2 - X| is at most 2^-30), -1 otherwise
+__global__ void tc2_status_kernel(const int* __restrict__ ctl, const unsigned* __restrict__ resid,
+                                  int* __restrict__ st) {
+  *st = (ctl[1] || __uint_as_float(*resid) <= ldexpf(1.f, -30)) ? 0 : -1;
+}
+
 struct Site4 {
   int64_t b, i, o, b2;
 };
+
+// Largest number of purification steps (the loop stops itself once X is a
+// projector; about 2 log2(|Z|_F / gap at the cut) + 6 are needed, ~45 at the
+// benchmark's bonds) and Newton-Schulz steps.
+constexpr int TC2_ITERS = 90;
+constexpr int NS_ITERS = 2;
 
 // Pair matrix buffers (hi, lo) carved from the arena.
 struct Pair {
@@ -678,6 +898,8 @@ int oz_round_impl(cudaStream_t st, int n, const double* const* W, const int64_t*
   Pair Vk = take_pair(ar, chi * cmax);
   Sliced Vks = take_sliced(ar, chi, cmax);
   int* perm = ar.take<int>((size_t)cmax);
+  double* dscal = ar.take<double>(2);
+  int* ichoice = ar.take<int>(2);  // purification: [0] the step's choice, [1] converged
   // split-K partials: the largest requirement of the products below
   size_t part_bytes = 0;
   for (int k = 0; k < n; ++k) {
@@ -831,6 +1053,57 @@ int oz_round_impl(cudaStream_t st, int n, const double* const* W, const int64_t*
     SGT_TRY(gemm(c, c, r, 1.f, Yts.mat(), GYs.mat(), 0.f, Z, c));
     pair_symmetrize_kernel<<<grid_for(c * c), 256, 0, st>>>(Z.h, Z.l, c);
     SGT_LAUNCHED();
+    if (!spectra && keep < c) {
+      // ---- kept subspace by purification (no eigenvectors, no spectrum) ----
+      pair_frob_trace_kernel<<<1, 1024, 0, st>>>(Z.h, Z.l, c, dscal, dscal + 1);
+      SGT_LAUNCHED();
+      pair_scale_by_kernel<<<grid_for(c * c), 256, 0, st>>>(Z.h, Z.l, c * c, dscal, VV.h, VV.l);
+      SGT_LAUNCHED();
+      Pair X = VV, X2 = T;
+      SGT_CUDA(cudaMemsetAsync(ichoice, 0, 2 * sizeof(int), st));
+      SGT_CUDA(cudaMemsetAsync(gmax, 0x3f, sizeof(unsigned), st));  // 0.75: not converged
+      for (int it = 0; it < TC2_ITERS; ++it) {
+        SGT_TRY(oz_split_pair(st, X.h, X.l, c, c, c, Vts.s, Vts.e, 1, ichoice + 1));
+        Vts.rows = c;
+        Vts.cols = c;
+        SGT_TRY(oz_gemm(st, c, c, c, 1.f, Vts.mat(), Vts.mat(), 0.f, X2.h, X2.l, c, part, part_floats, err,
+                        ichoice + 1));
+        tc2_choose_kernel<<<1, 512, 0, st>>>(X.h, X.l, X2.h, X2.l, (int)c, (int)keep, ichoice, gmax);
+        SGT_LAUNCHED();
+        tc2_update_kernel<<<grid_for(c * c), 256, 0, st>>>(X.h, X.l, X2.h, X2.l, (int)c, ichoice, gmax);
+        SGT_LAUNCHED();
+      }
+      tc2_status_kernel<<<1, 1, 0, st>>>(ichoice, gmax, stat + k);
+      SGT_LAUNCHED();
+      // basis: Q = L^T X with L the rank-keep pivoted Cholesky factor of X's FP32 part
+      SGT_REQUIRE(c * sizeof(float) <= 48 * 1024, SGT_ERR_INVALID, "mpo_mps_round: bond problem too large");
+      pivoted_chol_kernel<<<1, 1024, c * sizeof(float), st>>>(X.h, (int)c, (int)keep, Vt32, perm);
+      SGT_LAUNCHED();
+      SGT_TRY(oz_split_pair(st, Vt32, nullptr, c, keep, c, Ets.s, Ets.e, 1));
+      Ets.rows = keep;
+      Ets.cols = c;
+      SGT_TRY(split_pair(st, X, c, Vts, c, c));
+      SGT_TRY(gemm(keep, c, c, 1.f, Ets.mat(), Vts.mat(), 0.f, Vk, c));
+      // Newton-Schulz: Q <- 1.5 Q - 0.5 (Q Q^T) Q
+      for (int it = 0; it < NS_ITERS; ++it) {
+        SGT_TRY(split_pair(st, Vk, c, Vks, keep, c));
+        SGT_TRY(gemm(keep, keep, c, 1.f, Vks.mat(), Vks.mat(), 0.f, S, keep));
+        SGT_TRY(split_pair(st, S, keep, Ts, keep, keep));
+        SGT_TRY(pair_transpose(st, Xv, keep, 0, Vk, c, 0, keep, c, 1));
+        SGT_TRY(split_pair(st, Xv, keep, Xvs, c, keep));
+        SGT_TRY(gemm(keep, c, keep, -0.5f, Ts.mat(), Xvs.mat(), 1.5f, Vk, c));
+      }
+      pair_to_f64_kernel<<<grid_for(keep * c), 256, 0, st>>>(Vk.h, Vk.l, c, out[k], c, keep, c);
+      SGT_LAUNCHED();
+      if (discarded) {
+        // discarded weight = 1 - trace(Q Z Q^T) / trace(Z)
+        SGT_TRY(split_pair(st, Vk, c, Vks, keep, c));
+        SGT_TRY(split_pair(st, Z, c, Zs, c, c));
+        SGT_TRY(gemm(keep, c, c, 1.f, Vks.mat(), Zs.mat(), 0.f, S, c));
+        kept_trace_kernel<<<1, 1024, 0, st>>>(S.h, S.l, Vk.h, Vk.l, keep * c, dscal + 1, discarded + (k - 1));
+        SGT_LAUNCHED();
+      }
+    } else {
     // FP32 Jacobi on the leading part of Z: first approximation
     SGT_CUDA(cudaMemcpyAsync(Z32, Z.h, sizeof(float) * c * c, cudaMemcpyDeviceToDevice, st));
     {
@@ -881,6 +1154,7 @@ int oz_round_impl(cudaStream_t st, int n, const double* const* W, const int64_t*
     oz_spectrum_kernel<<<1, 256, 0, st>>>(lamp.h, lamp.l, perm, (int)cnt[k], (int)keep, spec_k,
                                           discarded ? discarded + (k - 1) : nullptr, gexp + k);
     SGT_LAUNCHED();
+    }
     // Ft_k (keep x r) = Vk Y^T with Y = Yt^T (r x c)
     Pair Y = Ytp;  // Ytp is free again
     SGT_TRY(pair_transpose(st, Y, c, 0, Yt, r, 0, c, r, 1));

@@ -99,8 +99,11 @@ inline size_t oz_slice_elems(int64_t rows, int64_t cols) { return (size_t)OZ_SLI
 // may be null) holds the split-K partials when K > OZ_KC or the output has few
 // tiles; oz_gemm_ws_bytes gives the bytes that allow every split the kernel
 // wants.  `err` (device int, may be null) is set when a pipeline wait timed out.
+// `skip` (device int, may be null): when nonzero at launch time the call does
+// nothing (iterations that a device-side test found converged).
 int oz_gemm(cudaStream_t st, int64_t M, int64_t N, int64_t K, float alpha, const OzMat& A, const OzMat& B, float beta,
-            float* Chi, float* Clo, int64_t ldc, float* part, int64_t part_floats, int* err);
+            float* Chi, float* Clo, int64_t ldc, float* part, int64_t part_floats, int* err,
+            const int* skip = nullptr);
 size_t oz_gemm_ws_bytes(int64_t M, int64_t N, int64_t K);
 int oz_profile(int enable, double* ms, double* flops, long long* launches);
 
@@ -108,7 +111,7 @@ int oz_profile(int enable, double* ms, double* flops, long long* launches);
 // may be null) into `out` (oz_slice_elems(rows, cols) bf16, slice stride
 // rows * oz_ld(cols)) with one exponent per row into e[r * estride].
 int oz_split_pair(cudaStream_t st, const float* hi, const float* lo, int64_t ld, int64_t rows, int64_t cols,
-                  __nv_bfloat16* out, int* e, int64_t estride);
+                  __nv_bfloat16* out, int* e, int64_t estride, const int* skip = nullptr);
 // The same from FP64 with general strides: element (r, c) = x[r * rs + c * cs].
 int oz_split_f64(cudaStream_t st, const double* x, int64_t rs, int64_t cs, int64_t rows, int64_t cols,
                  __nv_bfloat16* out, int* e, int64_t estride);

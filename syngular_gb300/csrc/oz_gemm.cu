@@ -167,6 +167,8 @@ struct OzArgs {
   int M, N, K;
   float alpha, beta;
   int kps;  // K-tiles per split
+  int mfast;  // 1: blockIdx.x walks the M tiles (consecutive CTAs share a B tile), 0: the N tiles
+  const int* skip;  // when non-null and nonzero at launch, the launch does nothing
   int* err;
 };
 
@@ -181,6 +183,7 @@ __device__ __forceinline__ void pair_add(float& h, float& l, float v) {
 
 __global__ void __launch_bounds__(OZ_THREADS, 1)
     oz_gemm_kernel(const __grid_constant__ CUtensorMap mA, const __grid_constant__ CUtensorMap mB, const OzArgs args) {
+  if (args.skip && *args.skip) return;  // uniform for the whole grid, before any barrier or TMEM
   extern __shared__ __align__(1024) unsigned char oz_smem_raw[];
   unsigned char* smem = reinterpret_cast<unsigned char*>(
       (reinterpret_cast<uintptr_t>(oz_smem_raw) + 1023) & ~uintptr_t(1023));
@@ -193,7 +196,8 @@ __global__ void __launch_bounds__(OZ_THREADS, 1)
   __shared__ int s_eb[OZ_BN];
 
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int m0 = blockIdx.y * OZ_BM, n0 = blockIdx.x * OZ_BN;
+  const int m0 = (args.mfast ? blockIdx.x : blockIdx.y) * OZ_BM;
+  const int n0 = (args.mfast ? blockIdx.y : blockIdx.x) * OZ_BN;
   const int kt0 = (int)blockIdx.z * args.kps;
   const int KT = min((args.K + OZ_BK - 1) / OZ_BK - kt0, args.kps);
 
@@ -361,9 +365,11 @@ __global__ void __launch_bounds__(OZ_THREADS, 1)
 }
 
 // C = beta C + sum_z part[z] in pair arithmetic, z in order (deterministic).
-__global__ void oz_splitk_sum_kernel(const float* __restrict__ ph, const float* __restrict__ pl, int S, int64_t M,
+__global__ void oz_splitk_sum_kernel(const int* __restrict__ skip, const float* __restrict__ ph,
+                                     const float* __restrict__ pl, int S, int64_t M,
                                      int64_t N, float beta, float* __restrict__ Chi, float* __restrict__ Clo,
                                      int64_t ldc) {
+  if (skip && *skip) return;
   const int64_t mn = M * N;
   for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < mn; i += (int64_t)gridDim.x * blockDim.x) {
     float h = ph[i], l = pl[i];
@@ -386,9 +392,11 @@ __global__ void oz_splitk_sum_kernel(const float* __restrict__ ph, const float* 
 }
 
 // One warp per row: exponent of the row's largest |hi|, then the slices.
-__global__ void oz_split_pair_kernel(const float* __restrict__ hi, const float* __restrict__ lo, int64_t ld,
+__global__ void oz_split_pair_kernel(const int* __restrict__ skip, const float* __restrict__ hi,
+                                     const float* __restrict__ lo, int64_t ld,
                                      int64_t rows, int64_t cols, __nv_bfloat16* __restrict__ out, int64_t ldo,
                                      int64_t sstride, int* __restrict__ ex, int64_t exs) {
+  if (skip && *skip) return;
   const int lane = threadIdx.x & 31;
   const int64_t warps = (int64_t)gridDim.x * (blockDim.x >> 5);
   for (int64_t r = (int64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); r < rows; r += warps) {
@@ -492,7 +500,7 @@ size_t oz_gemm_ws_bytes(int64_t M, int64_t N, int64_t K) {
 }
 
 int oz_gemm(cudaStream_t st, int64_t M, int64_t N, int64_t K, float alpha, const OzMat& A, const OzMat& B, float beta,
-            float* Chi, float* Clo, int64_t ldc, float* part, int64_t part_floats, int* err) {
+            float* Chi, float* Clo, int64_t ldc, float* part, int64_t part_floats, int* err, const int* skip) {
   if (M <= 0 || N <= 0) return SGT_OK;
   SGT_REQUIRE(K > 0, SGT_ERR_INVALID, "oz_gemm: empty K");
   SGT_REQUIRE(M < (1ll << 31) && N < (1ll << 31) && K < (1ll << 31), SGT_ERR_INVALID, "oz_gemm: too large");
@@ -507,7 +515,11 @@ int oz_gemm(cudaStream_t st, int64_t M, int64_t N, int64_t K, float alpha, const
               (long long)M, (long long)N, (long long)K);
   const int KTall = (int)cdiv(K, OZ_BK);
   const int kps = (int)cdiv(KTall, S);
-  OzArgs args{Chi, Clo, ldc, 0, A.e, B.e, A.estride, B.estride, (int)M, (int)N, (int)K, alpha, beta, kps, err};
+  // raster order: the CTAs that share the larger operand's tile run side by
+  // side, so that tile is read from DRAM once (the smaller operand stays in L2)
+  const int mfast = N > M ? 1 : 0;
+  OzArgs args{Chi, Clo, ldc, 0, A.e, B.e, A.estride, B.estride, (int)M, (int)N, (int)K, alpha, beta, kps, mfast,
+              skip, err};
   if (S > 1) {
     args.Chi = part;
     args.Clo = part + (int64_t)S * M * N;
@@ -515,10 +527,12 @@ int oz_gemm(cudaStream_t st, int64_t M, int64_t N, int64_t K, float alpha, const
     args.beta = 0.f;
     args.pstride = M * N;
   }
-  dim3 grid((unsigned)cdiv(N, OZ_BN), (unsigned)cdiv(M, OZ_BM), (unsigned)S);
-  SGT_REQUIRE(grid.y <= 65535, SGT_ERR_INVALID, "oz_gemm: M too large");
+  const unsigned mt = (unsigned)cdiv(M, OZ_BM), nt = (unsigned)cdiv(N, OZ_BN);
+  dim3 grid(mfast ? mt : nt, mfast ? nt : mt, (unsigned)S);
+  SGT_REQUIRE(grid.y <= 65535, SGT_ERR_INVALID, "oz_gemm: too many tiles along %s", mfast ? "N" : "M");
   OzProf rec{};
-  if (g_oz_prof_on) {
+  const bool prof = g_oz_prof_on && !skip;  // a launch that may do nothing is not timed
+  if (prof) {
     SGT_CUDA(cudaEventCreate(&rec.a));
     SGT_CUDA(cudaEventCreate(&rec.b));
     SGT_CUDA(cudaEventRecord(rec.a, st));
@@ -527,10 +541,10 @@ int oz_gemm(cudaStream_t st, int64_t M, int64_t N, int64_t K, float alpha, const
   SGT_LAUNCHED();
   if (S > 1) {
     oz_splitk_sum_kernel<<<(unsigned)std::min<int64_t>(cdiv(M * N, 256), 152 * 8), 256, 0, st>>>(
-        part, part + (int64_t)S * M * N, S, M, N, beta, Chi, Clo, ldc);
+        skip, part, part + (int64_t)S * M * N, S, M, N, beta, Chi, Clo, ldc);
     SGT_LAUNCHED();
   }
-  if (g_oz_prof_on) {
+  if (prof) {
     SGT_CUDA(cudaEventRecord(rec.b, st));
     rec.flops = 2.0 * (double)M * (double)N * (double)K;
     g_oz_prof.push_back(rec);
@@ -539,10 +553,11 @@ int oz_gemm(cudaStream_t st, int64_t M, int64_t N, int64_t K, float alpha, const
 }
 
 int oz_split_pair(cudaStream_t st, const float* hi, const float* lo, int64_t ld, int64_t rows, int64_t cols,
-                  __nv_bfloat16* out, int* e, int64_t estride) {
+                  __nv_bfloat16* out, int* e, int64_t estride, const int* skip) {
   if (rows <= 0 || cols <= 0) return SGT_OK;
   const unsigned g = (unsigned)std::max<int64_t>(1, std::min<int64_t>(cdiv(rows, 8), 152 * 16));
-  oz_split_pair_kernel<<<g, 256, 0, st>>>(hi, lo, ld, rows, cols, out, oz_ld(cols), rows * oz_ld(cols), e, estride);
+  oz_split_pair_kernel<<<g, 256, 0, st>>>(skip, hi, lo, ld, rows, cols, out, oz_ld(cols), rows * oz_ld(cols), e,
+                                          estride);
   SGT_LAUNCHED();
   return SGT_OK;
 }

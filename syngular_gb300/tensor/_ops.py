@@ -248,10 +248,12 @@ def svd_round_shapes(cores: Cores, chi: int):
     return shapes, [cnt[k] for k in range(n - 1)]
 
 
-def svd_round(cores: Cores, chi: int, precision: int = L.PREC_F64):
-    """TT-SVD rounding to ``chi``.  Returns ``(cores, spectra, discarded,
-    status)``: device tensors; ``spectra`` concatenates every bond's singular
-    values (``counts`` gives the split), ``status`` the Jacobi verdict."""
+def svd_round(cores: Cores, chi: int, precision: int = L.PREC_F64, spectra: bool = True):
+    """TT-SVD rounding to ``chi``.  Returns ``(cores, spectra, counts,
+    discarded, status)``: device tensors; ``spectra`` concatenates every bond's
+    singular values (``counts`` gives the split), ``status`` the solver's
+    verdict.  ``spectra=False`` asks for none (returned as None): the BF16X6
+    form then finds each kept subspace without an eigensolve."""
     _check(cores)
     n = len(cores)
     shapes3, counts = svd_round_shapes(cores, chi)
@@ -266,14 +268,14 @@ def svd_round(cores: Cores, chi: int, precision: int = L.PREC_F64):
         l, p, r = shapes3[k]
         outs.append(empty((l,) + tuple(c.shape[1:-1]) + (r,)))
     dev = L.device()
-    spectra = torch.zeros(max(1, sum(counts)), dtype=torch.float64, device=dev)
+    spec = torch.zeros(max(1, sum(counts)), dtype=torch.float64, device=dev) if spectra else None
     disc = torch.zeros(max(1, n - 1), dtype=torch.float64, device=dev)
     status = torch.zeros(1, dtype=torch.int32, device=dev)
     cp, _c = L.ptr_array(cores)
     op, _o = L.ptr_array(outs)
-    L.call("sgt_svd_round", n, cp, sh, chi, precision, op, L.ptr(spectra), L.ptr(disc), L.ptr(status),
-           L.ptr(ws), ws.numel(), L.stream_ptr())
-    return outs, spectra, counts, disc, status
+    L.call("sgt_svd_round", n, cp, sh, chi, precision, op, L.ptr(spec) if spectra else None, L.ptr(disc),
+           L.ptr(status), L.ptr(ws), ws.numel(), L.stream_ptr())
+    return outs, spec, counts, disc, status
 
 
 # ---------------------------------------------------------------------------
@@ -400,9 +402,11 @@ def eig_method(method: int = 0) -> int:
     return int(L.load().sgt_eig_method(int(method)))
 
 
-def mpo_mps_round(W: Cores, X: Cores, chi: int, precision: int = L.PREC_F64):
+def mpo_mps_round(W: Cores, X: Cores, chi: int, precision: int = L.PREC_F64, spectra: bool = True):
     """Raw ``W @ X`` followed by TT-SVD rounding to ``chi`` in one library call.
-    Returns ``(cores, spectra, counts, discarded, status)`` (device tensors)."""
+    Returns ``(cores, spectra, counts, discarded, status)`` (device tensors);
+    ``spectra=False`` asks for none (returned as None), which lets the BF16X6
+    form find each kept subspace without an eigensolve."""
     _check(W)
     _check(X)
     n = len(X)
@@ -421,12 +425,12 @@ def mpo_mps_round(W: Cores, X: Cores, chi: int, precision: int = L.PREC_F64):
     ws = L.workspace(nbytes)
     outs = [empty((out_arr[3 * k], out_arr[3 * k + 1], out_arr[3 * k + 2])) for k in range(n)]
     dev = L.device()
-    spectra = torch.zeros(max(1, sum(counts)), dtype=torch.float64, device=dev)
+    spec = torch.zeros(max(1, sum(counts)), dtype=torch.float64, device=dev) if spectra else None
     disc = torch.zeros(max(1, n - 1), dtype=torch.float64, device=dev)
     status = torch.zeros(1, dtype=torch.int32, device=dev)
     wp, _wp = L.ptr_array(W)
     xp, _xp = L.ptr_array(X)
     op, _o = L.ptr_array(outs)
-    L.call("sgt_mpo_mps_round", n, wp, wsh, xp, xsh, chi, precision, op, L.ptr(spectra), L.ptr(disc),
-           L.ptr(status), L.ptr(ws), ws.numel(), L.stream_ptr())
-    return outs, spectra, counts, disc, status
+    L.call("sgt_mpo_mps_round", n, wp, wsh, xp, xsh, chi, precision, op, L.ptr(spec) if spectra else None,
+           L.ptr(disc), L.ptr(status), L.ptr(ws), ws.numel(), L.stream_ptr())
+    return outs, spec, counts, disc, status

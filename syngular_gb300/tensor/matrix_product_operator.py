@@ -100,7 +100,8 @@ class MatrixProductOperator:
                     if min_bond >= min(s.bond_shape):
                         return s
                     out, _sp, _c, _d, _st = _ops.mpo_mps_round(self.sites, mp.sites, min_bond,
-                                                               precision_code(type(self).PRECISION))
+                                                               precision_code(type(self).PRECISION),
+                                                               spectra=False)
                     return MatrixProductState.from_sites(out)
                 return s >> min_bond if auto else s
             return None
@@ -245,7 +246,8 @@ class MatrixProductOperator:
     def _round(self, cores, dim):
         flat = [c.reshape(c.shape[0], c.shape[1] * c.shape[2], c.shape[3]) for c in cores]
         if type(self).ROUNDING == "svd":
-            out, _spec, _cnt, _disc, _st = _ops.svd_round(flat, dim, precision_code(type(self).PRECISION))
+            out, _spec, _cnt, _disc, _st = _ops.svd_round(flat, dim, precision_code(type(self).PRECISION),
+                                                          spectra=False)
         else:
             out = _ops.qr_truncate(flat, dim)
         return [o.reshape(o.shape[0], c.shape[1], c.shape[2], o.shape[2]) for o, c in zip(out, cores)]

@@ -242,7 +242,7 @@ class MatrixProductState:
                 and type(self).ROUNDING == "svd"):
             # fused raw product + TT-SVD round: the product is never stored
             W, X, prec = self._lazy
-            out, _spec, _cnt, _disc, _st = _ops.mpo_mps_round(W, X, dim, precision_code(prec))
+            out, _spec, _cnt, _disc, _st = _ops.mpo_mps_round(W, X, dim, precision_code(prec), spectra=False)
             return MatrixProductState.from_sites(out)
         that = self.copy()
         if mode == "left":
@@ -254,7 +254,8 @@ class MatrixProductState:
 
     def _round(self, cores, dim):
         if type(self).ROUNDING == "svd":
-            out, _spec, _cnt, _disc, _st = _ops.svd_round(cores, dim, precision_code(type(self).PRECISION))
+            out, _spec, _cnt, _disc, _st = _ops.svd_round(cores, dim, precision_code(type(self).PRECISION),
+                                                          spectra=False)
             return out
         return _ops.qr_truncate(cores, dim)
 

@@ -113,3 +113,24 @@ def test_truncating_chains_golden(golden, case, n, seed, prec_name, tol_ov, tol_
     np.testing.assert_allclose(disc[: n - 1], g(case, "discarded"), rtol=1e-6, atol=1e-14)
     # the middle bonds really truncate (product rank 512 / 1024 > 256)
     assert max(g(case, "discarded")) > 1e-3
+
+
+@pytest.mark.parametrize("case,n,seed", [("n20", 20, 11), ("n24", 24, 12)])
+def test_truncating_chains_golden_without_spectra(golden, case, n, seed):
+    """The BF16X6 form without spectra (kept subspaces by purification, the
+    path of ``(W @ X) >> chi`` through the API) at the benchmark's shapes."""
+    from syngular_gb300 import _lib as L
+    from syngular_gb300.tensor import _ops
+
+    g = golden("config2_cores.npz")
+    X, W = golden_inputs(n, seed)
+    Xd, Wd = dev(X), dev(W)
+    Z, spec, counts, disc, status = _ops.mpo_mps_round(Wd, Xd, CHI, L.PREC_BF16X6, spectra=False)
+    xz = _ops.decode_overlap(_ops.overlap_device(Xd, Z).cpu().tolist())
+    zz = _ops.decode_overlap(_ops.overlap_device(Z, Z).cpu().tolist())
+    torch.cuda.synchronize()
+    assert int(status.item()) >= 0
+    xzr, zzr = decode(g(case, "xz")), decode(g(case, "zz"))
+    assert abs(xz - xzr) / abs(xzr) < 1e-6, (xz, xzr)
+    assert abs(zz - zzr) / abs(zzr) < 1e-6, (zz, zzr)
+    np.testing.assert_allclose(disc.cpu().numpy()[: n - 1], g(case, "discarded"), rtol=1e-6, atol=1e-9)

@@ -150,3 +150,33 @@ def test_bf16x6_svd_round_chain():
     assert abs(ov - ovr) / abs(ovr) < 1e-8
     zz, zzr = _ops.overlap(Z, Z), O.overlap(Zr, Zr)
     assert abs(zz - zzr) / zzr < 1e-9
+
+
+@pytest.mark.parametrize("n,d,chi,D,cut", CASES)
+def test_bf16x6_round_without_spectra(n, d, chi, D, cut):
+    """Without spectra the BF16X6 form finds each kept subspace by purification
+    (no eigensolve): the rounded state, the discarded weights and the right
+    orthonormality of the cores match the FP64 oracle."""
+    from syngular_gb300 import _lib as L
+    from syngular_gb300.tensor import _ops
+
+    rng = np.random.default_rng(1000 * n + chi)
+    X = O.random_mps_cores(rng, n, d, chi)
+    W = O.random_mpo_cores(rng, n, d, D)
+    Zr, spec_r, disc_r = O.tt_svd_round(O.mpo_mps_product(W, X), cut)
+    Z, spec, counts, disc, status = _ops.mpo_mps_round(dev(W), dev(X), cut, L.PREC_BF16X6, spectra=False)
+    torch.cuda.synchronize()
+    assert spec is None and int(status.item()) >= 0
+    assert [tuple(z.shape) for z in Z] == [z.shape for z in Zr]
+    e_ov, e_zz = rel_overlaps(X, Z, Zr)
+    assert e_ov < 1e-6 and e_zz < 1e-6, (e_ov, e_zz)
+    assert e_ov < 1e-8 and e_zz < 1e-9, (e_ov, e_zz)
+    # discarded weights from traces; eigenvalues below ~1e-11 of the largest
+    # sit at the products' own error and may fall on either side of the cut
+    np.testing.assert_allclose(disc.cpu().numpy()[: n - 1], disc_r, rtol=1e-6, atol=1e-9)
+    # right orthonormal cores where the bond truncates (there the kept subspace
+    # is a full-rank projector's range)
+    for k in range(1, n):
+        if disc_r[k - 1] > 1e-9:
+            m = Z[k].reshape(Z[k].shape[0], -1).cpu().numpy()
+            np.testing.assert_allclose(m @ m.T, np.eye(m.shape[0]), rtol=0, atol=1e-10)
