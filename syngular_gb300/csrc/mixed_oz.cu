@@ -29,6 +29,7 @@
 // separately (steps A-D), and the right sweep forms Y_k = P_k F_{k+1} as
 // (F W^T) then X, 2.2e9 instead of 1.7e10 FP64-equivalent flops per site at
 // the benchmark's shapes.
+#include <cooperative_groups.h>
 #include <float.h>
 
 #include <algorithm>
@@ -36,6 +37,8 @@
 
 #include "common.cuh"
 #include "oz.cuh"
+
+namespace cg = cooperative_groups;
 
 namespace sgt {
 
@@ -542,27 +545,69 @@ __global__ void axpby_pair_f64_kernel(const float* __restrict__ h, const float* 
 // gauge choice), so this replaces the eigensolve when no spectrum is wanted.
 // ---------------------------------------------------------------------------
 
-// out = sum of squares of h (double); one block
-__global__ void pair_frob_trace_kernel(const float* __restrict__ h, const float* __restrict__ l, int64_t n,
-                                       double* __restrict__ frob, double* __restrict__ trace) {
-  __shared__ double red[2][32];
-  double ss = 0.0, tr = 0.0;
-  for (int64_t i = threadIdx.x; i < n * n; i += blockDim.x) {
-    const double v = (double)h[i];
-    ss += v * v;
-    if (i / n == i % n) tr += v + (double)l[i];
+// Deterministic grid reductions: every block writes its partial sums, and the
+// last block to finish (an atomic ticket, reset for the next launch) adds them
+// in block order.  RED_BLOCKS blocks of 256 threads.
+constexpr int RED_BLOCKS = 2 * 152;
+
+template <int NV>
+__device__ __forceinline__ void block_sums(double (&v)[NV], double (*red)[32]) {
+#pragma unroll
+  for (int q = 0; q < NV; ++q) {
+    for (int o = 16; o > 0; o >>= 1) v[q] += __shfl_xor_sync(0xffffffffu, v[q], o);
+    if ((threadIdx.x & 31) == 0) red[q][threadIdx.x >> 5] = v[q];
   }
-  for (int o = 16; o > 0; o >>= 1) {
-    ss += __shfl_xor_sync(0xffffffffu, ss, o);
-    tr += __shfl_xor_sync(0xffffffffu, tr, o);
-  }
-  if ((threadIdx.x & 31) == 0) red[0][threadIdx.x >> 5] = ss, red[1][threadIdx.x >> 5] = tr;
   __syncthreads();
   if (threadIdx.x == 0) {
-    double a = 0.0, b = 0.0;
-    for (int w = 0; w < (int)(blockDim.x >> 5); ++w) a += red[0][w], b += red[1][w];
-    *frob = sqrt(a);
-    *trace = b;
+#pragma unroll
+    for (int q = 0; q < NV; ++q) {
+      double a = 0.0;
+      for (int w = 0; w < (int)(blockDim.x >> 5); ++w) a += red[q][w];
+      v[q] = a;
+    }
+  }
+}
+
+// thread 0 of the last block returns true with the grid totals in v
+template <int NV>
+__device__ __forceinline__ bool grid_sums(double (&v)[NV], double* __restrict__ part, unsigned* __restrict__ ticket) {
+  __shared__ double red[NV][32];
+  __shared__ bool s_last;
+  block_sums<NV>(v, red);
+  if (threadIdx.x == 0) {
+#pragma unroll
+    for (int q = 0; q < NV; ++q) part[(int64_t)blockIdx.x * NV + q] = v[q];
+    __threadfence();
+    s_last = atomicAdd(ticket, 1u) == gridDim.x - 1;
+  }
+  __syncthreads();
+  if (!s_last || threadIdx.x != 0) return false;
+  __threadfence();
+#pragma unroll
+  for (int q = 0; q < NV; ++q) {
+    double a = 0.0;
+    for (unsigned b = 0; b < gridDim.x; ++b) a += __ldcg(part + (int64_t)b * NV + q);
+    v[q] = a;
+  }
+  *ticket = 0u;
+  return true;
+}
+
+// |h|_F (double) and trace(h + l) of a pair matrix (n x n)
+__global__ void __launch_bounds__(256) pair_frob_trace_kernel(const float* __restrict__ h, const float* __restrict__ l,
+                                                              int64_t n, double* __restrict__ part,
+                                                              unsigned* __restrict__ ticket,
+                                                              double* __restrict__ frob, double* __restrict__ trace) {
+  double v[2] = {0.0, 0.0};
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x, t0 = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  for (int64_t i = t0; i < n * n; i += stride) {
+    const double a = (double)h[i];
+    v[0] += a * a;
+  }
+  for (int64_t i = t0; i < n; i += stride) v[1] += (double)h[i * n + i] + (double)l[i * n + i];
+  if (grid_sums<2>(v, part, ticket)) {
+    *frob = sqrt(v[0]);
+    *trace = v[1];
   }
 }
 
@@ -713,22 +758,141 @@ __global__ void __launch_bounds__(1024) pivoted_chol_kernel(const float* __restr
   }
 }
 
-// disc = 1 - sum_j (T[j] . Q[j]) / trace(Z)   (T = Q Z, rows of Q the kept basis)
-__global__ void kept_trace_kernel(const float* __restrict__ th, const float* __restrict__ tl,
-                                  const float* __restrict__ qh, const float* __restrict__ ql, int64_t count,
-                                  const double* __restrict__ trace_z, double* __restrict__ disc) {
-  __shared__ double red[32];
-  double s = 0.0;
-  for (int64_t i = threadIdx.x; i < count; i += blockDim.x)
-    s += ((double)th[i] + (double)tl[i]) * ((double)qh[i] + (double)ql[i]);
-  for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
-  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = s;
+// The same factorisation across one cluster of PC_CS CTAs (the kernel above
+// is the fallback where this one does not fit).  CTA b owns rows
+// [b R, b R + R) of A and of L and keeps its slice of L in shared memory
+// (column t of its rows at Ls[t Rp + r]), so a step reads no global memory but
+// its part of A's pivot row (A is symmetric).  A step:
+//   1. every warp reads the PC_CS published candidates (remaining diagonal,
+//      row) over distributed shared memory and takes the largest, ties to the
+//      lowest row: the pivot p, owned by CTA p / R;
+//   2. the pivot's row of L (columns < s) is copied from the owner's shared
+//      memory, where it was published with the candidate;
+//   3. group g of the CTA's threads forms the partial dot products of its rows
+//      with that row over the columns t = g (mod G), group 0 adds them in
+//      order, writes column s of L and lowers the remaining diagonal;
+//   4. the CTA publishes its next candidate and that row of L (double
+//      buffered by step parity), and the cluster barrier releases them.
+// Candidates are 64-bit keys (order-preserving value bits, then the
+// complemented row), so the largest key is the largest value at the lowest
+// row, as in the one-block kernel.
+constexpr int PC_CS = 16;
+constexpr int PC_THREADS = 512;
+
+__device__ __forceinline__ unsigned long long pc_key(float v, int row) {
+  unsigned u = __float_as_uint(v);
+  u = (u & 0x80000000u) ? ~u : (u | 0x80000000u);
+  return ((unsigned long long)u << 32) | (unsigned)(~(unsigned)row);
+}
+__device__ __forceinline__ float pc_key_value(unsigned long long k) {
+  unsigned u = (unsigned)(k >> 32);
+  u = (u & 0x80000000u) ? (u & 0x7fffffffu) : ~u;
+  return __uint_as_float(u);
+}
+__device__ __forceinline__ int pc_key_row(unsigned long long k) { return (int)(~(unsigned)(k & 0xffffffffu)); }
+__device__ __forceinline__ unsigned long long pc_warp_max(unsigned long long k) {
+  for (int o = 16; o > 0; o >>= 1) {
+    const unsigned long long x = __shfl_xor_sync(0xffffffffu, k, o);
+    k = x > k ? x : k;
+  }
+  return k;
+}
+
+__global__ void __launch_bounds__(PC_THREADS) pivoted_chol_cluster_kernel(const float* __restrict__ A, int c,
+                                                                          int keep, int R, int Rp,
+                                                                          float* __restrict__ Lt) {
+  cg::cluster_group cluster = cg::this_cluster();
+  extern __shared__ float pcs[];
+  const int G = PC_THREADS / Rp;
+  float* Ls = pcs;                             // keep x Rp
+  float* part = Ls + (int64_t)keep * Rp;       // G x Rp
+  float* diag = part + (int64_t)G * Rp;        // Rp
+  float* prow = diag + Rp;                     // keep
+  float* crow = prow + keep;                   // 2 x keep: published candidate rows
+  int* used = reinterpret_cast<int*>(crow + 2 * keep);  // Rp
+  __shared__ unsigned long long s_key[2];
+  __shared__ unsigned long long s_wkey[PC_THREADS / 32];
+  const int tid = threadIdx.x, r = tid % Rp, g = tid / Rp, lane = tid & 31, warp = tid >> 5;
+  const int row0 = (int)cluster.block_rank() * R;
+  const int nrows = max(0, min(R, c - row0));
+  const int nw = Rp / 32;
+  for (int i = tid; i < Rp; i += PC_THREADS) {
+    diag[i] = i < nrows ? A[(int64_t)(row0 + i) * c + row0 + i] : 0.f;
+    used[i] = i < nrows ? 0 : 1;
+  }
   __syncthreads();
-  if (threadIdx.x == 0) {
-    double a = 0.0;
-    for (int w = 0; w < (int)(blockDim.x >> 5); ++w) a += red[w];
+  // this CTA's candidate for step 0
+  if (g == 0) {
+    unsigned long long k = pc_key(used[r] ? -INFINITY : diag[r], row0 + r);
+    k = pc_warp_max(k);
+    if (lane == 0) s_wkey[warp] = k;
+  }
+  __syncthreads();
+  if (tid == 0) {
+    unsigned long long k = 0ull;
+    for (int w = 0; w < nw; ++w) k = s_wkey[w] > k ? s_wkey[w] : k;
+    s_key[0] = k;
+  }
+  cluster.sync();
+  for (int s = 0; s < keep; ++s) {
+    const int cb = s & 1, nb = cb ^ 1;
+    // 1. the pivot
+    unsigned long long k = 0ull;
+    if (lane < PC_CS) k = *cluster.map_shared_rank(&s_key[cb], lane);
+    k = pc_warp_max(k);
+    const int p = pc_key_row(k);
+    const int owner = p / R;
+    const float inv = 1.f / sqrtf(fmaxf(pc_key_value(k), 1e-30f));
+    // 2. the pivot's row of L; this CTA's part of A's pivot row
+    const float* orow = cluster.map_shared_rank(crow + cb * keep, owner);
+    for (int t = tid; t < s; t += PC_THREADS) prow[t] = orow[t];
+    const float a = (g == 0 && r < nrows) ? A[(int64_t)p * c + row0 + r] : 0.f;
+    __syncthreads();
+    // 3. partial dot products, then column s
+    if (r < nrows) {
+      float acc = 0.f;
+      for (int t = g; t < s; t += G) acc = fmaf(Ls[(int64_t)t * Rp + r], prow[t], acc);
+      part[g * Rp + r] = acc;
+    }
+    __syncthreads();
+    if (g == 0) {
+      if (r < nrows) {
+        float sum = 0.f;
+        for (int q = 0; q < G; ++q) sum += part[q * Rp + r];
+        const float l = (a - sum) * inv;
+        Ls[(int64_t)s * Rp + r] = l;
+        Lt[(int64_t)s * c + row0 + r] = l;
+        diag[r] -= l * l;
+        if (row0 + r == p) used[r] = 1;
+      }
+      unsigned long long kk = pc_key(used[r] ? -INFINITY : diag[r], row0 + r);
+      kk = pc_warp_max(kk);
+      if (lane == 0) s_wkey[warp] = kk;
+    }
+    __syncthreads();
+    // 4. publish the next candidate with its row of L (columns <= s)
+    unsigned long long kn = 0ull;
+    for (int w = 0; w < nw; ++w) kn = s_wkey[w] > kn ? s_wkey[w] : kn;
+    const int lr = pc_key_row(kn) - row0;
+    if (tid == 0) s_key[nb] = kn;
+    if (lr >= 0 && lr < Rp)
+      for (int t = tid; t <= s; t += PC_THREADS) crow[nb * keep + t] = Ls[(int64_t)t * Rp + lr];
+    cluster.sync();
+  }
+}
+
+// disc = 1 - sum_j (T[j] . Q[j]) / trace(Z)   (T = Q Z, rows of Q the kept basis)
+__global__ void __launch_bounds__(256) kept_trace_kernel(const float* __restrict__ th, const float* __restrict__ tl,
+                                                         const float* __restrict__ qh, const float* __restrict__ ql,
+                                                         int64_t count, const double* __restrict__ trace_z,
+                                                         double* __restrict__ part, unsigned* __restrict__ ticket,
+                                                         double* __restrict__ disc) {
+  double v[1] = {0.0};
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < count; i += (int64_t)gridDim.x * blockDim.x)
+    v[0] += ((double)th[i] + (double)tl[i]) * ((double)qh[i] + (double)ql[i]);
+  if (grid_sums<1>(v, part, ticket)) {
     const double tz = *trace_z;
-    *disc = tz > 0.0 ? fmax(0.0, 1.0 - a / tz) : 0.0;
+    *disc = tz > 0.0 ? fmax(0.0, 1.0 - v[0] / tz) : 0.0;
   }
 }
 
@@ -737,6 +901,47 @@ __global__ void kept_trace_kernel(const float* __restrict__ th, const float* __r
 __global__ void tc2_status_kernel(const int* __restrict__ ctl, const unsigned* __restrict__ resid,
                                   int* __restrict__ st) {
   *st = (ctl[1] || __uint_as_float(*resid) <= ldexpf(1.f, -30)) ? 0 : -1;
+}
+
+// Rank-keep pivoted Cholesky factor Lt (keep x c) of the FP32 projector A
+// (c x c): the cluster kernel where it fits, else the one-block kernel.
+int pivoted_chol(cudaStream_t st, const float* A, int64_t c, int64_t keep, float* Lt, int* used) {
+  const int64_t R = cdiv(c, (int64_t)PC_CS);
+  int64_t Rp = 32;
+  while (Rp < R) Rp *= 2;
+  const size_t smem =
+      sizeof(float) * ((size_t)keep * (size_t)(Rp + 3) + (size_t)Rp * (size_t)(PC_THREADS / Rp + 2));
+  if (c >= 2 * PC_CS && Rp <= PC_THREADS && smem <= 200 * 1024) {
+    bool ok = func_attr_at_least((const void*)pivoted_chol_cluster_kernel,
+                                 cudaFuncAttributeNonPortableClusterSizeAllowed, 1) == cudaSuccess &&
+              func_attr_at_least((const void*)pivoted_chol_cluster_kernel,
+                                 cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) == cudaSuccess;
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(PC_CS, 1, 1);
+    cfg.blockDim = dim3(PC_THREADS, 1, 1);
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = st;
+    cudaLaunchAttribute at[1];
+    at[0].id = cudaLaunchAttributeClusterDimension;
+    at[0].val.clusterDim.x = PC_CS;
+    at[0].val.clusterDim.y = 1;
+    at[0].val.clusterDim.z = 1;
+    cfg.attrs = at;
+    cfg.numAttrs = 1;
+    int clusters = 0;
+    ok = ok && cudaOccupancyMaxActiveClusters(&clusters, pivoted_chol_cluster_kernel, &cfg) == cudaSuccess &&
+         clusters >= 1;
+    if (ok) {
+      SGT_CUDA(cudaLaunchKernelEx(&cfg, pivoted_chol_cluster_kernel, A, (int)c, (int)keep, (int)R, (int)Rp, Lt));
+      note_launch();
+      return SGT_OK;
+    }
+    cudaGetLastError();  // not here: the one-block kernel
+  }
+  SGT_REQUIRE(c * sizeof(float) <= 48 * 1024, SGT_ERR_INVALID, "mpo_mps_round: bond problem too large");
+  pivoted_chol_kernel<<<1, 1024, c * sizeof(float), st>>>(A, (int)c, (int)keep, Lt, used);
+  SGT_LAUNCHED();
+  return SGT_OK;
 }
 
 struct Site4 {
@@ -900,6 +1105,8 @@ int oz_round_impl(cudaStream_t st, int n, const double* const* W, const int64_t*
   int* perm = ar.take<int>((size_t)cmax);
   double* dscal = ar.take<double>(2);
   int* ichoice = ar.take<int>(2);  // purification: [0] the step's choice, [1] converged
+  double* rpart = ar.take<double>(2 * RED_BLOCKS);
+  unsigned* ticket = ar.take<unsigned>(1);
   // split-K partials: the largest requirement of the products below
   size_t part_bytes = 0;
   for (int k = 0; k < n; ++k) {
@@ -931,6 +1138,7 @@ int oz_round_impl(cudaStream_t st, int n, const double* const* W, const int64_t*
   if (ar.measure) return SGT_OK;
   SGT_REQUIRE(ar.ok(), SGT_ERR_WORKSPACE, "mpo_mps_round: workspace too small");
   SGT_CUDA(cudaMemsetAsync(stat, 0, sizeof(int) * (n + 1), st));
+  SGT_CUDA(cudaMemsetAsync(ticket, 0, sizeof(unsigned), st));
   SGT_CUDA(cudaMemsetAsync(err, 0, sizeof(int), st));
   SGT_CUDA(cudaMemsetAsync(gexp, 0, sizeof(int) * (n + 1), st));
 
@@ -1055,7 +1263,7 @@ int oz_round_impl(cudaStream_t st, int n, const double* const* W, const int64_t*
     SGT_LAUNCHED();
     if (!spectra && keep < c) {
       // ---- kept subspace by purification (no eigenvectors, no spectrum) ----
-      pair_frob_trace_kernel<<<1, 1024, 0, st>>>(Z.h, Z.l, c, dscal, dscal + 1);
+      pair_frob_trace_kernel<<<RED_BLOCKS, 256, 0, st>>>(Z.h, Z.l, c, rpart, ticket, dscal, dscal + 1);
       SGT_LAUNCHED();
       pair_scale_by_kernel<<<grid_for(c * c), 256, 0, st>>>(Z.h, Z.l, c * c, dscal, VV.h, VV.l);
       SGT_LAUNCHED();
@@ -1076,9 +1284,7 @@ int oz_round_impl(cudaStream_t st, int n, const double* const* W, const int64_t*
       tc2_status_kernel<<<1, 1, 0, st>>>(ichoice, gmax, stat + k);
       SGT_LAUNCHED();
       // basis: Q = L^T X with L the rank-keep pivoted Cholesky factor of X's FP32 part
-      SGT_REQUIRE(c * sizeof(float) <= 48 * 1024, SGT_ERR_INVALID, "mpo_mps_round: bond problem too large");
-      pivoted_chol_kernel<<<1, 1024, c * sizeof(float), st>>>(X.h, (int)c, (int)keep, Vt32, perm);
-      SGT_LAUNCHED();
+      SGT_TRY(pivoted_chol(st, X.h, c, keep, Vt32, perm));
       SGT_TRY(oz_split_pair(st, Vt32, nullptr, c, keep, c, Ets.s, Ets.e, 1));
       Ets.rows = keep;
       Ets.cols = c;
@@ -1100,7 +1306,8 @@ int oz_round_impl(cudaStream_t st, int n, const double* const* W, const int64_t*
         SGT_TRY(split_pair(st, Vk, c, Vks, keep, c));
         SGT_TRY(split_pair(st, Z, c, Zs, c, c));
         SGT_TRY(gemm(keep, c, c, 1.f, Vks.mat(), Zs.mat(), 0.f, S, c));
-        kept_trace_kernel<<<1, 1024, 0, st>>>(S.h, S.l, Vk.h, Vk.l, keep * c, dscal + 1, discarded + (k - 1));
+        kept_trace_kernel<<<RED_BLOCKS, 256, 0, st>>>(S.h, S.l, Vk.h, Vk.l, keep * c, dscal + 1, rpart, ticket,
+                                                       discarded + (k - 1));
         SGT_LAUNCHED();
       }
     } else {
