@@ -626,80 +626,105 @@ __global__ void pair_scale_by_kernel(const float* __restrict__ zh, const float* 
   }
 }
 
-// TC2 decision from the traces of X and X^2 (one block): choice = 1 for X^2,
-// 0 for 2X - X^2.  ctl[1] (done) is set once the previous step's largest
-// |X^2 - X| (resid) fell to 2^-34: X is then a projector to the products'
-// accuracy, and every later step of the loop returns at once.
-__global__ void tc2_choose_kernel(const float* __restrict__ xh, const float* __restrict__ xl,
-                                  const float* __restrict__ x2h, const float* __restrict__ x2l, int n, int keep,
-                                  int* __restrict__ ctl, unsigned* __restrict__ resid) {
-  __shared__ double red[2][32];
-  __shared__ int s_done;
-  if (threadIdx.x == 0) {
-    s_done = ctl[1];
-    if (!s_done && __uint_as_float(*resid) <= ldexpf(1.f, -34)) s_done = ctl[1] = 1;
-  }
-  __syncthreads();
-  if (s_done) return;
-  double t = 0.0, t2 = 0.0;
-  for (int i = threadIdx.x; i < n; i += blockDim.x) {
-    const int64_t d = (int64_t)i * n + i;
-    t += (double)xh[d] + (double)xl[d];
-    t2 += (double)x2h[d] + (double)x2l[d];
-  }
-  for (int o = 16; o > 0; o >>= 1) {
-    t += __shfl_xor_sync(0xffffffffu, t, o);
-    t2 += __shfl_xor_sync(0xffffffffu, t2, o);
-  }
-  if ((threadIdx.x & 31) == 0) red[0][threadIdx.x >> 5] = t, red[1][threadIdx.x >> 5] = t2;
-  __syncthreads();
-  if (threadIdx.x == 0) {
+// One purification step after X2 = X X (the sliced GEMM), fused: the TC2
+// choice from trace(X) (dcur: X's diagonal, hi then lo, written by the
+// previous step) and trace(X2); X <- X2 or 2X - X2 in place, a warp per row;
+// the largest |X2 - X| into resid[t]; the new diagonal into dnext; and the
+// slices of the new X for the next product, in oz_split_pair's layout (row
+// exponent from the row's largest |hi|, zero padding to ldo).  X2 is
+// symmetric to the level-4 rounding of the sliced product (~2^-50), so rows
+// are updated independently and X is symmetrised once after the loop.  The
+// last block to finish (atomic ticket, reset for the next launch) sets ctl[1]
+// when resid[t] <= 2^-34: X was a projector to the products' accuracy, and
+// every later step returns at once, as do the products (skip flag ctl[1]).
+__global__ void __launch_bounds__(256) tc2_step_kernel(float* __restrict__ xh, float* __restrict__ xl,
+                                                       const float* __restrict__ x2h, const float* __restrict__ x2l,
+                                                       int n, int keep, const float* __restrict__ dcur,
+                                                       float* __restrict__ dnext, int* __restrict__ ctl,
+                                                       unsigned* __restrict__ resid, unsigned* __restrict__ ticket,
+                                                       __nv_bfloat16* __restrict__ out, int64_t ldo, int64_t sstride,
+                                                       int* __restrict__ ex) {
+  __shared__ double red[2][8];
+  __shared__ int s_ch;
+  __shared__ bool s_last;
+  if (ctl[1]) return;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  {
     double a = 0.0, b = 0.0;
-    for (int w = 0; w < (int)(blockDim.x >> 5); ++w) a += red[0][w], b += red[1][w];
-    ctl[0] = fabs(b - keep) < fabs(2.0 * a - b - keep) ? 1 : 0;
-    *resid = 0u;  // this step's update records its own largest |X^2 - X|
+    for (int i = threadIdx.x; i < n; i += blockDim.x) {
+      const int64_t d = (int64_t)i * n + i;
+      a += (double)dcur[i] + (double)dcur[n + i];
+      b += (double)x2h[d] + (double)x2l[d];
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+      a += __shfl_xor_sync(0xffffffffu, a, o);
+      b += __shfl_xor_sync(0xffffffffu, b, o);
+    }
+    if (lane == 0) red[0][warp] = a, red[1][warp] = b;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      double ta = 0.0, tb = 0.0;
+      for (int w = 0; w < (int)(blockDim.x >> 5); ++w) ta += red[0][w], tb += red[1][w];
+      s_ch = fabs(tb - keep) < fabs(2.0 * ta - tb - keep) ? 1 : 0;
+    }
+    __syncthreads();
+  }
+  const int ch = s_ch;
+  float worst = 0.f;
+  const int64_t warps = (int64_t)gridDim.x * (blockDim.x >> 5);
+  for (int64_t r = (int64_t)blockIdx.x * (blockDim.x >> 5) + warp; r < n; r += warps) {
+    float mx = 0.f;
+    for (int64_t c = lane; c < n; c += 32) {
+      const int64_t i = r * n + c;
+      const float h2 = x2h[i], l2 = x2l[i];
+      float h = xh[i], l = xl[i];
+      worst = fmaxf(worst, fabsf((h2 - h) + (l2 - l)));
+      if (ch) {
+        h = h2;
+        l = l2;
+      } else {  // 2X - X^2
+        h *= 2.f;
+        l *= 2.f;
+        df_add(h, l, -h2, -l2);
+      }
+      xh[i] = h;
+      xl[i] = l;
+      mx = fmaxf(mx, fabsf(h));
+      if (c == r) dnext[r] = h, dnext[n + r] = l;
+    }
+    for (int o = 16; o > 0; o >>= 1) mx = fmaxf(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+    int e = 0;
+    if (mx > 0.f && isfinite(mx)) frexpf(mx, &e);
+    if (lane == 0) ex[r] = e;
+    // each lane re-reads only the elements it wrote above
+    for (int64_t c = lane; c < n; c += 32) {
+      const int64_t i = r * n + c;
+      slice_store(ldexpf(xh[i], 6 - e), ldexpf(xl[i], 6 - e), out, sstride, r * ldo + c);
+    }
+    for (int64_t c = n + lane; c < ldo; c += 32) slice_zero(out, sstride, r * ldo + c);
+  }
+  for (int o = 16; o > 0; o >>= 1) worst = fmaxf(worst, __shfl_xor_sync(0xffffffffu, worst, o));
+  if (lane == 0 && worst > 0.f) atomicMax(resid, __float_as_uint(worst));
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    __threadfence();
+    s_last = atomicAdd(ticket, 1u) == gridDim.x - 1;
+  }
+  __syncthreads();
+  if (s_last && threadIdx.x == 0) {
+    __threadfence();
+    if (__uint_as_float(atomicAdd(resid, 0u)) <= ldexpf(1.f, -34)) ctl[1] = 1;
+    *ticket = 0u;
   }
 }
 
-// X <- X^2 or 2X - X^2 (pair), symmetrised; |X^2 - X| max into resid (bits)
-__global__ void tc2_update_kernel(float* __restrict__ xh, float* __restrict__ xl, const float* __restrict__ x2h,
-                                  const float* __restrict__ x2l, int n, const int* __restrict__ ctl,
-                                  unsigned* __restrict__ resid) {
-  if (ctl[1]) return;
-  const int ch = ctl[0];
-  float worst = 0.f;
-  for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < (int64_t)n * n;
-       t += (int64_t)gridDim.x * blockDim.x) {
-    const int i = (int)(t / n), j = (int)(t % n);
-    if (j < i) continue;
-    const int64_t a = (int64_t)i * n + j, b = (int64_t)j * n + i;
-    float vh[2], vl[2];
-    const int64_t idx[2] = {a, b};
-#pragma unroll
-    for (int q = 0; q < 2; ++q) {
-      float h2 = x2h[idx[q]], l2 = x2l[idx[q]];
-      worst = fmaxf(worst, fabsf((h2 - xh[idx[q]]) + (l2 - xl[idx[q]])));
-      if (ch) {
-        vh[q] = h2;
-        vl[q] = l2;
-      } else {  // 2X - X^2
-        float h = 2.f * xh[idx[q]], l = 2.f * xl[idx[q]];
-        df_add(h, l, -h2, -l2);
-        vh[q] = h;
-        vl[q] = l;
-      }
-    }
-    float h = vh[0], l = vl[0];
-    df_add(h, l, vh[1], vl[1]);
-    h *= 0.5f;
-    l *= 0.5f;
-    xh[a] = h;
-    xl[a] = l;
-    xh[b] = h;
-    xl[b] = l;
+// diagonal of a pair matrix (n x n) into d (hi then lo)
+__global__ void pair_diag_kernel(const float* __restrict__ h, const float* __restrict__ l, int n,
+                                 float* __restrict__ d) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    d[i] = h[(int64_t)i * n + i];
+    d[n + i] = l[(int64_t)i * n + i];
   }
-  for (int o = 16; o > 0; o >>= 1) worst = fmaxf(worst, __shfl_xor_sync(0xffffffffu, worst, o));
-  if ((threadIdx.x & 31) == 0 && worst > 0.f) atomicMax(resid, __float_as_uint(worst));
 }
 
 // Pivoted Cholesky of the purified projector's FP32 part, stopped at rank
@@ -1107,6 +1132,8 @@ int oz_round_impl(cudaStream_t st, int n, const double* const* W, const int64_t*
   int* ichoice = ar.take<int>(2);  // purification: [0] the step's choice, [1] converged
   double* rpart = ar.take<double>(2 * RED_BLOCKS);
   unsigned* ticket = ar.take<unsigned>(1);
+  unsigned* tc2_resid = ar.take<unsigned>(TC2_ITERS);  // purification: largest |X^2 - X| of each step
+  float* tc2_diag = ar.take<float>((size_t)(4 * cmax));  // purification: X's diagonal, two buffers
   // split-K partials: the largest requirement of the products below
   size_t part_bytes = 0;
   for (int k = 0; k < n; ++k) {
@@ -1269,19 +1296,24 @@ int oz_round_impl(cudaStream_t st, int n, const double* const* W, const int64_t*
       SGT_LAUNCHED();
       Pair X = VV, X2 = T;
       SGT_CUDA(cudaMemsetAsync(ichoice, 0, 2 * sizeof(int), st));
-      SGT_CUDA(cudaMemsetAsync(gmax, 0x3f, sizeof(unsigned), st));  // 0.75: not converged
+      SGT_CUDA(cudaMemsetAsync(tc2_resid, 0, sizeof(unsigned) * TC2_ITERS, st));
+      pair_diag_kernel<<<grid_for(c), 256, 0, st>>>(X.h, X.l, (int)c, tc2_diag);
+      SGT_LAUNCHED();
+      SGT_TRY(oz_split_pair(st, X.h, X.l, c, c, c, Vts.s, Vts.e, 1));
+      Vts.rows = c;
+      Vts.cols = c;
+      const unsigned sg = (unsigned)std::min<int64_t>(cdiv(c, 8), 152 * 4);
       for (int it = 0; it < TC2_ITERS; ++it) {
-        SGT_TRY(oz_split_pair(st, X.h, X.l, c, c, c, Vts.s, Vts.e, 1, ichoice + 1));
-        Vts.rows = c;
-        Vts.cols = c;
         SGT_TRY(oz_gemm(st, c, c, c, 1.f, Vts.mat(), Vts.mat(), 0.f, X2.h, X2.l, c, part, part_floats, err,
                         ichoice + 1));
-        tc2_choose_kernel<<<1, 512, 0, st>>>(X.h, X.l, X2.h, X2.l, (int)c, (int)keep, ichoice, gmax);
-        SGT_LAUNCHED();
-        tc2_update_kernel<<<grid_for(c * c), 256, 0, st>>>(X.h, X.l, X2.h, X2.l, (int)c, ichoice, gmax);
+        tc2_step_kernel<<<sg, 256, 0, st>>>(X.h, X.l, X2.h, X2.l, (int)c, (int)keep, tc2_diag + (it & 1) * 2 * c,
+                                             tc2_diag + ((it + 1) & 1) * 2 * c, ichoice, tc2_resid + it, ticket,
+                                             Vts.s, oz_ld(c), c * oz_ld(c), Vts.e);
         SGT_LAUNCHED();
       }
-      tc2_status_kernel<<<1, 1, 0, st>>>(ichoice, gmax, stat + k);
+      tc2_status_kernel<<<1, 1, 0, st>>>(ichoice, tc2_resid + (TC2_ITERS - 1), stat + k);
+      SGT_LAUNCHED();
+      pair_symmetrize_kernel<<<grid_for(c * c), 256, 0, st>>>(X.h, X.l, c);
       SGT_LAUNCHED();
       // basis: Q = L^T X with L the rank-keep pivoted Cholesky factor of X's FP32 part
       SGT_TRY(pivoted_chol(st, X.h, c, keep, Vt32, perm));
