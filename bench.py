@@ -843,55 +843,60 @@ def run_hbm(args):
 
     out = {"metric": "HBM-bound kernels: achieved GB/s of algorithmic bytes", "unit": "GB/s",
            "peak_hbm_gbs": hbm, "steps": args.steps, "warmup": max(args.warmup, 1), "kernels": {}}
+    want = set(args.hbm_kernels.split(","))
     # contract
-    X = L.as_device(rng.standard_normal((256, 2, 256)) / 16.0)
-    W = L.as_device(rng.standard_normal((16, 2, 2, 16)) / 6.0)
-    ms = timed(lambda: _ops.contract_mpo_mps([W], [X]))
-    by = 4096 * 2 * 4096 * 8 + X.numel() * 8 + W.numel() * 8
-    out["kernels"]["contract_mpo_mps_kernel"] = {"ms": ms, "bytes": by, "gbs": by / ms / 1e6,
-                                                 "frac": by / ms / 1e6 / hbm}
+    if "contract" in want:
+        X = L.as_device(rng.standard_normal((256, 2, 256)) / 16.0)
+        W = L.as_device(rng.standard_normal((16, 2, 2, 16)) / 6.0)
+        ms = timed(lambda: _ops.contract_mpo_mps([W], [X]))
+        by = 4096 * 2 * 4096 * 8 + X.numel() * 8 + W.numel() * 8
+        out["kernels"]["contract_mpo_mps_kernel"] = {"ms": ms, "bytes": by, "gbs": by / ms / 1e6,
+                                                     "frac": by / ms / 1e6 / hbm}
     # concat (config 4 shapes)
-    A, B = config4_inputs()
-    Ad = [L.as_device(c) for c in A]
-    Bd = [L.as_device(c) for c in B]
-    outs = _ops.concat(Ad, Bd)
-    by = sum(o.numel() for o in outs) * 8 + sum(c.numel() for c in Ad + Bd) * 8
-    del outs
-    ms = timed(lambda: _ops.concat(Ad, Bd))
-    out["kernels"]["concat_kernel"] = {"ms": ms, "bytes": by, "gbs": by / ms / 1e6, "frac": by / ms / 1e6 / hbm,
-                                       "note": "one launch for all 32 sites (zero blocks written too)"}
-    del Ad, Bd
+    if "concat" in want:
+        A, B = config4_inputs()
+        Ad = [L.as_device(c) for c in A]
+        Bd = [L.as_device(c) for c in B]
+        outs = _ops.concat(Ad, Bd)
+        by = sum(o.numel() for o in outs) * 8 + sum(c.numel() for c in Ad + Bd) * 8
+        del outs
+        ms = timed(lambda: _ops.concat(Ad, Bd))
+        out["kernels"]["concat_kernel"] = {"ms": ms, "bytes": by, "gbs": by / ms / 1e6, "frac": by / ms / 1e6 / hbm,
+                                           "note": "one launch for all 32 sites (zero blocks written too)"}
+        del Ad, Bd
     # overlap over two 64-site chi=256 chains
-    Xh, _Wh = make_inputs()
-    Yh = [rng.standard_normal(c.shape) / math.sqrt(CHI * D_PHYS) for c in Xh]
-    Xd = [L.as_device(c) for c in Xh]
-    Yd = [L.as_device(c) for c in Yh]
-    ms = timed(lambda: _ops.overlap_device(Xd, Yd))
-    by = sum(c.size for c in Xh + Yh) * 8
-    fl = sum(2 * D_PHYS * (x.shape[0] * x.shape[2] * y.shape[2] + x.shape[0] * y.shape[0] * y.shape[2])
-             for x, y in zip(Xh, Yh))
-    out["kernels"]["overlap_sweep"] = {"ms": ms, "bytes": by, "gbs": by / ms / 1e6, "frac": by / ms / 1e6 / hbm,
-                                       "fp64_tflops": fl / ms / 1e9,
-                                       "note": "a chain of FP64 GEMMs (2 per site, sequential): FP64-pipe and "
-                                               "latency bound, its bytes are small next to its flops"}
+    if "overlap" in want:
+        Xh, _Wh = make_inputs()
+        Yh = [rng.standard_normal(c.shape) / math.sqrt(CHI * D_PHYS) for c in Xh]
+        Xd = [L.as_device(c) for c in Xh]
+        Yd = [L.as_device(c) for c in Yh]
+        ms = timed(lambda: _ops.overlap_device(Xd, Yd))
+        by = sum(c.size for c in Xh + Yh) * 8
+        fl = sum(2 * D_PHYS * (x.shape[0] * x.shape[2] * y.shape[2] + x.shape[0] * y.shape[0] * y.shape[2])
+                 for x, y in zip(Xh, Yh))
+        out["kernels"]["overlap_sweep"] = {"ms": ms, "bytes": by, "gbs": by / ms / 1e6, "frac": by / ms / 1e6 / hbm,
+                                           "fp64_tflops": fl / ms / 1e9,
+                                           "note": "a chain of FP64 GEMMs (2 per site, sequential): FP64-pipe and "
+                                                   "latency bound, its bytes are small next to its flops"}
     # Householder QR of one 8192 x 4096 unfolding + thin Q (4096 columns)
-    m, n = 8192, 4096
-    A0 = torch.from_numpy(rng.standard_normal((m, n))).to("cuda")
-    Aw = torch.empty_like(A0)
-    Q = torch.empty((m, n), dtype=torch.float64, device="cuda")
-    tau = torch.empty(n, dtype=torch.float64, device="cuda")
-    ws = L.workspace(L.query("sgt_qr_workspace_size", m, n, n))
+    if "qr" in want:
+        m, n = 8192, 4096
+        A0 = torch.from_numpy(rng.standard_normal((m, n))).to("cuda")
+        Aw = torch.empty_like(A0)
+        Q = torch.empty((m, n), dtype=torch.float64, device="cuda")
+        tau = torch.empty(n, dtype=torch.float64, device="cuda")
+        ws = L.workspace(L.query("sgt_qr_workspace_size", m, n, n))
 
-    def qr():
-        Aw.copy_(A0)
-        L.call("sgt_qr", L.ptr(Aw), m, n, n, L.ptr(tau), L.ptr(Q), n, L.ptr(ws), ws.numel(), L.stream_ptr())
+        def qr():
+            Aw.copy_(A0)
+            L.call("sgt_qr", L.ptr(Aw), m, n, n, L.ptr(tau), L.ptr(Q), n, L.ptr(ws), ws.numel(), L.stream_ptr())
 
-    ms = timed(qr)
-    fl = 2 * (2 * m * n * n - 2 * n ** 3 / 3)
-    out["kernels"]["householder_qr_8192x4096"] = {
-        "ms": ms, "fp64_tflops": fl / ms / 1e9,
-        "note": "panel_kernel (cluster panel factorisation) + FP64 trailing updates; FP64-pipe bound"}
-    out["value"] = out["kernels"]["contract_mpo_mps_kernel"]["gbs"]
+        ms = timed(qr)
+        fl = 2 * (2 * m * n * n - 2 * n ** 3 / 3)
+        out["kernels"]["householder_qr_8192x4096"] = {
+            "ms": ms, "fp64_tflops": fl / ms / 1e9,
+            "note": "panel_kernel (cluster panel factorisation) + FP64 trailing updates; FP64-pipe bound"}
+    out["value"] = next(iter(out["kernels"].values())).get("gbs") if out["kernels"] else None
     print(json.dumps(out))
     return 0
 
@@ -987,6 +992,8 @@ def main():
     ap.add_argument("--duration", type=float, default=5.0)
     ap.add_argument("--sessions", type=int, default=16)
     ap.add_argument("--drain", type=float, default=120.0)
+    ap.add_argument("--hbm-kernels", default="contract,concat,overlap,qr",
+                    help="--workload hbm: comma-separated subset of contract, concat, overlap, qr")
     ap.add_argument("--chi-max", type=int, default=128,
                     help="serving sessions: upper end of the log-uniform bond range (bond problems d*chi "
                          "above 512 leave the cluster-resident eigensolver)")

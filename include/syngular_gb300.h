@@ -221,6 +221,44 @@ SGT_API int sgt_mpo_mps_round(int n, const double* const* W, const int64_t* wsha
                               void* stream);
 
 /* ----------------------------------------------------------------------
+ * DMRG environment blocks (variational/dmrg.py:65-112, DMRG.__left_blocks /
+ * DMRG.__right_blocks) and the two-site effective contraction
+ * (variational/dmrg.py:143-165, the `site` tensor of each sweep step).
+ *
+ * Shapes: `wshape` holds quadruples (b, in, out, b') per site; `xshape` (the
+ * bra, contracted with the operator's OUT leg) and `yshape` (the ket,
+ * contracted with its IN leg) hold triples.  The reference passes the same
+ * state for both (dmrg.py:78-81).
+ *   side 0: blocks[k] = L_k (x_r, w_r, y_r) for k = 0..count-1,
+ *           L_k[a',b',c'] = sum L_{k-1}[a,b,c] X_k[a,o,a'] W_k[b,i,o,b'] Y_k[c,i,c']
+ *   side 1: blocks[k] = R_k (x_l, w_l, y_l) for k = n-1 down to n-count,
+ *           R_k[a,b,c] = sum X_k[a,o,a'] W_k[b,i,o,b'] Y_k[c,i,c'] R_{k+1}[a',b',c']
+ * with the unit 1x1x1 block beyond the chain ends.  The reference computes
+ * count = n-2 blocks on each side.  `blocks` is an array of n device pointers
+ * (entries outside the computed range are ignored).  Plain FP64, no
+ * rescaling.
+ * -------------------------------------------------------------------- */
+SGT_API size_t sgt_env_blocks_workspace_size(int n, const int64_t* wshape, const int64_t* xshape,
+                                             const int64_t* yshape, int side, int count);
+SGT_API int sgt_env_blocks(int n, const double* const* W, const int64_t* wshape, const double* const* X,
+                           const int64_t* xshape, const double* const* Y, const int64_t* yshape, int side,
+                           int count, double* const* blocks, void* ws, size_t ws_bytes, void* stream);
+
+/* out[a,o1,o2,a4] = sum L[a,b,c] M[c,i1,i2,c4] W1[b,i1,o1,b2] W2[b2,i2,o2,b3] R[a4,b3,c4]:
+ * the effective operator of sites k, k+1 applied to their merged tensor M
+ * (c, in_k, in_{k+1}, c4).  lshape/rshape are triples; L = lshape = NULL
+ * stands for the unit block (first step, dmrg.py:143-149; needs b = c = 1),
+ * likewise R = rshape = NULL (last step, dmrg.py:150-157).  mshape, w1shape,
+ * w2shape are quadruples; `out` holds (a, out_k, out_{k+1}, a4). */
+SGT_API size_t sgt_env_two_site_workspace_size(const int64_t* lshape, const int64_t* mshape,
+                                               const int64_t* w1shape, const int64_t* w2shape,
+                                               const int64_t* rshape);
+SGT_API int sgt_env_two_site(const double* L, const int64_t* lshape, const double* M, const int64_t* mshape,
+                             const double* W1, const int64_t* w1shape, const double* W2,
+                             const int64_t* w2shape, const double* R, const int64_t* rshape, double* out,
+                             void* ws, size_t ws_bytes, void* stream);
+
+/* ----------------------------------------------------------------------
  * Dense primitives (exported for composition and tests)
  * -------------------------------------------------------------------- */
 

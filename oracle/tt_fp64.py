@@ -544,3 +544,58 @@ def sweep_fp64(W: Cores, X: Cores, chi: int):
     P = mpo_mps_product(W, X)
     Z, spectra, disc = tt_svd_round(P, chi)
     return Z, overlap(X, Z), spectra, disc
+
+
+# ---------------------------------------------------------------------------
+# DMRG environment blocks (variational/dmrg.py)
+# ---------------------------------------------------------------------------
+
+def env_left_blocks(W: Cores, X: Cores, Y: Cores = None) -> list:
+    """``DMRG.__left_blocks`` (``variational/dmrg.py:89-112``): for k = 0..n-3,
+    ``L_k[a', b', c'] = sum L_{k-1}[a, b, c] X_k[a, o, a'] W_k[b, i, o, b']
+    Y_k[c, i, c']`` (the bra X on the operator's output leg, the ket Y on its
+    input leg; the reference uses one state for both), the first block without
+    ``L_{-1}``.  Entries k >= n-2 are None, as in the reference."""
+    Y = X if Y is None else Y
+    n = len(W)
+    out = [None] * n
+    prev = np.ones((1, 1, 1))
+    for k in range(n - 2):
+        t = np.tensordot(prev, X[k], axes=([0], [0]))            # [b, c, o, a']
+        t = np.tensordot(t, W[k], axes=([0, 2], [0, 2]))         # [c, a', i, b']
+        t = np.tensordot(t, Y[k], axes=([0, 2], [0, 1]))         # [a', b', c']
+        out[k] = t
+        prev = t
+    return out
+
+
+def env_right_blocks(W: Cores, X: Cores, Y: Cores = None) -> list:
+    """``DMRG.__right_blocks`` (``variational/dmrg.py:65-87``): for k = n-1
+    down to 2, ``R_k[a, b, c] = sum X_k[a, o, a'] W_k[b, i, o, b']
+    Y_k[c, i, c'] R_{k+1}[a', b', c']``, the last block without ``R_n``.
+    Entries k < 2 are None."""
+    Y = X if Y is None else Y
+    n = len(W)
+    out = [None] * n
+    nxt = np.ones((1, 1, 1))
+    for k in range(n - 1, 1, -1):
+        t = np.tensordot(X[k], nxt, axes=([2], [0]))             # [a, o, b', c']
+        t = np.tensordot(t, W[k], axes=([1, 2], [2, 3]))         # [a, c', b, i]
+        t = np.tensordot(t, Y[k], axes=([3, 1], [1, 2]))         # [a, b, c]
+        out[k] = t
+        nxt = t
+    return out
+
+
+def env_two_site(Lb, merge: np.ndarray, W1: np.ndarray, W2: np.ndarray, Rb) -> np.ndarray:
+    """The tensor each DMRG sweep step hands to its optimiser
+    (``variational/dmrg.py:143-165``): ``out[a, o1, o2, a4] = sum L[a, b, c]
+    M[c, i1, i2, c4] W1[b, i1, o1, b2] W2[b2, i2, o2, b3] R[a4, b3, c4]``, with
+    L (first step) or R (last step) absent, i.e. the unit block."""
+    Lb = np.ones((1, 1, 1)) if Lb is None else Lb
+    Rb = np.ones((1, 1, 1)) if Rb is None else Rb
+    t = np.tensordot(Lb, merge, axes=([2], [0]))                 # [a, b, i1, i2, c4]
+    t = np.tensordot(t, W1, axes=([1, 2], [0, 1]))               # [a, i2, c4, o1, b2]
+    t = np.tensordot(t, W2, axes=([4, 1], [0, 1]))               # [a, c4, o1, o2, b3]
+    t = np.tensordot(t, Rb, axes=([4, 1], [1, 2]))               # [a, o1, o2, a4]
+    return t

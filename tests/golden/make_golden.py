@@ -468,6 +468,52 @@ def mul_cases(st: Store):
     st.put("syn", "exact_xw", np.matmul(x, w).astype(np.float64))
 
 
+def dmrg_cases(st: Store):
+    """DMRG environment blocks (variational/dmrg.py:65-112) and the two-site
+    tensors a sweep hands to its optimiser (dmrg.py:128-165), from the
+    reference's own private methods.  The right sweep runs with a stand-in
+    optimiser that records each step's input and returns it normalised (a
+    power-iteration step), so the state changes from step to step as in a real
+    sweep; every record keeps the state's two sites at that moment."""
+    from syngular.variational.dmrg import DMRG as RefDMRG
+
+    cases = [("dmrg_a", (3, 3, 3, 3), (4, 4, 4), (3, 3, 3), 5),
+             ("dmrg_b", (2, 2, 2, 2, 2), (3, 5, 5, 3), (2, 4, 4, 2), 6)]
+    for case, phys, wb, xb, seed in cases:
+        np.random.seed(seed)
+        with quiet():
+            op = MPO.random(input_shape=phys, output_shape=phys, bond_shape=wb)
+            state = MPS.random(input_shape=phys, bond_shape=xb)
+            left = RefDMRG._DMRG__left_blocks(operator=op, state=state)
+            right = RefDMRG._DMRG__right_blocks(operator=op, state=state)
+        st.put(case, "W", cores(op))
+        st.put(case, "X", cores(state))
+        n = len(phys)
+        for k in range(n):
+            if left[k] is not None:
+                st.put(case, "left/%d" % k, np.asarray(left[k], dtype=np.float64))
+            if right[k] is not None:
+                st.put(case, "right/%d" % k, np.asarray(right[k], dtype=np.float64))
+        records = []
+
+        class Recorder:
+            @staticmethod
+            def fit(site, init_vec=None):
+                k = len(records)
+                records.append((np.array(state.sites[k]), np.array(state.sites[k + 1]), np.array(site)))
+                v = np.asarray(site).reshape(-1)
+                return 0.0, v / np.linalg.norm(v)
+
+        with quiet():
+            RefDMRG._DMRG__right_sweep(operator=op, state=state, left_blocks=left, right_blocks=right,
+                                       optimizer=Recorder)
+        for k, (s0, s1, site) in enumerate(records):
+            st.put(case, "step/%d/x0" % k, s0)
+            st.put(case, "step/%d/x1" % k, s1)
+            st.put(case, "step/%d/site" % k, site)
+        st.put(case, "steps", len(records))
+
+
 GROUPS = {
     "readme_flow": readme_flow,
     "config1": config1,
@@ -475,6 +521,7 @@ GROUPS = {
     "random_cases": random_cases,
     "apply_cases": apply_cases,
     "mul_cases": mul_cases,
+    "dmrg_cases": dmrg_cases,
 }
 
 

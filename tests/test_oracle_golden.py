@@ -242,3 +242,32 @@ def test_mul(golden):
     np.testing.assert_allclose(O.to_tensor(xw).reshape(-1), g("syn", "exact_xw"), rtol=1e-12)
     _, xx = O.mul("mps", X, "mps", X)
     assert abs(xx - float(g("syn", "XX"))) <= TOL * abs(xx)
+
+
+@pytest.mark.parametrize("case", ["dmrg_a", "dmrg_b"])
+def test_dmrg_environment(golden, case):
+    """Environment blocks and the sweep's two-site tensors (variational/dmrg.py:65-165)."""
+    g = golden("dmrg_cases.npz")
+    W, X = g(case, "W"), g(case, "X")
+    n = len(W)
+    left = O.env_left_blocks(W, X)
+    right = O.env_right_blocks(W, X)
+    for k in range(n):
+        if k <= n - 3:
+            assert rel(left[k], g(case, "left/%d" % k)) < TOL
+        else:
+            assert left[k] is None
+        if k >= 2:
+            assert rel(right[k], g(case, "right/%d" % k)) < TOL
+        else:
+            assert right[k] is None
+    # the sweep uses the blocks built before it (dmrg.py:41-42), with the state's current sites
+    steps = int(g(case, "steps"))
+    assert steps == n - 1
+    for k in range(steps):
+        x0, x1 = g(case, "step/%d/x0" % k), g(case, "step/%d/x1" % k)
+        merge = np.tensordot(x0, x1, axes=([2], [0]))
+        Lb = None if k == 0 else left[k - 1]
+        Rb = None if k == n - 2 else right[k + 2]
+        site = O.env_two_site(Lb, merge, W[k], W[k + 1], Rb)
+        assert rel(site, g(case, "step/%d/site" % k)) < TOL
