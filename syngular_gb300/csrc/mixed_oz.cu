@@ -928,9 +928,110 @@ __global__ void tc2_status_kernel(const int* __restrict__ ctl, const unsigned* _
   *st = (ctl[1] || __uint_as_float(*resid) <= ldexpf(1.f, -30)) ? 0 : -1;
 }
 
+// Blocked right-looking form of the same factorisation, for projectors whose
+// factor does not fit one cluster's shared memory (keep x c beyond ~48 K
+// floats per CTA: bond problems of 2048 and more).  Aw is a working copy of A
+// that holds the Schur complement left by the previous panels; a panel of
+// PB_NB pivots is chosen by one block (pivot = largest remaining diagonal,
+// ties to the lowest row, as the kernels above; each column is A's pivot row
+// minus the panel's earlier columns, A symmetric), then every SM subtracts the
+// panel's outer product from Aw.  O(c^2 keep) FP32 work, all of it in the
+// trailing updates.
+constexpr int PB_NB = 32;
+
+__global__ void __launch_bounds__(1024) pchol_panel_kernel(const float* __restrict__ Aw, int c, int j0, int nb,
+                                                           float* __restrict__ Lt, float* __restrict__ d,
+                                                           int* __restrict__ used) {
+  __shared__ float s_val[32];
+  __shared__ int s_idx[32];
+  __shared__ int s_p[PB_NB];
+  __shared__ float s_inv;
+  for (int s = j0; s < j0 + nb; ++s) {
+    float best = -1.f;
+    int bi = 0;
+    for (int i = threadIdx.x; i < c; i += blockDim.x) {
+      const float v = used[i] ? -1.f : d[i];
+      if (v > best) best = v, bi = i;
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+      const float ov = __shfl_xor_sync(0xffffffffu, best, o);
+      const int oi = __shfl_xor_sync(0xffffffffu, bi, o);
+      if (ov > best || (ov == best && oi < bi)) best = ov, bi = oi;
+    }
+    if ((threadIdx.x & 31) == 0) s_val[threadIdx.x >> 5] = best, s_idx[threadIdx.x >> 5] = bi;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      float b = -1.f;
+      int p = 0;
+      for (int w = 0; w < (int)(blockDim.x >> 5); ++w)
+        if (s_val[w] > b || (s_val[w] == b && s_idx[w] < p)) b = s_val[w], p = s_idx[w];
+      s_p[s - j0] = p;
+      used[p] = 1;
+      s_inv = 1.f / sqrtf(fmaxf(b, 1e-30f));
+    }
+    __syncthreads();
+    const int p = s_p[s - j0];
+    const float inv = s_inv;
+    for (int i = threadIdx.x; i < c; i += blockDim.x) {
+      float v = Aw[(int64_t)p * c + i];
+      for (int t = j0; t < s; ++t) v -= Lt[(int64_t)t * c + i] * Lt[(int64_t)t * c + s_p[t - j0]];
+      const float l = v * inv;
+      Lt[(int64_t)s * c + i] = l;
+      d[i] -= l * l;
+    }
+    __syncthreads();
+  }
+}
+
+// Aw (c x c) -= P^T P with P = Lt rows [j0, j0 + nb), nb <= PB_NB: 64 x 64
+// tiles, 4 x 4 outputs per thread, P's two column ranges staged in shared
+// memory.
+__global__ void __launch_bounds__(256) pchol_update_kernel(float* __restrict__ Aw, int c,
+                                                           const float* __restrict__ P, int nb) {
+  __shared__ float Ps[PB_NB][64];
+  __shared__ float Qs[PB_NB][64];
+  const int tid = threadIdx.x, tx = tid % 16, ty = tid / 16;
+  const int i0 = blockIdx.y * 64, j0 = blockIdx.x * 64;
+  for (int idx = tid; idx < PB_NB * 64; idx += 256) {
+    const int t = idx / 64, q = idx % 64;
+    Ps[t][q] = (t < nb && i0 + q < c) ? P[(int64_t)t * c + i0 + q] : 0.f;
+    Qs[t][q] = (t < nb && j0 + q < c) ? P[(int64_t)t * c + j0 + q] : 0.f;
+  }
+  __syncthreads();
+  float acc[4][4] = {};
+#pragma unroll 8
+  for (int t = 0; t < PB_NB; ++t) {
+    float a[4], b[4];
+#pragma unroll
+    for (int u = 0; u < 4; ++u) a[u] = Ps[t][ty + 16 * u], b[u] = Qs[t][tx + 16 * u];
+#pragma unroll
+    for (int u = 0; u < 4; ++u)
+#pragma unroll
+      for (int v = 0; v < 4; ++v) acc[u][v] = fmaf(a[u], b[v], acc[u][v]);
+  }
+#pragma unroll
+  for (int u = 0; u < 4; ++u) {
+    const int i = i0 + ty + 16 * u;
+    if (i >= c) continue;
+#pragma unroll
+    for (int v = 0; v < 4; ++v) {
+      const int j = j0 + tx + 16 * v;
+      if (j < c) Aw[(int64_t)i * c + j] -= acc[u][v];
+    }
+  }
+}
+
+__global__ void pchol_init_kernel(const float* __restrict__ A, int c, float* __restrict__ d, int* __restrict__ used) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < c; i += gridDim.x * blockDim.x) {
+    d[i] = A[(int64_t)i * c + i];
+    used[i] = 0;
+  }
+}
+
 // Rank-keep pivoted Cholesky factor Lt (keep x c) of the FP32 projector A
-// (c x c): the cluster kernel where it fits, else the one-block kernel.
-int pivoted_chol(cudaStream_t st, const float* A, int64_t c, int64_t keep, float* Lt, int* used) {
+// (c x c): the cluster kernel where it fits, else (work: c*c + c floats of
+// scratch) the blocked form, else the one-block kernel.
+int pivoted_chol(cudaStream_t st, const float* A, int64_t c, int64_t keep, float* Lt, int* used, float* work) {
   const int64_t R = cdiv(c, (int64_t)PC_CS);
   int64_t Rp = 32;
   while (Rp < R) Rp *= 2;
@@ -961,7 +1062,25 @@ int pivoted_chol(cudaStream_t st, const float* A, int64_t c, int64_t keep, float
       note_launch();
       return SGT_OK;
     }
-    cudaGetLastError();  // not here: the one-block kernel
+    cudaGetLastError();  // not here: the blocked or one-block kernel
+  }
+  if (work && c >= 64) {
+    float* Aw = work;
+    float* d = work + c * c;
+    SGT_CUDA(cudaMemcpyAsync(Aw, A, sizeof(float) * c * c, cudaMemcpyDeviceToDevice, st));
+    pchol_init_kernel<<<(unsigned)cdiv(c, 256), 256, 0, st>>>(A, (int)c, d, used);
+    SGT_LAUNCHED();
+    const dim3 ug((unsigned)cdiv(c, 64), (unsigned)cdiv(c, 64));
+    for (int64_t j0 = 0; j0 < keep; j0 += PB_NB) {
+      const int nb = (int)std::min<int64_t>(PB_NB, keep - j0);
+      pchol_panel_kernel<<<1, 1024, 0, st>>>(Aw, (int)c, (int)j0, nb, Lt, d, used);
+      SGT_LAUNCHED();
+      if (j0 + nb < keep) {
+        pchol_update_kernel<<<ug, 256, 0, st>>>(Aw, (int)c, Lt + j0 * c, nb);
+        SGT_LAUNCHED();
+      }
+    }
+    return SGT_OK;
   }
   SGT_REQUIRE(c * sizeof(float) <= 48 * 1024, SGT_ERR_INVALID, "mpo_mps_round: bond problem too large");
   pivoted_chol_kernel<<<1, 1024, c * sizeof(float), st>>>(A, (int)c, (int)keep, Lt, used);
@@ -1117,7 +1236,7 @@ int oz_round_impl(cudaStream_t st, int n, const double* const* W, const int64_t*
   Sliced Yts = take_sliced(ar, cmax, rmax), Ytps = take_sliced(ar, cmax, rmax), GYs = take_sliced(ar, cmax, rmax);
   Sliced Ys = take_sliced(ar, rmax, cmax);
   Pair Z = take_pair(ar, cmax * cmax);
-  float* Z32 = ar.take<float>((size_t)(cmax * cmax));
+  float* Z32 = ar.take<float>((size_t)(cmax * cmax + cmax));  // + the blocked pivoted Cholesky's diagonal
   float* Vt32 = ar.take<float>((size_t)(cmax * cmax));
   float* lam32 = ar.take<float>((size_t)cmax);
   Pair Vt = take_pair(ar, cmax * cmax), Xv = take_pair(ar, cmax * cmax), VV = take_pair(ar, cmax * cmax);
@@ -1316,7 +1435,7 @@ int oz_round_impl(cudaStream_t st, int n, const double* const* W, const int64_t*
       pair_symmetrize_kernel<<<grid_for(c * c), 256, 0, st>>>(X.h, X.l, c);
       SGT_LAUNCHED();
       // basis: Q = L^T X with L the rank-keep pivoted Cholesky factor of X's FP32 part
-      SGT_TRY(pivoted_chol(st, X.h, c, keep, Vt32, perm));
+      SGT_TRY(pivoted_chol(st, X.h, c, keep, Vt32, perm, Z32));  // Z32 (c*c) and lam32 (c) are free here
       SGT_TRY(oz_split_pair(st, Vt32, nullptr, c, keep, c, Ets.s, Ets.e, 1));
       Ets.rows = keep;
       Ets.cols = c;
