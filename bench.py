@@ -97,6 +97,14 @@ def _eig_summary(stats, ms_total, kernel="gjacobi_kernel<1>"):
     }
 
 
+def _pct(values, p):
+    """Nearest-rank percentile of a small sample (None when empty)."""
+    v = sorted(values)
+    if not v:
+        return None
+    return v[min(len(v) - 1, max(0, int(math.ceil(p / 100.0 * len(v))) - 1))]
+
+
 def workload_name():
     return ("config2: MPS N=%d d=2 chi=256 x MPO D=16 -> raw product (bond 4096) -> TT-SVD round to chi=256 -> <X|Z>"
             % N_SITES) + ("" if N_SITES == 64 else " (shortened chain for profiling, not the headline)")
@@ -418,13 +426,17 @@ def run_gpu(args, rank, world, local_rank):
     launches0 = L.load().sgt_launch_count()
     barrier()
     torch.cuda.synchronize()
-    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    # one event per step boundary: the K steps are also K jobs whose device
+    # latencies give the p50/p99 of the metric
+    evs = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps + 1)]
+    e0, e1 = evs[0], evs[-1]
     e0.record()
-    for _ in range(args.steps):
+    for i in range(args.steps):
         Z, res, status = step(Xd, Wd)
-    e1.record()
+        evs[i + 1].record()
     torch.cuda.synchronize()
     barrier()
+    step_ms = [evs[i].elapsed_time(evs[i + 1]) for i in range(args.steps)]
     launches = L.load().sgt_launch_count() - launches0
     tc_ms, tc_flops, tc_n = ctypes.c_double(), ctypes.c_double(), ctypes.c_longlong()
     L.call("sgt_tc_profile", 0, ctypes.byref(tc_ms), ctypes.byref(tc_flops), ctypes.byref(tc_n))
@@ -450,11 +462,14 @@ def run_gpu(args, rank, world, local_rank):
         torch.cuda.synchronize()
         barrier()
         t0 = time.perf_counter()
+        e2e_job_ms = []
         for _ in range(args.steps):
+            tj = time.perf_counter()
             Xm = MatrixProductState.from_sites([c.to(dev, non_blocking=True) for c in Xp])
             Wm = MatrixProductOperator.from_sites([c.to(dev, non_blocking=True) for c in Wp])
             Zm = (Wm @ Xm) >> CHI
             ov_api = float(Xm | Zm)
+            e2e_job_ms.append((time.perf_counter() - tj) * 1e3)
         torch.cuda.synchronize()
         barrier()
         e2e_s = max_over_ranks(time.perf_counter() - t0)
@@ -474,6 +489,10 @@ def run_gpu(args, rank, world, local_rank):
         "e2e": {"value": e2e_value, "unit": "sweeps/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": 16,
                 "api": "(MatrixProductOperator @ MatrixProductState) >> chi with AUTO_ROUND=False, ROUNDING='svd', "
                        "PRECISION='%s'; then X | Z" % args.precision, "overlap": ov_api},
+        "latency": {"p50_ms": _pct(step_ms, 50), "p99_ms": _pct(step_ms, 99), "jobs": len(step_ms),
+                    "e2e_p50_ms": _pct(e2e_job_ms, 50), "e2e_p99_ms": _pct(e2e_job_ms, 99),
+                    "note": "one job = one sweep; device time per step (inputs resident) and wall time per "
+                            "API call with host inputs and the overlap read back"},
         "gpu_launches": int(launches),
         "clocks": clk,
         "overlap": ov_fast,
@@ -663,11 +682,14 @@ def run_batched(args):
     mine = shard(list(range(len(data))), rank, world)
     insts = [Instance(*data[i]) for i in mine]
     log("%d instances, %d on this rank" % (len(data), len(insts)))
-    tune = autotune(insts, precision=prec, candidates=(4, 8), reps=1)
+    # the batch returns rounded cores and overlaps (no per-bond spectra)
+    # lane count timed on a sample of the batch (graph replays), then used for all of it
+    tune = autotune(insts[: min(len(insts), 128)], precision=prec, candidates=(4, 8, 16), reps=1, spectra=False,
+                    per_lane=args.graph_per_lane)
     log("autotune: %s" % json.dumps(tune))
-    b = BatchedRound(insts, precision=prec, streams=tune["streams"])
-    b.capture()
-    log("graph captured")
+    b = BatchedRound(insts, precision=prec, streams=tune["streams"], spectra=False)
+    b.capture(per_lane=args.graph_per_lane)
+    log("%d graph(s) captured" % len(b.graphs))
     for _ in range(max(args.warmup, 3)):
         b.replay()
     torch.cuda.synchronize()
@@ -687,7 +709,7 @@ def run_batched(args):
     log("timed replays: %.1f ms per batch" % ms)
     # plain FP64 per-instance form on a sample, scaled to the batch by instance count
     sample = insts[: args.plain_sample]
-    bp = BatchedRound(sample, precision=L.PREC_F64, streams=1)
+    bp = BatchedRound(sample, precision=L.PREC_F64, streams=1, spectra=False)
     bp.launch()
     torch.cuda.synchronize()
     p0, p1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
@@ -711,7 +733,8 @@ def run_batched(args):
         "ms_per_step": ms, "higher_is_better": True, "scaling": "strong" if world > 1 else "weak",
         "dtype": DTYPES[args.precision], "data": "synthetic (seeded)",
         "config": {"workload": "config3: %d instances, N~U[8,64], d in {2,3,4}, chi~U[16,128], D in {4,8,16}"
-                   % len(data), "streams": tune["streams"], "graph": "one captured CUDA graph per batch and rank",
+                   % len(data), "streams": tune["streams"],
+                   "graph": "%d captured CUDA graph(s) per batch and rank, replayed back to back" % len(b.graphs),
                    "autotune": tune, "parallelism": "instances sharded over %d rank(s)" % world},
         "converged": converged, "instances": len(data), "plain_fp64_instances_per_s": 1e3 / plain_ms_per_inst,
         "plain_fp64_sample": len(sample),
@@ -863,7 +886,9 @@ def run_hbm(args):
     if "contract" in want:
         X = L.as_device(rng.standard_normal((256, 2, 256)) / 16.0)
         W = L.as_device(rng.standard_normal((16, 2, 2, 16)) / 6.0)
-        ms = timed(lambda: _ops.contract_mpo_mps([W], [X]))
+        P = _ops.empty((256 * 16, 2, 256 * 16))
+        ms = timed(lambda: L.call("sgt_site_contract_mpo_mps", L.ptr(X), 256, 2, 256, L.ptr(W), 16, 2, 16, L.ptr(P),
+                                  L.stream_ptr()))
         by = 4096 * 2 * 4096 * 8 + X.numel() * 8 + W.numel() * 8
         out["kernels"]["contract_mpo_mps_kernel"] = {"ms": ms, "bytes": by, "gbs": by / ms / 1e6,
                                                      "frac": by / ms / 1e6 / hbm}
@@ -874,8 +899,14 @@ def run_hbm(args):
         Bd = [L.as_device(c) for c in B]
         outs = _ops.concat(Ad, Bd)
         by = sum(o.numel() for o in outs) * 8 + sum(c.numel() for c in Ad + Bd) * 8
+        # the kernel alone: outputs allocated once, one C-ABI call per step
+        ap, _ap = L.ptr_array(Ad)
+        bp, _bp = L.ptr_array(Bd)
+        op, _op = L.ptr_array(outs)
+        ash, _as = L.shape_array([_ops.shape3(c) for c in Ad])
+        bsh, _bs = L.shape_array([_ops.shape3(c) for c in Bd])
+        ms = timed(lambda: L.call("sgt_bond_concat_chain", len(Ad), ap, ash, bp, bsh, op, None, 0, L.stream_ptr()))
         del outs
-        ms = timed(lambda: _ops.concat(Ad, Bd))
         out["kernels"]["concat_kernel"] = {"ms": ms, "bytes": by, "gbs": by / ms / 1e6, "frac": by / ms / 1e6 / hbm,
                                            "note": "one launch for all 32 sites (zero blocks written too)"}
         del Ad, Bd
@@ -962,7 +993,7 @@ def run_serving(args):
         sid = "s%d" % int(rng.integers(0, nsess))
         kind = ["round", "add_round", "overlap"][int(rng.integers(0, 3))]
         chi = srv.sessions[sid]["chi"]
-        j = Job(kind=kind, session=sid, chi=chi, precision=L.PREC_TF32X3, other=sid, job_id=k,
+        j = Job(kind=kind, session=sid, chi=chi, precision=PRECISIONS[args.precision], other=sid, job_id=k,
                 arrival=t0 + ta)
         jobs.append(srv.submit(j))
     log("%d jobs submitted" % len(jobs))
@@ -977,7 +1008,8 @@ def run_serving(args):
     stats = latency_stats(done)
     out = {
         "metric": "serving jobs/s with p50/p99 latency", "value": len(done) / wall, "unit": "jobs/s",
-        "n_gpus": 1, "higher_is_better": True, "dtype": "tf32x3/f32 (round), f64 (add_round, overlap)",
+        "n_gpus": 1, "higher_is_better": True,
+        "dtype": "%s (round, add_round; no spectra), f64 (overlap)" % DTYPES[args.precision],
         "data": "synthetic seeded Poisson stream",
         "config": {"workload": "config5 stream: %.0f jobs/s for %.1f s, %d resident sessions, N~U[8,128], "
                                "d in {2,4}, chi log-uniform [8,%d], D in {4,16}, HBM budget 120 GB"
@@ -1009,11 +1041,12 @@ def main():
     ap.add_argument("--drain", type=float, default=120.0)
     ap.add_argument("--config4-spectra", action="store_true",
                     help="--workload config4: also run the rounding that returns every bond's spectrum")
+    ap.add_argument("--graph-per-lane", type=int, default=4,
+                    help="--workload batched: instances per lane in each captured graph (0 = one graph)")
     ap.add_argument("--hbm-kernels", default="contract,concat,overlap,qr",
                     help="--workload hbm: comma-separated subset of contract, concat, overlap, qr")
-    ap.add_argument("--chi-max", type=int, default=128,
-                    help="serving sessions: upper end of the log-uniform bond range (bond problems d*chi "
-                         "above 512 leave the cluster-resident eigensolver)")
+    ap.add_argument("--chi-max", type=int, default=512,
+                    help="serving sessions: upper end of the log-uniform bond range")
     ap.add_argument("--sites", type=int, default=64, help="chain length (64 = the headline workload; shorter "
                     "chains only for profiling captures)")
     args = ap.parse_args()

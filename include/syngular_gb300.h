@@ -210,7 +210,14 @@ SGT_API int sgt_svd_round(int n, const double* const* cores, const int64_t* shap
  * O(R^3) step the sliced bf16 GEMM below (sgt_gemm_f64_sliced), Gram matrices
  * and intermediates in FP32 pairs, each bond's FP32 Jacobi eigenvectors
  * refined by two Ogita-Aishima steps against the pair-accurate bond matrix;
- * product cores are sliced site by site and never stored whole.
+ * product cores are sliced site by site and never stored whole.  With
+ * `spectra` NULL no eigensolve runs: each bond's kept subspace is the range of
+ * the projector that trace-correcting purification (X <- X^2 or 2X - X^2 on
+ * the sliced GEMM, at most 90 steps, stopped on the device once X^2 = X to
+ * 2^-34) makes from the bond matrix, its basis the rows of L^T X (L the
+ * pivoted Cholesky factor of X) made orthonormal by Newton-Schulz steps; a
+ * bond where nothing is cut takes the identity.  The rounded state depends on
+ * the kept subspaces only, so both variants give the same state.
  * -------------------------------------------------------------------- */
 SGT_API size_t sgt_mpo_mps_round_workspace_size(int n, const int64_t* wshape, const int64_t* xshape,
                                                 int64_t chi, int precision);

@@ -41,9 +41,12 @@ class Instance:
 
 class BatchedRound:
     def __init__(self, instances: List[Instance], precision: int = L.PREC_TF32X3, streams: int = 4,
-                 budget_bytes: int = 160 << 30):
+                 budget_bytes: int = 160 << 30, spectra: bool = True):
         self.instances = instances
         self.precision = precision
+        # without spectra the rounding returns only the rounded cores (the
+        # BF16X6 form then finds kept subspaces by purification)
+        self.spectra = bool(spectra)
         dev = L.device()
         # output shapes, spectra counts, workspace sizes
         self.ws_need = []
@@ -86,6 +89,7 @@ class BatchedRound:
         self.ws = [torch.empty(b, dtype=torch.uint8, device=dev) for b in lane_ws]
         self.streams = [torch.cuda.Stream() for _ in self.lanes]
         self.graph: Optional[torch.cuda.CUDAGraph] = None
+        self.graphs: List[torch.cuda.CUDAGraph] = []
         # keep the ctypes argument arrays alive for graph replays
         self._keep = []
         self._args = [self._build_args(inst) for inst in instances]
@@ -101,40 +105,53 @@ class BatchedRound:
         self._keep += [a1, a2, a3, a4, a5, a6]
         return (n, wp, wsh, xp, xsh, op, osh)
 
-    def launch(self):
-        """Enqueue every instance on its stream (no synchronisation)."""
+    def launch(self, chunk=None):
+        """Enqueue every instance on its stream (no synchronisation); with
+        ``chunk = (j0, j1)`` only the instances at positions j0..j1-1 of every
+        lane."""
         cur = torch.cuda.current_stream()
         for lane, ws, st in zip(self.lanes, self.ws, self.streams):
             st.wait_stream(cur)
             sp = L._c_vp(st.cuda_stream)
-            for i in lane:
+            for i in (lane if chunk is None else lane[chunk[0]:chunk[1]]):
                 inst = self.instances[i]
                 n, wp, wsh, xp, xsh, op, osh = self._args[i]
                 L.call("sgt_mpo_mps_round", n, wp, wsh, xp, xsh, inst.chi, self.precision, op,
-                       L.ptr(inst.spectra), L.ptr(inst.disc), L.ptr(inst.status), L.ptr(ws), ws.numel(), sp)
+                       L.ptr(inst.spectra) if self.spectra else None, L.ptr(inst.disc), L.ptr(inst.status),
+                       L.ptr(ws), ws.numel(), sp)
                 L.call("sgt_overlap_sweep", n, xp, xsh, op, osh, L.ptr(inst.ovl), L.ptr(ws), ws.numel(), sp)
         for st in self.streams:
             cur.wait_stream(st)
 
-    def capture(self):
-        """Capture launch() once into a CUDA graph (run launch() eagerly first
-        so every one-time set-up inside the library has happened)."""
+    def capture(self, per_lane: int = 0):
+        """Capture launch() into CUDA graphs (run launch() eagerly first so
+        every one-time set-up inside the library has happened).  ``per_lane >
+        0`` splits the batch into graphs of at most that many instances per
+        lane, replayed back to back: a large batch of long chains holds
+        millions of kernel nodes, more than one graph should."""
         self.launch()
         torch.cuda.synchronize()
-        g = torch.cuda.CUDAGraph()
+        longest = max(len(l) for l in self.lanes)
+        step = longest if per_lane <= 0 else per_lane
+        graphs = []
         side = torch.cuda.Stream()
         side.wait_stream(torch.cuda.current_stream())
-        with torch.cuda.stream(side):
-            with torch.cuda.graph(g, stream=side):
-                self.launch()
+        for j0 in range(0, longest, step):
+            g = torch.cuda.CUDAGraph()
+            with torch.cuda.stream(side):
+                with torch.cuda.graph(g, stream=side):
+                    self.launch((j0, j0 + step))
+            graphs.append(g)
         torch.cuda.current_stream().wait_stream(side)
-        self.graph = g
-        return g
+        self.graphs = graphs
+        self.graph = graphs[0]
+        return graphs
 
     def replay(self):
         if self.graph is None:
             self.capture()
-        self.graph.replay()
+        for g in self.graphs:
+            g.replay()
 
     def overlaps(self) -> List[float]:
         from .tensor._ops import decode_overlap
@@ -195,8 +212,10 @@ class NativeBatchedRound:
     lanes off the current stream and joins them): same results as BatchedRound,
     graph-capturable."""
 
-    def __init__(self, instances: List[Instance], precision: int = L.PREC_TF32X3, lanes: int = 4):
+    def __init__(self, instances: List[Instance], precision: int = L.PREC_TF32X3, lanes: int = 4,
+                 spectra: bool = True):
         self.instances = instances
+        self.spectra = bool(spectra)
         self.plan = NativePlan([(i.wsh, i.xsh, i.chi) for i in instances], precision, lanes)
         dev = L.device()
         self._keep = []
@@ -229,8 +248,8 @@ class NativeBatchedRound:
 
     def launch(self):
         W, X, O, SP, DI, ST, OV = self._arrs
-        L.call("sgt_batched_launch", self.plan.handle, W, X, O, SP, DI, ST, OV, L.ptr(self.ws), self.ws.numel(),
-               L.stream_ptr())
+        L.call("sgt_batched_launch", self.plan.handle, W, X, O, SP if self.spectra else None, DI, ST, OV,
+               L.ptr(self.ws), self.ws.numel(), L.stream_ptr())
 
     def capture(self):
         self.launch()
@@ -267,10 +286,10 @@ def shape_class(instances: List[Instance]) -> str:
 
 def autotune(instances: List[Instance], precision: int = L.PREC_TF32X3,
              candidates: Sequence[int] = (2, 4, 8, 16), budget_bytes: int = 160 << 30,
-             reps: int = 2) -> Dict:
+             reps: int = 2, spectra: bool = True, per_lane: int = 0) -> Dict:
     """Pick the stream count with the fastest graph replay for this shape class;
     the result is cached in TUNE_FILE."""
-    key = "%s_p%d" % (shape_class(instances), precision)
+    key = "%s_p%d%s" % (shape_class(instances), precision, "" if spectra else "_nospec")
     cache = {}
     if os.path.exists(TUNE_FILE):
         try:
@@ -284,10 +303,10 @@ def autotune(instances: List[Instance], precision: int = L.PREC_TF32X3,
     trials = {}
     for s in candidates:
         try:
-            b = BatchedRound(instances, precision, streams=s, budget_bytes=budget_bytes)
+            b = BatchedRound(instances, precision, streams=s, budget_bytes=budget_bytes, spectra=spectra)
         except MemoryError:
             continue
-        b.capture()
+        b.capture(per_lane=per_lane)
         torch.cuda.synchronize()
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         e0.record()

@@ -718,6 +718,15 @@ __global__ void __launch_bounds__(256) tc2_step_kernel(float* __restrict__ xh, f
   }
 }
 
+// identity pair matrix (rows x cols, ld = cols)
+__global__ void pair_eye_kernel(float* __restrict__ h, float* __restrict__ l, int64_t rows, int64_t cols) {
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < rows * cols;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    h[i] = (i / cols == i % cols) ? 1.f : 0.f;
+    l[i] = 0.f;
+  }
+}
+
 // diagonal of a pair matrix (n x n) into d (hi then lo)
 __global__ void pair_diag_kernel(const float* __restrict__ h, const float* __restrict__ l, int n,
                                  float* __restrict__ d) {
@@ -1396,6 +1405,15 @@ int oz_round_impl(cudaStream_t st, int n, const double* const* W, const int64_t*
       break;
     }
     const int64_t keep = x[k];
+    if (!spectra && keep >= c) {
+      // nothing is cut at this bond (the rank bound keeps all c directions):
+      // the identity is an orthonormal basis of the kept space, no bond matrix needed
+      pair_eye_kernel<<<grid_for(keep * c), 256, 0, st>>>(Vk.h, Vk.l, keep, c);
+      SGT_LAUNCHED();
+      pair_to_f64_kernel<<<grid_for(keep * c), 256, 0, st>>>(Vk.h, Vk.l, c, out[k], c, keep, c);
+      SGT_LAUNCHED();
+      if (discarded) SGT_CUDA(cudaMemsetAsync(discarded + (k - 1), 0, sizeof(double), st));
+    } else {
     // GY (c x r) = Ytp G_k^T, with Ytp = Yt's columns in G_k's (b, a) column order
     const int64_t chik = xs[3 * k], Dk = w[k].b;
     SGT_TRY(pair_transpose(st, Ytp, chik, r, Yt, Dk, r, chik, Dk, c));
@@ -1513,6 +1531,7 @@ int oz_round_impl(cudaStream_t st, int n, const double* const* W, const int64_t*
                                           discarded ? discarded + (k - 1) : nullptr, gexp + k);
     SGT_LAUNCHED();
     }
+    }  // bond matrix branches
     // Ft_k (keep x r) = Vk Y^T with Y = Yt^T (r x c)
     Pair Y = Ytp;  // Ytp is free again
     SGT_TRY(pair_transpose(st, Y, c, 0, Yt, r, 0, c, r, 1));

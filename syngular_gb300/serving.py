@@ -36,7 +36,8 @@ class Job:
     kind: str
     session: str
     chi: int = 0
-    precision: int = L.PREC_TF32X3
+    precision: int = L.PREC_BF16X6
+    spectra: bool = False                # rounding jobs: also return every bond's singular values
     other: Optional[str] = None          # second operand's session (add_round / overlap)
     arrival: float = 0.0                 # seconds (time.perf_counter clock)
     job_id: int = 0
@@ -121,7 +122,7 @@ class RoundServer:
                     x.shape[2] + (y.shape[2] if k < len(X) - 1 else 0)) for k, (x, y) in enumerate(zip(X, Y))]
             shp[0] = (1, shp[0][1], shp[0][2])
             sh, _c = L.shape_array(shp)
-            ws = L.query("sgt_svd_round_workspace_size", len(X), sh, job.chi, L.PREC_F64)
+            ws = L.query("sgt_svd_round_workspace_size", len(X), sh, job.chi, job.precision)
             return cat + ws if ws else -1
         X, Y = s["mps"], self.sessions[job.other]["mps"]
         xs, _d = L.shape_array([tuple(x.shape) for x in X])
@@ -135,11 +136,11 @@ class RoundServer:
         st.wait_stream(torch.cuda.current_stream())
         with torch.cuda.stream(st):
             if job.kind == "round":
-                res = _ops.mpo_mps_round(s["mpo"], s["mps"], job.chi, job.precision)
+                res = _ops.mpo_mps_round(s["mpo"], s["mps"], job.chi, job.precision, spectra=job.spectra)
                 out = (res[0], res[1], res[2], res[3], res[4])
             elif job.kind == "add_round":
                 S = _ops.concat(s["mps"], self.sessions[job.other]["mps"])
-                out = _ops.svd_round(S, job.chi)
+                out = _ops.svd_round(S, job.chi, job.precision, spectra=job.spectra)
             else:
                 out = _ops.overlap_device(s["mps"], self.sessions[job.other]["mps"])
             ev = torch.cuda.Event()

@@ -33,14 +33,14 @@ def server_with_sessions(rng, count, budget=8 << 30, slots=4):
     return srv
 
 
-def jobs_for(rng, count):
+def jobs_for(rng, count, precision=0):
     from syngular_gb300.serving import Job
 
     jobs = []
     for i in range(count):
         kind = ["round", "add_round", "overlap"][i % 3]
         s = "s%d" % i
-        jobs.append(Job(kind=kind, session=s, chi=int(rng.integers(3, 9)), precision=0, other=s, job_id=i))
+        jobs.append(Job(kind=kind, session=s, chi=int(rng.integers(3, 9)), precision=precision, other=s, job_id=i))
     return jobs
 
 
@@ -55,10 +55,15 @@ def summary(job):
     return _ops.overlap(cores, cores)
 
 
-def test_mix_equals_alone():
+@pytest.mark.parametrize("precision", [0, 5])
+def test_mix_equals_alone(precision):
+    """Each job's result alone (one slot) equals its result in the mix (four
+    slots, overlapping on the device): FP64 and the BF16X6 precision form
+    (rounding without spectra, the serving default).  Every kernel of both
+    forms sums in a fixed order, so the tolerance is FP64 rounding."""
     rng = np.random.default_rng(3)
     srv = server_with_sessions(rng, 12).start()
-    jobs = jobs_for(rng, 12)
+    jobs = jobs_for(rng, 12, precision)
     for j in jobs:
         srv.submit(j)
     for j in jobs:
@@ -69,7 +74,7 @@ def test_mix_equals_alone():
     # alone: one slot, one job at a time
     rng = np.random.default_rng(3)
     solo = server_with_sessions(rng, 12, slots=1).start()
-    jobs2 = jobs_for(rng, 12)
+    jobs2 = jobs_for(rng, 12, precision)
     alone = []
     for j in jobs2:
         solo.submit(j)
