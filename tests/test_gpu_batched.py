@@ -35,20 +35,25 @@ def make(rng, count):
     return insts, ref
 
 
-@pytest.mark.parametrize("prec,tol", [(0, 1e-12), (4, 1e-6)])
-def test_batched_eager_and_graph(prec, tol):
+@pytest.mark.parametrize("prec,tol,spectra,per_lane", [(0, 1e-12, True, 0), (4, 1e-6, True, 0),
+                                                      (5, 1e-9, False, 2)])
+def test_batched_eager_and_graph(prec, tol, spectra, per_lane):
+    """Eager launch against the FP64 oracle, then graph replay against the
+    eager results; the BF16X6 case runs without spectra (purification) and
+    captures the batch as several graphs of two instances per lane."""
     from syngular_gb300.batched import BatchedRound
 
     rng = np.random.default_rng(77)
     insts, ref = make(rng, 12)
-    b = BatchedRound(insts, precision=prec, streams=4)
+    b = BatchedRound(insts, precision=prec, streams=4, spectra=spectra)
     b.launch()
     torch.cuda.synchronize()
     eager = b.overlaps()
     assert all(s >= 0 for s in b.statuses())
     for v, (r, scale) in zip(eager, ref):
         assert abs(v - r) <= tol * scale
-    b.capture()
+    b.capture(per_lane=per_lane)
+    assert len(b.graphs) == (1 if per_lane == 0 else -(-max(len(l) for l in b.lanes) // per_lane))
     for inst in insts:
         inst.ovl.zero_()
     b.replay()
