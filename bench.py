@@ -97,6 +97,17 @@ def _eig_summary(stats, ms_total, kernel="gjacobi_kernel<1>"):
     }
 
 
+def _apply_split(args, L):
+    """--split CTAS,KTILES sets the sliced GEMM's split-K shape (library
+    tuning); returns the shape in effect."""
+    if args.split:
+        ctas, kt = (int(v) for v in args.split.split(","))
+        L.call("sgt_set_tuning", L.TUNE_SLICED_SPLIT_CTAS, ctas)
+        L.call("sgt_set_tuning", L.TUNE_SLICED_SPLIT_MIN_KTILES, kt)
+    lib = L.load()
+    return [int(lib.sgt_get_tuning(L.TUNE_SLICED_SPLIT_CTAS)), int(lib.sgt_get_tuning(L.TUNE_SLICED_SPLIT_MIN_KTILES))]
+
+
 def _pct(values, p):
     """Nearest-rank percentile of a small sample (None when empty)."""
     v = sorted(values)
@@ -381,6 +392,7 @@ def run_gpu(args, rank, world, local_rank):
     torch.cuda.set_device(local_rank)
     dev = torch.device("cuda", local_rank)
     prec = PRECISIONS[args.precision]
+    split = _apply_split(args, L)
 
     Xh, Wh = make_inputs()
     Xd = [torch.from_numpy(c).to(dev) for c in Xh]
@@ -482,7 +494,7 @@ def run_gpu(args, rank, world, local_rank):
         "warmup": max(args.warmup, 3), "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": DTYPES[args.precision],
         "data": "synthetic (seeded N(0,1)/sqrt(chi*d) cores)",
-        "config": {"workload": workload_name(), "form": args.precision, "l2": "working set larger than L2 every step (bf16x6: %.1f GB of Gram-matrix slices written and "
+        "config": {"workload": workload_name(), "form": args.precision, "sliced_split": split, "l2": "working set larger than L2 every step (bf16x6: %.1f GB of Gram-matrix slices written and "
                    "read per sweep; tf32 forms: %.1f GB of split product cores)"
                    % (N_SITES * 4096 * 4096 * 12 / 1e9, N_SITES * 4096 * 2 * 4096 * 8 / 1e9),
                    "parallelism": "replicas" if world > 1 else "single GPU"},
@@ -685,7 +697,8 @@ def run_batched(args):
     # the batch returns rounded cores and overlaps (no per-bond spectra)
     # lane count timed on a sample of the batch (graph replays), then used for all of it
     tune = autotune(insts[: min(len(insts), 128)], precision=prec, candidates=(4, 8, 16), reps=1, spectra=False,
-                    per_lane=args.graph_per_lane)
+                    per_lane=args.graph_per_lane,
+                    splits=((148, 8), (152, 4), (304, 4)) if prec == L.PREC_BF16X6 else ())
     log("autotune: %s" % json.dumps(tune))
     b = BatchedRound(insts, precision=prec, streams=tune["streams"], spectra=False)
     b.capture(per_lane=args.graph_per_lane)
@@ -1041,6 +1054,8 @@ def main():
     ap.add_argument("--drain", type=float, default=120.0)
     ap.add_argument("--config4-spectra", action="store_true",
                     help="--workload config4: also run the rounding that returns every bond's spectrum")
+    ap.add_argument("--split", default="",
+                    help="CTAS,KTILES: the sliced GEMM's split-K shape (default: the library's 148,8)")
     ap.add_argument("--graph-per-lane", type=int, default=4,
                     help="--workload batched: instances per lane in each captured graph (0 = one graph)")
     ap.add_argument("--hbm-kernels", default="contract,concat,overlap,qr",

@@ -398,6 +398,21 @@ SGT_API int sgt_gemm_f64_sliced(int64_t M, int64_t N, int64_t K, double alpha, c
                                 const double* B, int64_t ldb, double beta, double* C, int64_t ldc, void* ws,
                                 size_t ws_bytes, void* stream);
 
+/* Process-wide tuning of the sliced GEMM (no reference counterpart; the
+ * batched engine's autotuner sets it).  SGT_TUNE_SLICED_SPLIT_CTAS: a product
+ * whose output has fewer 128 x 96 tiles than this many CTAs is split along K
+ * (partials added in a fixed order) until it fills about that many CTAs, each
+ * split keeping at least SGT_TUNE_SLICED_SPLIT_MIN_KTILES tiles of 32 along K
+ * (defaults 148 and 8; ranges 1..608 and 2..32).  Workspace queries made
+ * under one setting stay valid under another: a split that would not fit the
+ * workspace is not taken.  Results do not depend on the setting beyond FP32
+ * pair rounding of the partial sums.  sgt_get_tuning returns the current
+ * value (-1 for an unknown key). */
+#define SGT_TUNE_SLICED_SPLIT_CTAS 0
+#define SGT_TUNE_SLICED_SPLIT_MIN_KTILES 1
+SGT_API int sgt_set_tuning(int key, int value);
+SGT_API int sgt_get_tuning(int key);
+
 /* Event timing of the sliced bf16 GEMM launches, as sgt_tc_profile (flops
  * counted as 2 M N K per call, the FP64-equivalent work). */
 SGT_API int sgt_sliced_profile(int enable, double* ms, double* flops, long long* launches);

@@ -31,6 +31,9 @@ PREC_BF16X3 = 3
 PREC_TF32X3 = 4
 PREC_BF16X6 = 5
 
+TUNE_SLICED_SPLIT_CTAS = 0
+TUNE_SLICED_SPLIT_MIN_KTILES = 1
+
 _c_i64 = ctypes.c_int64
 _c_vp = ctypes.c_void_p
 _c_int = ctypes.c_int
@@ -74,6 +77,8 @@ SIGNATURES = {
     "sgt_split_tf32": (_c_int, [_c_vp, _c_vp, _c_vp, _c_i64, _c_vp]),
     "sgt_gemm_f64_sliced_workspace_size": (_c_size, [_c_i64, _c_i64, _c_i64]),
     "sgt_gemm_f64_sliced": (_c_int, [_c_i64, _c_i64, _c_i64, _c_dbl, _c_vp, _c_i64, _c_vp, _c_i64, _c_dbl, _c_vp, _c_i64, _c_vp, _c_size, _c_vp]),
+    "sgt_set_tuning": (_c_int, [_c_int, _c_int]),
+    "sgt_get_tuning": (_c_int, [_c_int]),
     "sgt_sliced_profile": (_c_int, [_c_int, ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_longlong)]),
     "sgt_launch_count": (ctypes.c_ulonglong, []),
     "sgt_sym_eig_f32_workspace_size": (_c_size, [_c_i64]),

@@ -17,7 +17,7 @@ import ctypes
 import json
 import math
 import os
-from typing import Dict, List, Optional, Sequence
+from typing import Dict, List, Optional, Sequence, Tuple
 
 import torch
 
@@ -284,12 +284,37 @@ def shape_class(instances: List[Instance]) -> str:
     return "r%d_n%d_c%d" % (2 ** math.ceil(math.log2(max(r, 1))), 8 * ((nb + 7) // 8), len(instances))
 
 
+def _time_config(instances, precision, streams, budget_bytes, reps, spectra, per_lane):
+    b = BatchedRound(instances, precision, streams=streams, budget_bytes=budget_bytes, spectra=spectra)
+    b.capture(per_lane=per_lane)
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    for _ in range(reps):
+        b.replay()
+    e1.record()
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1) / reps
+    del b
+    torch.cuda.empty_cache()
+    return ms
+
+
 def autotune(instances: List[Instance], precision: int = L.PREC_TF32X3,
              candidates: Sequence[int] = (2, 4, 8, 16), budget_bytes: int = 160 << 30,
-             reps: int = 2, spectra: bool = True, per_lane: int = 0) -> Dict:
-    """Pick the stream count with the fastest graph replay for this shape class;
-    the result is cached in TUNE_FILE."""
-    key = "%s_p%d%s" % (shape_class(instances), precision, "" if spectra else "_nospec")
+             reps: int = 2, spectra: bool = True, per_lane: int = 0,
+             splits: Sequence[Tuple[int, int]] = ()) -> Dict:
+    """Pick, by timed graph replays of this batch, the stream-lane count and
+    (when ``splits`` lists candidates) the sliced GEMM's split-K shape: the
+    CTA count a product with few output tiles is spread over and the least K
+    extent (in 32-wide tiles) each split keeps, i.e. the K depth of the tiles
+    of the bond-sized products (the library's SGT_TUNE_SLICED_SPLIT_CTAS and
+    SGT_TUNE_SLICED_SPLIT_MIN_KTILES).  Lanes are tuned first at the library's
+    current split shape, then the split shape at the best lane count.  The
+    choice is cached in TUNE_FILE per shape class and applied to the library
+    before returning."""
+    key = "%s_p%d%s%s" % (shape_class(instances), precision, "" if spectra else "_nospec",
+                          "_k" + "-".join("%dx%d" % (int(a), int(b)) for a, b in splits) if splits else "")
     cache = {}
     if os.path.exists(TUNE_FILE):
         try:
@@ -297,30 +322,45 @@ def autotune(instances: List[Instance], precision: int = L.PREC_TF32X3,
                 cache = json.load(f)
         except (OSError, ValueError):
             cache = {}
+    lib = L.load()
+
+    def apply(split):
+        L.call("sgt_set_tuning", L.TUNE_SLICED_SPLIT_CTAS, int(split[0]))
+        L.call("sgt_set_tuning", L.TUNE_SLICED_SPLIT_MIN_KTILES, int(split[1]))
+
     if key in cache:
-        return cache[key]
+        res = cache[key]
+        if res.get("split"):
+            apply(res["split"])
+        return res
+    base = (int(lib.sgt_get_tuning(L.TUNE_SLICED_SPLIT_CTAS)), int(lib.sgt_get_tuning(L.TUNE_SLICED_SPLIT_MIN_KTILES)))
     best = None
     trials = {}
     for s in candidates:
         try:
-            b = BatchedRound(instances, precision, streams=s, budget_bytes=budget_bytes, spectra=spectra)
+            ms = _time_config(instances, precision, s, budget_bytes, reps, spectra, per_lane)
         except MemoryError:
             continue
-        b.capture(per_lane=per_lane)
-        torch.cuda.synchronize()
-        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        e0.record()
-        for _ in range(reps):
-            b.replay()
-        e1.record()
-        torch.cuda.synchronize()
-        ms = e0.elapsed_time(e1) / reps
-        trials[str(s)] = ms
+        trials["lanes=%d" % s] = ms
         if best is None or ms < best[1]:
             best = (s, ms)
-        del b
-        torch.cuda.empty_cache()
-    res = {"streams": best[0] if best else candidates[0], "ms": best[1] if best else None, "trials": trials}
+    lanes = best[0] if best else candidates[0]
+    chosen = base
+    for sp in splits:
+        sp = (int(sp[0]), int(sp[1]))
+        if sp == base and best is not None:
+            continue
+        apply(sp)
+        try:
+            ms = _time_config(instances, precision, lanes, budget_bytes, reps, spectra, per_lane)
+        except MemoryError:
+            continue
+        trials["lanes=%d,split=%dx%d" % (lanes, sp[0], sp[1])] = ms
+        if best is None or ms < best[1]:
+            best = (lanes, ms)
+            chosen = sp
+    apply(chosen)
+    res = {"streams": lanes, "split": list(chosen), "ms": best[1] if best else None, "trials": trials}
     cache[key] = res
     try:
         with open(TUNE_FILE, "w") as f:

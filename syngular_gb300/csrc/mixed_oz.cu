@@ -637,9 +637,31 @@ __global__ void pair_scale_by_kernel(const float* __restrict__ zh, const float* 
 // last block to finish (atomic ticket, reset for the next launch) sets ctl[1]
 // when resid[t] <= 2^-34: X was a projector to the products' accuracy, and
 // every later step returns at once, as do the products (skip flag ctl[1]).
+// X2 element i: the product itself (S = 1) or the sum of its S split-K
+// partials in split order (the order of the product's own partial sum).
+__device__ __forceinline__ void tc2_x2(const float* __restrict__ x2h, const float* __restrict__ x2l, int S,
+                                      int64_t mn, int64_t i, float& h, float& l) {
+  h = x2h[i];
+  l = x2l[i];
+  if (S > 1) {
+    for (int z = 1; z < S; ++z) {
+      const float v = x2h[(int64_t)z * mn + i];
+      const float sum = h + v;
+      const float bb = sum - h;
+      const float e = (h - (sum - bb)) + (v - bb);
+      h = sum;
+      l += e;
+      l += x2l[(int64_t)z * mn + i];
+    }
+    const float t = h + l;
+    l = l - (t - h);
+    h = t;
+  }
+}
+
 __global__ void __launch_bounds__(256) tc2_step_kernel(float* __restrict__ xh, float* __restrict__ xl,
                                                        const float* __restrict__ x2h, const float* __restrict__ x2l,
-                                                       int n, int keep, const float* __restrict__ dcur,
+                                                       int S, int n, int keep, const float* __restrict__ dcur,
                                                        float* __restrict__ dnext, int* __restrict__ ctl,
                                                        unsigned* __restrict__ resid, unsigned* __restrict__ ticket,
                                                        __nv_bfloat16* __restrict__ out, int64_t ldo, int64_t sstride,
@@ -653,8 +675,10 @@ __global__ void __launch_bounds__(256) tc2_step_kernel(float* __restrict__ xh, f
     double a = 0.0, b = 0.0;
     for (int i = threadIdx.x; i < n; i += blockDim.x) {
       const int64_t d = (int64_t)i * n + i;
+      float h2, l2;
+      tc2_x2(x2h, x2l, S, (int64_t)n * n, d, h2, l2);
       a += (double)dcur[i] + (double)dcur[n + i];
-      b += (double)x2h[d] + (double)x2l[d];
+      b += (double)h2 + (double)l2;
     }
     for (int o = 16; o > 0; o >>= 1) {
       a += __shfl_xor_sync(0xffffffffu, a, o);
@@ -676,7 +700,8 @@ __global__ void __launch_bounds__(256) tc2_step_kernel(float* __restrict__ xh, f
     float mx = 0.f;
     for (int64_t c = lane; c < n; c += 32) {
       const int64_t i = r * n + c;
-      const float h2 = x2h[i], l2 = x2l[i];
+      float h2, l2;
+      tc2_x2(x2h, x2l, S, (int64_t)n * n, i, h2, l2);
       float h = xh[i], l = xl[i];
       worst = fmaxf(worst, fabsf((h2 - h) + (l2 - l)));
       if (ch) {
@@ -1441,9 +1466,13 @@ int oz_round_impl(cudaStream_t st, int n, const double* const* W, const int64_t*
       Vts.cols = c;
       const unsigned sg = (unsigned)std::min<int64_t>(cdiv(c, 8), 152 * 4);
       for (int it = 0; it < TC2_ITERS; ++it) {
+        // X2 = X X; a split-K product leaves its partials, which the step adds
+        int S = 1;
         SGT_TRY(oz_gemm(st, c, c, c, 1.f, Vts.mat(), Vts.mat(), 0.f, X2.h, X2.l, c, part, part_floats, err,
-                        ichoice + 1));
-        tc2_step_kernel<<<sg, 256, 0, st>>>(X.h, X.l, X2.h, X2.l, (int)c, (int)keep, tc2_diag + (it & 1) * 2 * c,
+                        ichoice + 1, &S));
+        const float* x2h = S > 1 ? part : X2.h;
+        const float* x2l = S > 1 ? part + (int64_t)S * c * c : X2.l;
+        tc2_step_kernel<<<sg, 256, 0, st>>>(X.h, X.l, x2h, x2l, S, (int)c, (int)keep, tc2_diag + (it & 1) * 2 * c,
                                              tc2_diag + ((it + 1) & 1) * 2 * c, ichoice, tc2_resid + it, ticket,
                                              Vts.s, oz_ld(c), c * oz_ld(c), Vts.e);
         SGT_LAUNCHED();
@@ -1614,6 +1643,19 @@ extern "C" SGT_API int sgt_gemm_f64_sliced(int64_t M, int64_t N, int64_t K, doub
   SGT_REQUIRE(A && B && C && ws, SGT_ERR_INVALID, "gemm_f64_sliced: null argument");
   Arena a(ws, ws_bytes);
   return gemm_f64_sliced_impl(as_stream(stream), M, N, K, alpha, A, lda, B, ldb, beta, C, ldc, a);
+}
+
+extern "C" SGT_API int sgt_set_tuning(int key, int value) {
+  if (key == SGT_TUNE_SLICED_SPLIT_CTAS) return sgt::oz_set_split_ctas(value);
+  if (key == SGT_TUNE_SLICED_SPLIT_MIN_KTILES) return sgt::oz_set_split_min_ktiles(value);
+  sgt::set_error("set_tuning: unknown key %d", key);
+  return SGT_ERR_INVALID;
+}
+
+extern "C" SGT_API int sgt_get_tuning(int key) {
+  if (key == SGT_TUNE_SLICED_SPLIT_CTAS) return sgt::oz_split_ctas();
+  if (key == SGT_TUNE_SLICED_SPLIT_MIN_KTILES) return sgt::oz_split_min_ktiles();
+  return -1;
 }
 
 extern "C" SGT_API int sgt_sliced_profile(int enable, double* ms, double* flops, long long* launches) {

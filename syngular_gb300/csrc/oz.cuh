@@ -101,10 +101,19 @@ inline size_t oz_slice_elems(int64_t rows, int64_t cols) { return (size_t)OZ_SLI
 // wants.  `err` (device int, may be null) is set when a pipeline wait timed out.
 // `skip` (device int, may be null): when nonzero at launch time the call does
 // nothing (iterations that a device-side test found converged).
+// `splits` (may be null): with it, a split-K product leaves its S partials in
+// `part` (hi of split z at part[z M N], lo at part[(S + z) M N], row-major
+// M x N, alpha applied, beta must be 0) for the caller to add in split order,
+// and *splits = S; S = 1 writes C as usual.
 int oz_gemm(cudaStream_t st, int64_t M, int64_t N, int64_t K, float alpha, const OzMat& A, const OzMat& B, float beta,
             float* Chi, float* Clo, int64_t ldc, float* part, int64_t part_floats, int* err,
-            const int* skip = nullptr);
+            const int* skip = nullptr, int* splits = nullptr);
 size_t oz_gemm_ws_bytes(int64_t M, int64_t N, int64_t K);
+// split-K target of products with few output tiles (see sgt_set_tuning)
+int oz_set_split_ctas(int v);
+int oz_split_ctas();
+int oz_set_split_min_ktiles(int v);
+int oz_split_min_ktiles();
 int oz_profile(int enable, double* ms, double* flops, long long* launches);
 
 // Slice a pair matrix (element (r, c) = hi[r * ld + c] + lo[r * ld + c]; lo

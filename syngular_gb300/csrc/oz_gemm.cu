@@ -417,6 +417,66 @@ __global__ void oz_split_pair_kernel(const int* __restrict__ skip, const float* 
   }
 }
 
+// Vector form of the kernel above (cols, ld multiples of 4 and 16-byte aligned
+// rows): each lane reads 4 consecutive hi / lo values with one 16-byte load
+// and writes each slice's 4 values with one 8-byte store.
+__device__ __forceinline__ void slice_store4(float4 h, float4 l, int sh, __nv_bfloat16* out, int64_t sstride,
+                                             int64_t idx) {
+  const float hv[4] = {h.x, h.y, h.z, h.w}, lv[4] = {l.x, l.y, l.z, l.w};
+  float rh[4], rl[4];
+  __nv_bfloat16 q[4];
+#pragma unroll
+  for (int j = 0; j < 4; ++j) {
+    const float hh = ldexpf(hv[j], sh), ll = ldexpf(lv[j], sh);
+    const float m = rintf(hh);
+    rh[j] = hh - m;  // exact
+    rl[j] = ll;
+    q[j] = __float2bfloat16_rn(m);
+  }
+  *reinterpret_cast<uint2*>(out + idx) = *reinterpret_cast<const uint2*>(q);
+#pragma unroll
+  for (int s = 1; s < OZ_SLICES; ++s) {
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+      const float t = rh[j] + rl[j];
+      const float bb = t - rh[j];
+      rl[j] = (rh[j] - (t - bb)) + (rl[j] - bb);
+      rh[j] = t * 128.f;
+      rl[j] *= 128.f;
+      const float m = rintf(rh[j] + rl[j]);
+      rh[j] = rh[j] - m;
+      q[j] = __float2bfloat16_rn(ldexpf(m, -7 * s));
+    }
+    *reinterpret_cast<uint2*>(out + (int64_t)s * sstride + idx) = *reinterpret_cast<const uint2*>(q);
+  }
+}
+
+__global__ void oz_split_pair4_kernel(const int* __restrict__ skip, const float* __restrict__ hi,
+                                      const float* __restrict__ lo, int64_t ld, int64_t rows, int64_t cols,
+                                      __nv_bfloat16* __restrict__ out, int64_t ldo, int64_t sstride,
+                                      int* __restrict__ ex, int64_t exs) {
+  if (skip && *skip) return;
+  const int lane = threadIdx.x & 31;
+  const int64_t warps = (int64_t)gridDim.x * (blockDim.x >> 5);
+  const int64_t c4 = cols >> 2;
+  for (int64_t r = (int64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); r < rows; r += warps) {
+    const float4* hr = reinterpret_cast<const float4*>(hi + r * ld);
+    const float4* lr = lo ? reinterpret_cast<const float4*>(lo + r * ld) : nullptr;
+    float mx = 0.f;
+    for (int64_t c = lane; c < c4; c += 32) {
+      const float4 h = hr[c];
+      mx = fmaxf(mx, fmaxf(fmaxf(fabsf(h.x), fabsf(h.y)), fmaxf(fabsf(h.z), fabsf(h.w))));
+    }
+    for (int o = 16; o > 0; o >>= 1) mx = fmaxf(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+    int e = 0;
+    if (mx > 0.f && isfinite(mx)) frexpf(mx, &e);
+    if (lane == 0) ex[r * exs] = e;
+    for (int64_t c = lane; c < c4; c += 32)
+      slice_store4(hr[c], lr ? lr[c] : make_float4(0.f, 0.f, 0.f, 0.f), 6 - e, out, sstride, r * ldo + 4 * c);
+    for (int64_t c = cols + lane; c < ldo; c += 32) slice_zero(out, sstride, r * ldo + c);
+  }
+}
+
 // The same from FP64 with general strides (small operands: site cores).
 __global__ void oz_split_f64_kernel(const double* __restrict__ x, int64_t rs, int64_t cs, int64_t rows, int64_t cols,
                                     __nv_bfloat16* __restrict__ out, int64_t ldo, int64_t sstride,
@@ -481,16 +541,38 @@ std::vector<OzProf> g_oz_prof;
 }  // namespace
 
 // K splits of an M x N x K product: at least enough for OZ_KC of K per CTA
-// (exactness), more while the output has too few tiles to fill the GPU, the
-// splits keep >= 256 of K each and the workspace (part_floats) holds them.
+// (exactness), more while the output has too few tiles to fill the split
+// target's CTAs, the splits keep the minimum K-tiles each (default 8 x 32 =
+// 256 of K) and the workspace (part_floats) holds them.
 // -1 when even the required splits do not fit the workspace.
+// CTAs a product with few output tiles is split up to (process-wide tuning,
+// sgt_set_tuning(SGT_TUNE_SLICED_SPLIT_CTAS, v)).
+// Those splits keep at least this many K-tiles of OZ_BK each
+// (SGT_TUNE_SLICED_SPLIT_MIN_KTILES).
+static int g_oz_split_ctas = 148;
+static int g_oz_split_min_kt = 8;
+
+int oz_set_split_ctas(int v) {
+  SGT_REQUIRE(v >= 1 && v <= 4 * 152, SGT_ERR_INVALID, "sliced GEMM split target %d outside [1, 608]", v);
+  __atomic_store_n(&g_oz_split_ctas, v, __ATOMIC_RELAXED);
+  return SGT_OK;
+}
+int oz_split_ctas() { return __atomic_load_n(&g_oz_split_ctas, __ATOMIC_RELAXED); }
+int oz_set_split_min_ktiles(int v) {
+  SGT_REQUIRE(v >= 2 && v <= 32, SGT_ERR_INVALID, "sliced GEMM split K-tiles %d outside [2, 32]", v);
+  __atomic_store_n(&g_oz_split_min_kt, v, __ATOMIC_RELAXED);
+  return SGT_OK;
+}
+int oz_split_min_ktiles() { return __atomic_load_n(&g_oz_split_min_kt, __ATOMIC_RELAXED); }
+
 int oz_splits(int64_t M, int64_t N, int64_t K, int64_t part_floats) {
   const int64_t kt = cdiv(K, OZ_BK);
   auto norm = [&](int64_t S) { return cdiv(kt, cdiv(kt, S)); };
   int64_t S = norm(cdiv(K, OZ_KC));
   if (S > 1 && 2 * S * M * N > part_floats) return -1;
   const int64_t tiles = cdiv(N, OZ_BN) * cdiv(M, OZ_BM);
-  while (tiles * S < 148 && kt / (S * 2) >= 8 && 2 * norm(2 * S) * M * N <= part_floats) S = norm(2 * S);
+  const int64_t target = oz_split_ctas(), minkt = oz_split_min_ktiles();
+  while (tiles * S < target && kt / (S * 2) >= minkt && 2 * norm(2 * S) * M * N <= part_floats) S = norm(2 * S);
   return (int)S;
 }
 
@@ -500,7 +582,8 @@ size_t oz_gemm_ws_bytes(int64_t M, int64_t N, int64_t K) {
 }
 
 int oz_gemm(cudaStream_t st, int64_t M, int64_t N, int64_t K, float alpha, const OzMat& A, const OzMat& B, float beta,
-            float* Chi, float* Clo, int64_t ldc, float* part, int64_t part_floats, int* err, const int* skip) {
+            float* Chi, float* Clo, int64_t ldc, float* part, int64_t part_floats, int* err, const int* skip,
+            int* splits) {
   if (M <= 0 || N <= 0) return SGT_OK;
   SGT_REQUIRE(K > 0, SGT_ERR_INVALID, "oz_gemm: empty K");
   SGT_REQUIRE(M < (1ll << 31) && N < (1ll << 31) && K < (1ll << 31), SGT_ERR_INVALID, "oz_gemm: too large");
@@ -513,6 +596,8 @@ int oz_gemm(cudaStream_t st, int64_t M, int64_t N, int64_t K, float alpha, const
   const int S = oz_splits(M, N, K, part ? part_floats : 0);
   SGT_REQUIRE(S >= 1, SGT_ERR_WORKSPACE, "oz_gemm: split-K workspace too small for %lld x %lld x %lld",
               (long long)M, (long long)N, (long long)K);
+  SGT_REQUIRE(!splits || S == 1 || beta == 0.f, SGT_ERR_INVALID, "oz_gemm: deferred split-K sum needs beta = 0");
+  if (splits) *splits = S;
   const int KTall = (int)cdiv(K, OZ_BK);
   const int kps = (int)cdiv(KTall, S);
   // raster order: the CTAs that share the larger operand's tile run side by
@@ -539,7 +624,7 @@ int oz_gemm(cudaStream_t st, int64_t M, int64_t N, int64_t K, float alpha, const
   }
   oz_gemm_kernel<<<grid, OZ_THREADS, oz_smem_bytes(), st>>>(ma, mb, args);
   SGT_LAUNCHED();
-  if (S > 1) {
+  if (S > 1 && !splits) {
     oz_splitk_sum_kernel<<<(unsigned)std::min<int64_t>(cdiv(M * N, 256), 152 * 8), 256, 0, st>>>(
         skip, part, part + (int64_t)S * M * N, S, M, N, beta, Chi, Clo, ldc);
     SGT_LAUNCHED();
@@ -556,8 +641,14 @@ int oz_split_pair(cudaStream_t st, const float* hi, const float* lo, int64_t ld,
                   __nv_bfloat16* out, int* e, int64_t estride, const int* skip) {
   if (rows <= 0 || cols <= 0) return SGT_OK;
   const unsigned g = (unsigned)std::max<int64_t>(1, std::min<int64_t>(cdiv(rows, 8), 152 * 16));
-  oz_split_pair_kernel<<<g, 256, 0, st>>>(skip, hi, lo, ld, rows, cols, out, oz_ld(cols), rows * oz_ld(cols), e,
-                                          estride);
+  const bool vec = cols % 4 == 0 && ld % 4 == 0 && (reinterpret_cast<uintptr_t>(hi) & 15) == 0 &&
+                   (reinterpret_cast<uintptr_t>(lo) & 15) == 0 && (reinterpret_cast<uintptr_t>(out) & 15) == 0;
+  if (vec)
+    oz_split_pair4_kernel<<<g, 256, 0, st>>>(skip, hi, lo, ld, rows, cols, out, oz_ld(cols), rows * oz_ld(cols), e,
+                                             estride);
+  else
+    oz_split_pair_kernel<<<g, 256, 0, st>>>(skip, hi, lo, ld, rows, cols, out, oz_ld(cols), rows * oz_ld(cols), e,
+                                            estride);
   SGT_LAUNCHED();
   return SGT_OK;
 }

@@ -166,3 +166,31 @@ def test_bench_cpu_port_machinery():
     assert r["seconds"] > 0 and r["overlap"] == r["overlap"]
     info = bench.cpu_info()
     assert info["cores"] >= 1 and info["numpy"]
+
+
+def test_sliced_split_tuning_host_only(lib):
+    """The sliced GEMM's split-K target is a process-wide host setting: range
+    checked, readable, and the workspace query follows it (more splits, more
+    partial sums) without any GPU call."""
+    from syngular_gb300 import _lib as L
+
+    before = lib.sgt_get_tuning(L.TUNE_SLICED_SPLIT_CTAS)
+    assert before == 148
+    try:
+        assert lib.sgt_set_tuning(L.TUNE_SLICED_SPLIT_CTAS, 0) == L.SGT_ERR_INVALID
+        assert lib.sgt_set_tuning(L.TUNE_SLICED_SPLIT_CTAS, 609) == L.SGT_ERR_INVALID
+        assert lib.sgt_set_tuning(99, 1) == L.SGT_ERR_INVALID
+        assert lib.sgt_get_tuning(99) == -1
+        assert lib.sgt_get_tuning(L.TUNE_SLICED_SPLIT_MIN_KTILES) == 8
+        assert lib.sgt_set_tuning(L.TUNE_SLICED_SPLIT_MIN_KTILES, 1) == L.SGT_ERR_INVALID
+        sizes = []
+        for t, kt in ((24, 8), (148, 8), (592, 8), (592, 2)):
+            assert lib.sgt_set_tuning(L.TUNE_SLICED_SPLIT_CTAS, t) == L.SGT_OK
+            assert lib.sgt_set_tuning(L.TUNE_SLICED_SPLIT_MIN_KTILES, kt) == L.SGT_OK
+            assert lib.sgt_get_tuning(L.TUNE_SLICED_SPLIT_CTAS) == t
+            sizes.append(lib.sgt_gemm_f64_sliced_workspace_size(512, 512, 512))
+        # 512^3: one split at target 24, two while each keeps 8 K-tiles, eight at 2
+        assert sizes[0] < sizes[1] == sizes[2] < sizes[3]
+    finally:
+        lib.sgt_set_tuning(L.TUNE_SLICED_SPLIT_CTAS, before)
+        lib.sgt_set_tuning(L.TUNE_SLICED_SPLIT_MIN_KTILES, 8)

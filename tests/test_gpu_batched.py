@@ -69,9 +69,32 @@ def test_autotune_caches_choice(tmp_path, monkeypatch):
     rng = np.random.default_rng(5)
     insts, _ = make(rng, 6)
     r1 = B.autotune(insts, precision=0, candidates=(1, 2), reps=1)
-    assert r1["streams"] in (1, 2) and set(r1["trials"]) <= {"1", "2"}
+    assert r1["streams"] in (1, 2) and set(r1["trials"]) <= {"lanes=1", "lanes=2"}
     r2 = B.autotune(insts, precision=0, candidates=(1, 2), reps=1)
     assert r2 == r1
+
+
+def test_autotune_split_depth(tmp_path, monkeypatch):
+    """BF16X6 batch: the tuner also times the sliced GEMM's split-K target and
+    leaves the library set to its choice."""
+    import syngular_gb300.batched as B
+    from syngular_gb300 import _lib as L
+
+    monkeypatch.setattr(B, "TUNE_FILE", str(tmp_path / "tune.json"))
+    rng = np.random.default_rng(6)
+    insts, _ = make(rng, 6)
+    lib = L.load()
+    before = (lib.sgt_get_tuning(L.TUNE_SLICED_SPLIT_CTAS), lib.sgt_get_tuning(L.TUNE_SLICED_SPLIT_MIN_KTILES))
+    try:
+        r = B.autotune(insts, precision=L.PREC_BF16X6, candidates=(2,), reps=1, spectra=False, per_lane=2,
+                       splits=((74, 8), (296, 4)))
+        assert tuple(r["split"]) in (before, (74, 8), (296, 4))
+        assert (lib.sgt_get_tuning(L.TUNE_SLICED_SPLIT_CTAS),
+                lib.sgt_get_tuning(L.TUNE_SLICED_SPLIT_MIN_KTILES)) == tuple(r["split"])
+        assert "lanes=2,split=74x8" in r["trials"] and "lanes=2,split=296x4" in r["trials"]
+    finally:
+        L.call("sgt_set_tuning", L.TUNE_SLICED_SPLIT_CTAS, before[0])
+        L.call("sgt_set_tuning", L.TUNE_SLICED_SPLIT_MIN_KTILES, before[1])
 
 
 @pytest.mark.parametrize("prec,tol", [(0, 1e-12), (4, 1e-6)])
