@@ -404,9 +404,12 @@ def run_gpu(args, rank, world, local_rank):
     # the metric's operation, as `(W @ X) >> chi` returns it: rounded cores (and
     # discarded weights), no per-bond spectra; `spectra=True` times the variant
     # that also returns every bond's singular values (an eigensolve per bond)
+    # the overlap in the same form (BF16X6: contractions on the sliced GEMM)
+    oprec = prec if prec == L.PREC_BF16X6 else L.PREC_F64
+
     def step(X, W, spectra=False):
         Z, spec, counts, disc, status = _ops.mpo_mps_round(W, X, CHI, prec, spectra=spectra)
-        res = _ops.overlap_device(X, Z)
+        res = _ops.overlap_device(X, Z, oprec)
         return Z, res, status
 
     def barrier():
@@ -466,10 +469,12 @@ def run_gpu(args, rank, world, local_rank):
     # TT-SVD rounding in the benchmark's precision, then X | Z back on the host
     from syngular_gb300.tensor import MatrixProductOperator, MatrixProductState
 
-    saved = (MatrixProductOperator.AUTO_ROUND, MatrixProductOperator.PRECISION, MatrixProductState.ROUNDING)
+    saved = (MatrixProductOperator.AUTO_ROUND, MatrixProductOperator.PRECISION, MatrixProductState.ROUNDING,
+             MatrixProductState.PRECISION)
     MatrixProductOperator.AUTO_ROUND = False
     MatrixProductOperator.PRECISION = args.precision
     MatrixProductState.ROUNDING = "svd"
+    MatrixProductState.PRECISION = args.precision
     try:
         torch.cuda.synchronize()
         barrier()
@@ -486,7 +491,8 @@ def run_gpu(args, rank, world, local_rank):
         barrier()
         e2e_s = max_over_ranks(time.perf_counter() - t0)
     finally:
-        MatrixProductOperator.AUTO_ROUND, MatrixProductOperator.PRECISION, MatrixProductState.ROUNDING = saved
+        (MatrixProductOperator.AUTO_ROUND, MatrixProductOperator.PRECISION, MatrixProductState.ROUNDING,
+         MatrixProductState.PRECISION) = saved
     e2e_value = world * args.steps / e2e_s
 
     out = {
@@ -500,7 +506,7 @@ def run_gpu(args, rank, world, local_rank):
                    "parallelism": "replicas" if world > 1 else "single GPU"},
         "e2e": {"value": e2e_value, "unit": "sweeps/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": 16,
                 "api": "(MatrixProductOperator @ MatrixProductState) >> chi with AUTO_ROUND=False, ROUNDING='svd', "
-                       "PRECISION='%s'; then X | Z" % args.precision, "overlap": ov_api},
+                       "PRECISION='%s' on both classes; then X | Z" % args.precision, "overlap": ov_api},
         "latency": {"p50_ms": _pct(step_ms, 50), "p99_ms": _pct(step_ms, 99), "jobs": len(step_ms),
                     "e2e_p50_ms": _pct(e2e_job_ms, 50), "e2e_p99_ms": _pct(e2e_job_ms, 99),
                     "note": "one job = one sweep; device time per step (inputs resident) and wall time per "

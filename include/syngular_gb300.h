@@ -113,6 +113,18 @@ SGT_API int sgt_overlap_sweep(int n, const double* const* X, const int64_t* xsha
                       const double* const* Y, const int64_t* yshape,
                       double* result, void* ws, size_t ws_bytes, void* stream);
 
+/* The same overlap in a chosen arithmetic (precision SGT_PREC_F64: exactly
+ * sgt_overlap_sweep; SGT_PREC_BF16X6: both contractions of every transfer
+ * step on the sliced bf16 tensor-core GEMM, FP64-class, the transfer matrix
+ * kept in FP64 and rescaled by exact powers of two; other codes are rejected).
+ * Replaces MatrixProductState.__or__ (mps:116-127) under the precision policy.
+ * Result as for sgt_overlap_sweep. */
+SGT_API size_t sgt_overlap_prec_workspace_size(int n, const int64_t* xshape, const int64_t* yshape,
+                                               int precision);
+SGT_API int sgt_overlap_sweep_prec(int n, const double* const* X, const int64_t* xshape,
+                                   const double* const* Y, const int64_t* yshape, int precision,
+                                   double* result, void* ws, size_t ws_bytes, void* stream);
+
 /* Overlap <X|Y> that allocates nothing and takes no workspace.  It has no
  * counterpart in the reference.  It serves callers that cannot give the
  * library scratch memory -- e.g. a C/ctypes binding whose process leaves all

@@ -53,6 +53,8 @@ SIGNATURES = {
     "sgt_bond_concat_chain_workspace_size": (_c_size, [_c_int]),
     "sgt_overlap_workspace_size": (_c_size, [_c_int, _PI64, _PI64]),
     "sgt_overlap_sweep": (_c_int, [_c_int, _PP, _PI64, _PP, _PI64, _c_vp, _c_vp, _c_size, _c_vp]),
+    "sgt_overlap_prec_workspace_size": (_c_size, [_c_int, _PI64, _PI64, _c_int]),
+    "sgt_overlap_sweep_prec": (_c_int, [_c_int, _PP, _PI64, _PP, _PI64, _c_int, _c_vp, _c_vp, _c_size, _c_vp]),
     "sgt_overlap_sweep_noalloc": (_c_int, [_c_int, _PP, _PI64, _PP, _PI64, _c_vp, _c_vp]),
     "sgt_qr_truncate_workspace_size": (_c_size, [_c_int, _PI64, _c_i64]),
     "sgt_qr_truncate_sweep": (_c_int, [_c_int, _PP, _PI64, _c_i64, _PP, _c_vp, _c_size, _c_vp]),

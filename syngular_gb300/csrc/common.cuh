@@ -128,6 +128,11 @@ int qr_form_q(cudaStream_t st, const double* A, int64_t m, int64_t n, int64_t ld
 int qr_extract_r(cudaStream_t st, const double* A, int64_t m, int64_t n, int64_t lda, double* R,
                  int64_t ldr, int64_t rows);
 
+// Transfer-sweep helpers (sweeps.cu): E /= 2^e with max|E| in [0.5, 1), the
+// exponent added to *expo; on the last site result = (E[0], *expo).
+int rescale_pow2(cudaStream_t st, double* E, int64_t n, double* expo, double* result, bool last);
+int zero_scalar(cudaStream_t st, double* p);
+
 // One-sided Jacobi SVD (see sgt_jacobi_svd).
 size_t jacobi_ws_bytes(int64_t m, int64_t n);
 int jacobi_svd(cudaStream_t st, double* A, int64_t m, int64_t n, double* V, double* s, int* status,

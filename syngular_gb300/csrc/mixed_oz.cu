@@ -1627,9 +1627,113 @@ static int gemm_f64_sliced_impl(cudaStream_t st, int64_t M, int64_t N, int64_t K
   return SGT_OK;
 }
 
+// Overlap <X|Y> with both contractions of every transfer step on the sliced
+// GEMM (tensor cores, FP64-class), the transfer matrix E kept in FP64 between
+// sites and rescaled by exact powers of two as in the FP64 sweep:
+//   T (a x p c2)  = E (a x c) Y_k (c x p c2)        [A = E, B = Y_k^T]
+//   E' (a2 x c2)  = X_k^T (a2 x a p) T (a p x c2)   [A = X_k^T, B = T^T]
+// The transposed operands are sliced straight from strided FP64 views.
+static int overlap_sliced_impl(cudaStream_t st, int n, const double* const* X, const int64_t* xs,
+                               const double* const* Y, const int64_t* ys, double* result, Arena& ar) {
+  SGT_REQUIRE(n >= 1 && xs && ys, SGT_ERR_INVALID, "overlap: empty chain");
+  int64_t emax = 1, tmax = 1, es = 1, ys_ = 1, ts = 1, xs_ = 1;
+  size_t pb = 0;
+  for (int k = 0; k < n; ++k) {
+    const int64_t a = xs[3 * k], p = xs[3 * k + 1], a2 = xs[3 * k + 2];
+    const int64_t c = ys[3 * k], c2 = ys[3 * k + 2];
+    SGT_REQUIRE(a > 0 && p > 0 && a2 > 0 && c > 0 && c2 > 0 && ys[3 * k + 1] == p, SGT_ERR_INVALID,
+                "overlap: bad shapes at site %d", k);
+    if (k + 1 < n)
+      SGT_REQUIRE(a2 == xs[3 * k + 3] && c2 == ys[3 * k + 3], SGT_ERR_INVALID,
+                  "overlap: bond mismatch between sites %d and %d", k, k + 1);
+    emax = std::max(emax, a2 * c2);
+    tmax = std::max(tmax, a * p * c2);
+    es = std::max<int64_t>(es, (int64_t)oz_slice_elems(a, c));
+    ys_ = std::max<int64_t>(ys_, (int64_t)oz_slice_elems(p * c2, c));
+    ts = std::max<int64_t>(ts, (int64_t)oz_slice_elems(c2, a * p));
+    xs_ = std::max<int64_t>(xs_, (int64_t)oz_slice_elems(a2, a * p));
+    pb = std::max(pb, oz_gemm_ws_bytes(a, p * c2, c));
+    pb = std::max(pb, oz_gemm_ws_bytes(a2, c2, a * p));
+  }
+  SGT_REQUIRE(xs[0] == 1 && ys[0] == 1 && xs[3 * n - 1] == 1 && ys[3 * n - 1] == 1, SGT_ERR_INVALID,
+              "overlap: boundary bonds must be 1");
+  int64_t rmax = 1;
+  for (int k = 0; k < n; ++k) rmax = std::max(rmax, std::max(xs[3 * k + 2], std::max(ys[3 * k], xs[3 * k])));
+  double* E = ar.take<double>(emax);
+  double* Td = ar.take<double>(tmax);
+  Pair Tp = take_pair(ar, std::max(tmax, emax));
+  Sliced Es, Ysl, Tsl, Xsl;
+  Es.s = ar.take<__nv_bfloat16>((size_t)es);
+  Es.e = ar.take<int>((size_t)rmax);
+  Ysl.s = ar.take<__nv_bfloat16>((size_t)ys_);
+  Ysl.e = ar.take<int>((size_t)tmax);
+  Tsl.s = ar.take<__nv_bfloat16>((size_t)ts);
+  Tsl.e = ar.take<int>((size_t)tmax);
+  Xsl.s = ar.take<__nv_bfloat16>((size_t)xs_);
+  Xsl.e = ar.take<int>((size_t)rmax);
+  float* part = ar.take<float>(pb / sizeof(float) + 1);
+  const int64_t part_floats = (int64_t)(pb / sizeof(float));
+  double* expo = ar.take<double>(1);
+  int* err = ar.take<int>(1);
+  if (ar.measure) return SGT_OK;
+  SGT_REQUIRE(ar.ok(), SGT_ERR_WORKSPACE, "overlap: workspace too small");
+  SGT_REQUIRE(X && Y && result, SGT_ERR_INVALID, "overlap: null argument");
+  SGT_TRY(fill_f64(st, E, 1, 1.0));
+  SGT_TRY(zero_scalar(st, expo));
+  SGT_CUDA(cudaMemsetAsync(err, 0, sizeof(int), st));
+  for (int k = 0; k < n; ++k) {
+    const int64_t a = xs[3 * k], p = xs[3 * k + 1], a2 = xs[3 * k + 2];
+    const int64_t c = ys[3 * k], c2 = ys[3 * k + 2];
+    // T = E Y_k: A = E (a x c, row stride c), B = Y_k^T (p c2 x c: element (j, i) = Y_k[i, j])
+    SGT_TRY(oz_split_f64(st, E, c, 1, a, c, Es.s, Es.e, 1));
+    Es.rows = a;
+    Es.cols = c;
+    SGT_TRY(oz_split_f64(st, Y[k], 1, p * c2, p * c2, c, Ysl.s, Ysl.e, 1));
+    Ysl.rows = p * c2;
+    Ysl.cols = c;
+    SGT_TRY(oz_gemm(st, a, p * c2, c, 1.f, Es.mat(), Ysl.mat(), 0.f, Tp.h, Tp.l, p * c2, part, part_floats, err));
+    pair_to_f64_kernel<<<grid_for(a * p * c2), 256, 0, st>>>(Tp.h, Tp.l, p * c2, Td, p * c2, a, p * c2);
+    SGT_LAUNCHED();
+    // E' = X_k^T T: A = X_k^T (a2 x a p: element (j, i) = X_k[i, j]), B = T^T (c2 x a p, T as (a p) x c2)
+    SGT_TRY(oz_split_f64(st, X[k], 1, a2, a2, a * p, Xsl.s, Xsl.e, 1));
+    Xsl.rows = a2;
+    Xsl.cols = a * p;
+    SGT_TRY(oz_split_f64(st, Td, 1, c2, c2, a * p, Tsl.s, Tsl.e, 1));
+    Tsl.rows = c2;
+    Tsl.cols = a * p;
+    SGT_TRY(oz_gemm(st, a2, c2, a * p, 1.f, Xsl.mat(), Tsl.mat(), 0.f, Tp.h, Tp.l, c2, part, part_floats, err));
+    pair_to_f64_kernel<<<grid_for(a2 * c2), 256, 0, st>>>(Tp.h, Tp.l, c2, E, c2, a2, c2);
+    SGT_LAUNCHED();
+    SGT_TRY(rescale_pow2(st, E, a2 * c2, expo, result, k == n - 1));
+  }
+  return SGT_OK;
+}
+
 }  // namespace sgt
 
 using namespace sgt;
+
+extern "C" SGT_API size_t sgt_overlap_prec_workspace_size(int n, const int64_t* xshape, const int64_t* yshape,
+                                                         int precision) {
+  if (precision == SGT_PREC_F64) return sgt_overlap_workspace_size(n, xshape, yshape);
+  if (precision != SGT_PREC_BF16X6) {
+    set_error("overlap: precision %d not supported (SGT_PREC_F64 or SGT_PREC_BF16X6)", precision);
+    return 0;
+  }
+  Arena a = Arena::measuring();
+  if (overlap_sliced_impl(nullptr, n, nullptr, xshape, nullptr, yshape, nullptr, a) != SGT_OK) return 0;
+  return a.used;
+}
+
+extern "C" SGT_API int sgt_overlap_sweep_prec(int n, const double* const* X, const int64_t* xshape,
+                                              const double* const* Y, const int64_t* yshape, int precision,
+                                              double* result, void* ws, size_t ws_bytes, void* stream) {
+  if (precision == SGT_PREC_F64) return sgt_overlap_sweep(n, X, xshape, Y, yshape, result, ws, ws_bytes, stream);
+  SGT_REQUIRE(precision == SGT_PREC_BF16X6, SGT_ERR_INVALID,
+              "overlap: precision %d not supported (SGT_PREC_F64 or SGT_PREC_BF16X6)", precision);
+  Arena a(ws, ws_bytes);
+  return overlap_sliced_impl(as_stream(stream), n, X, xshape, Y, yshape, result, a);
+}
 
 extern "C" SGT_API size_t sgt_gemm_f64_sliced_workspace_size(int64_t M, int64_t N, int64_t K) {
   Arena a = Arena::measuring();

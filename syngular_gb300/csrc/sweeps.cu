@@ -172,6 +172,20 @@ __global__ void reduce_status_kernel(const int* __restrict__ st, int n, int* __r
 
 }  // namespace
 
+// Exact power-of-two rescaling of a transfer matrix (see rescale_pow2_kernel),
+// shared with the sliced overlap sweep.
+int rescale_pow2(cudaStream_t st, double* E, int64_t n, double* expo, double* result, bool last) {
+  rescale_pow2_kernel<<<1, 256, 0, st>>>(E, n, expo, result, last ? 1 : 0);
+  SGT_LAUNCHED();
+  return SGT_OK;
+}
+
+int zero_scalar(cudaStream_t st, double* p) {
+  zero_scalar_kernel<<<1, 1, 0, st>>>(p);
+  SGT_LAUNCHED();
+  return SGT_OK;
+}
+
 // ============================================================================
 // overlap
 // ============================================================================

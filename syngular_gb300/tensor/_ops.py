@@ -111,9 +111,10 @@ def concat(A: Cores, B: Cores) -> Cores:
 # overlap
 # ---------------------------------------------------------------------------
 
-def overlap_device(X: Cores, Y: Cores) -> torch.Tensor:
+def overlap_device(X: Cores, Y: Cores, precision: int = L.PREC_F64) -> torch.Tensor:
     """Transfer sweep; returns a device tensor ``(mantissa, exponent2)`` with
-    ``<X|Y> = mantissa * 2**exponent2`` (no synchronisation)."""
+    ``<X|Y> = mantissa * 2**exponent2`` (no synchronisation).  ``precision``
+    PREC_BF16X6 runs the contractions on the sliced tensor-core GEMM."""
     _check(X)
     _check(Y)
     n = len(X)
@@ -121,11 +122,20 @@ def overlap_device(X: Cores, Y: Cores) -> torch.Tensor:
         raise ValueError("chains have different lengths")
     xs, _x = L.shape_array([shape3(c) for c in X])
     ys, _y = L.shape_array([shape3(c) for c in Y])
-    ws = L.workspace(L.query("sgt_overlap_workspace_size", n, xs, ys))
     res = torch.empty(2, dtype=torch.float64, device=L.device())
     xp, _xp = L.ptr_array(X)
     yp, _yp = L.ptr_array(Y)
-    L.call("sgt_overlap_sweep", n, xp, xs, yp, ys, L.ptr(res), L.ptr(ws), ws.numel(), L.stream_ptr())
+    if precision == L.PREC_F64:
+        ws = L.workspace(L.query("sgt_overlap_workspace_size", n, xs, ys))
+        L.call("sgt_overlap_sweep", n, xp, xs, yp, ys, L.ptr(res), L.ptr(ws), ws.numel(), L.stream_ptr())
+        return res
+    need = L.query("sgt_overlap_prec_workspace_size", n, xs, ys, precision)
+    if need == 0:
+        raise L.SyngularError("sgt_overlap_prec_workspace_size", L.SGT_ERR_INVALID,
+                              L.load().sgt_last_error().decode(errors="replace"))
+    ws = L.workspace(need)
+    L.call("sgt_overlap_sweep_prec", n, xp, xs, yp, ys, precision, L.ptr(res), L.ptr(ws), ws.numel(),
+           L.stream_ptr())
     return res
 
 
@@ -137,9 +147,9 @@ def decode_overlap(res) -> float:
         return math.copysign(math.inf, m)
 
 
-def overlap(X: Cores, Y: Cores) -> float:
+def overlap(X: Cores, Y: Cores, precision: int = L.PREC_F64) -> float:
     """``X | Y`` (matrix_product_state.py:116-127), as a Python float."""
-    return decode_overlap(overlap_device(X, Y).cpu().tolist())
+    return decode_overlap(overlap_device(X, Y, precision).cpu().tolist())
 
 
 # ---------------------------------------------------------------------------

@@ -119,7 +119,11 @@ class MatrixProductState:
     def __or__(self, mp):
         """Inner product without conjugation (mps:116-129)."""
         if isinstance(mp, MatrixProductState):
-            return np.float64(_ops.overlap(self.sites, mp.sites))
+            # "bf16x6" runs the transfer sweep's contractions on the sliced
+            # tensor-core GEMM; the TF32 forms have no overlap of their own
+            prec = precision_code(type(self).PRECISION)
+            prec = prec if prec == L.PREC_BF16X6 else L.PREC_F64
+            return np.float64(_ops.overlap(self.sites, mp.sites, prec))
         raise Exception("right-hand site must be a MatrixProductState")
 
     def __rshift__(self, dim: int):

@@ -180,3 +180,33 @@ def test_bf16x6_round_without_spectra(n, d, chi, D, cut):
         if disc_r[k - 1] > 1e-9:
             m = Z[k].reshape(Z[k].shape[0], -1).cpu().numpy()
             np.testing.assert_allclose(m @ m.T, np.eye(m.shape[0]), rtol=0, atol=1e-10)
+
+
+@pytest.mark.parametrize("n,d,chi,chi2", [(12, 2, 16, 9), (64, 2, 256, 256), (5, 3, 7, 11)])
+def test_overlap_on_sliced_gemm(n, d, chi, chi2):
+    """The transfer sweep with its contractions on the sliced GEMM against the
+    FP64 sweep: <X|Y> within 1e-10 of |X||Y| and <X|X> within 1e-10 relative
+    (FP64-class products, FP64 transfer matrix, exact power-of-two rescaling)."""
+    from syngular_gb300 import _lib as L
+    from syngular_gb300.tensor import _ops
+
+    rng = np.random.default_rng(n * 100 + chi)
+    X = [L.as_device(c) for c in O.random_mps_cores(rng, n, d, chi)]
+    Y = [L.as_device(c) for c in O.random_mps_cores(rng, n, d, chi2)]
+    xy = _ops.overlap(X, Y, L.PREC_BF16X6)
+    xy64 = _ops.overlap(X, Y)
+    xx = _ops.overlap(X, X, L.PREC_BF16X6)
+    xx64 = _ops.overlap(X, X)
+    yy64 = _ops.overlap(Y, Y)
+    assert abs(xy - xy64) <= 1e-10 * np.sqrt(xx64 * yy64)
+    assert abs(xx - xx64) <= 1e-10 * xx64
+    # the drop-in operator follows MatrixProductState.PRECISION
+    from syngular_gb300.tensor import MatrixProductState
+
+    saved = MatrixProductState.PRECISION
+    try:
+        MatrixProductState.PRECISION = "bf16x6"
+        a, b = MatrixProductState.from_sites(X), MatrixProductState.from_sites(Y)
+        assert float(a | b) == xy
+    finally:
+        MatrixProductState.PRECISION = saved
