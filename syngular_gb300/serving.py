@@ -56,9 +56,20 @@ class Job:
 class RoundServer:
     """Admission by HBM budget, one CUDA stream per in-flight job."""
 
-    def __init__(self, budget_bytes: int = 120 << 30, slots: int = 8):
+    def __init__(self, budget_bytes: int = 120 << 30, slots: int = 8, graphs: bool = True,
+                 graph_job_bytes: int = 2 << 30, graph_budget_bytes: int = 24 << 30):
         self.budget = int(budget_bytes)
         self.slots = int(slots)
+        # captured CUDA graphs, one per (kind, sessions, chi, precision): a job
+        # whose graph exists and is idle replays it (one launch instead of its
+        # thousands of kernel launches from this thread) and copies the graph's
+        # outputs out; the graphs' memory counts against the budget for good
+        self.use_graphs = bool(graphs)
+        self.graph_job_bytes = int(graph_job_bytes)
+        self.graph_budget = int(graph_budget_bytes)
+        self.graphs: Dict[tuple, "_Graph"] = {}
+        self.graph_bytes = 0
+        self.replayed = 0
         self.sessions: Dict[str, dict] = {}
         self.inbox: "queue.Queue[Job]" = queue.Queue()
         self.streams = [torch.cuda.Stream() for _ in range(self.slots)]
@@ -130,22 +141,61 @@ class RoundServer:
         return L.query("sgt_overlap_workspace_size", len(X), xs, ys) + 16
 
     # -------------------------------------------------------------- execution
-    def _launch(self, job: Job, stream_idx: int):
+    def _run(self, job: Job):
+        """Enqueue the job's work on the current stream; returns its outputs."""
         s = self.sessions[job.session]
+        if job.kind == "round":
+            res = _ops.mpo_mps_round(s["mpo"], s["mps"], job.chi, job.precision, spectra=job.spectra)
+            return (res[0], res[1], res[2], res[3], res[4])
+        if job.kind == "add_round":
+            S = _ops.concat(s["mps"], self.sessions[job.other]["mps"])
+            return _ops.svd_round(S, job.chi, job.precision, spectra=job.spectra)
+        return _ops.overlap_device(s["mps"], self.sessions[job.other]["mps"])
+
+    @staticmethod
+    def _graph_key(job: Job):
+        return (job.kind, job.session, job.other, job.chi, job.precision, job.spectra)
+
+    def _capture(self, job: Job, key) -> None:
+        """Capture the job's work into a CUDA graph (no GPU execution; the
+        library's one-time set-up already ran in the job's eager launch)."""
+        before = torch.cuda.memory_reserved()
+        g = torch.cuda.CUDAGraph()
+        side = torch.cuda.Stream()
+        side.wait_stream(torch.cuda.current_stream())
+        try:
+            with torch.cuda.stream(side):
+                with torch.cuda.graph(g, stream=side, capture_error_mode="thread_local"):
+                    outputs = self._run(job)
+        except Exception:  # a job that cannot be captured keeps running eagerly
+            self.graphs[key] = None
+            return
+        nbytes = max(0, torch.cuda.memory_reserved() - before)
+        self.graphs[key] = _Graph(g, outputs, nbytes)
+        self.graph_bytes += nbytes
+        self.used += nbytes
+
+    def _launch(self, job: Job, stream_idx: int):
         st = self.streams[stream_idx]
         st.wait_stream(torch.cuda.current_stream())
+        key = self._graph_key(job) if self.use_graphs else None
+        gr = self.graphs.get(key) if key is not None else None
         with torch.cuda.stream(st):
-            if job.kind == "round":
-                res = _ops.mpo_mps_round(s["mpo"], s["mps"], job.chi, job.precision, spectra=job.spectra)
-                out = (res[0], res[1], res[2], res[3], res[4])
-            elif job.kind == "add_round":
-                S = _ops.concat(s["mps"], self.sessions[job.other]["mps"])
-                out = _ops.svd_round(S, job.chi, job.precision, spectra=job.spectra)
+            if gr is not None and not gr.busy:
+                gr.graph.replay()
+                out = _clone(gr.outputs)
+                gr.busy = True
+                self.replayed += 1
             else:
-                out = _ops.overlap_device(s["mps"], self.sessions[job.other]["mps"])
+                gr = None
+                out = self._run(job)
             ev = torch.cuda.Event()
             ev.record(st)
-        return out, ev
+        if (key is not None and key not in self.graphs and job._need <= self.graph_job_bytes
+                and self.graph_bytes + job._need <= self.graph_budget
+                and self.used + job._need <= self.budget):
+            self._capture(job, key)
+        return out, ev, gr
 
     def _loop(self):
         while not self._stop.is_set() or self.pending or self.inflight or not self.inbox.empty():
@@ -173,16 +223,18 @@ class RoundServer:
                 pass
             # retire finished jobs
             still = []
-            for job, ev, out, sidx in self.inflight:
+            for job, ev, out, sidx, gr in self.inflight:
                 if ev.query():
                     job.end = time.perf_counter()
                     job.result = out
                     self.used -= job._need
                     self.free_streams.append(sidx)
+                    if gr is not None:
+                        gr.busy = False
                     self.completed.append(job)
                     job.done.set()
                 else:
-                    still.append((job, ev, out, sidx))
+                    still.append((job, ev, out, sidx, gr))
             self.inflight = still
             # admit in arrival order while memory and slots allow
             admitted = []
@@ -195,8 +247,8 @@ class RoundServer:
                 self.used += j._need
                 j.start = time.perf_counter()
                 try:
-                    out, ev = self._launch(j, sidx)
-                    self.inflight.append((j, ev, out, sidx))
+                    out, ev, gr = self._launch(j, sidx)
+                    self.inflight.append((j, ev, out, sidx, gr))
                 except Exception as e:  # surface the error on the job, keep serving
                     j.error = str(e)
                     j.end = time.perf_counter()
@@ -206,11 +258,29 @@ class RoundServer:
                     j.done.set()
                 admitted.append(j)
             if admitted:
-                self.pending = [j for j in self.pending if j not in admitted]
+                gone = set(id(j) for j in admitted)
+                self.pending = [j for j in self.pending if id(j) not in gone]
             if not admitted and not self.inflight:
                 time.sleep(0.0002)
             else:
                 time.sleep(0)
+
+
+@dataclass
+class _Graph:
+    graph: torch.cuda.CUDAGraph
+    outputs: object                      # the captured outputs (tensors the replays overwrite)
+    nbytes: int                          # device memory the graph holds
+    busy: bool = False                   # a replay's outputs are still being copied out
+
+
+def _clone(out):
+    """Fresh copies of a job's outputs (tensors cloned on the current stream)."""
+    if isinstance(out, torch.Tensor):
+        return out.clone()
+    if isinstance(out, (list, tuple)):
+        return type(out)(_clone(o) for o in out)
+    return out
 
 
 def latency_stats(jobs: List[Job]):

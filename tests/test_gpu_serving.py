@@ -120,3 +120,35 @@ def test_bad_job_does_not_stop_the_loop():
     srv.stop()
     assert bad.error is not None and "KeyError" in bad.error
     assert good.error is None and good.result is not None
+
+
+@pytest.mark.parametrize("precision", [0, 5])
+def test_repeated_jobs_replay_graphs(precision):
+    """A job kind seen before on the same sessions replays its captured CUDA
+    graph; the replayed results equal the first (eager) run bit for bit, and
+    a graph still in use by one job is not replayed by a second in flight."""
+    from syngular_gb300.serving import Job
+
+    rng = np.random.default_rng(17)
+    srv = server_with_sessions(rng, 2, slots=4).start()
+    results = {}
+    for kind in ("round", "add_round", "overlap"):
+        runs = []
+        for rep in range(3):
+            j = Job(kind=kind, session="s0", other="s1" if kind != "round" else "s0", chi=5,
+                    precision=precision, job_id=rep)
+            srv.submit(j)
+            assert j.done.wait(120) and j.error is None, j.error
+            runs.append(summary(j))
+        results[kind] = runs
+    # two at once: one replays, the other runs eagerly
+    burst = [Job(kind="round", session="s0", other="s0", chi=5, precision=precision, job_id=10 + i) for i in range(2)]
+    for j in burst:
+        srv.submit(j)
+    for j in burst:
+        assert j.done.wait(120) and j.error is None
+    srv.stop()
+    assert srv.replayed >= 6
+    for kind, runs in results.items():
+        np.testing.assert_allclose(runs, [runs[0]] * 3, rtol=1e-12, atol=0, err_msg=kind)
+    np.testing.assert_allclose([summary(j) for j in burst], [results["round"][0]] * 2, rtol=1e-12, atol=0)
