@@ -13,8 +13,9 @@ Deliberate deviations, on inputs where the reference misbehaves:
   * MPO x MPO uses the second operand's output dimension (mpo:285 reshapes with
     the first operand's, which only works when the two agree);
   * ``decompose`` prints nothing (mpo:442).
-``MATMUL_MODE`` values other than "standard" are unfinished in the reference
-(mpo:193-276) and return None here as there.
+``MATMUL_MODE`` "opti" (the reference's unfinished density-matrix compression,
+mpo:193-273) is the fused product + TT-SVD round to the min bond; "variational"
+and "fit-up" are empty in the reference and return None here as there.
 """
 from __future__ import annotations
 
@@ -104,6 +105,19 @@ class MatrixProductOperator:
                                                                spectra=False)
                     return MatrixProductState.from_sites(out)
                 return s >> min_bond if auto else s
+            if MatrixProductOperator.MATMUL_MODE == "opti":
+                # The reference's unfinished density-matrix mode (mpo:193-273):
+                # left blocks of <WX|WX>, then from the right the dominant
+                # eigenvectors of each bond's reduced density matrix, kept to
+                # min_bond.  That is the Gram-form TT-SVD of the fused
+                # product + round (the optimal truncation; "f64" computes the
+                # same state by QR + SVD), in this class's PRECISION.
+                s = MatrixProductState.lazy_product(self.sites, mp.sites, type(self).PRECISION)
+                if min_bond >= min(s.bond_shape):
+                    return s
+                out, _sp, _c, _d, _st = _ops.mpo_mps_round(self.sites, mp.sites, min_bond,
+                                                           precision_code(type(self).PRECISION), spectra=False)
+                return MatrixProductState.from_sites(out)
             return None
         if isinstance(mp, MatrixProductOperator):
             s = MatrixProductOperator.from_sites(_ops.contract_mpo_mpo(self.sites, mp.sites))

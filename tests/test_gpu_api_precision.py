@@ -94,3 +94,32 @@ def test_auto_round_svd_on_the_operator_class(policy):
     ref, _s, _c, _d, _st = _ops.mpo_mps_round(W.sites, X.sites, 4, L.PREC_BF16X6, spectra=False)
     for a, b in zip(Z.sites, ref):
         assert torch.equal(a, b)
+
+
+@pytest.mark.parametrize("prec", ["bf16x6", "f64"])
+def test_matmul_mode_opti_is_the_density_matrix_round(policy, prec):
+    """MATMUL_MODE = "opti" (the reference's unfinished density-matrix
+    compression, mpo:193-273) gives the optimal truncation to min_bond: the
+    fused product + TT-SVD round, against the FP64 oracle's rounding."""
+    from syngular_gb300 import _lib as L
+    from syngular_gb300.tensor import _ops
+
+    MPO, MPS = policy
+    saved = MPO.MATMUL_MODE
+    try:
+        MPO.MATMUL_MODE = "opti"
+        MPO.PRECISION = prec
+        rng = np.random.default_rng(19)
+        Xc = O.random_mps_cores(rng, 8, 2, 12)
+        Wc = O.random_mpo_cores(rng, 8, 2, 4)
+        X, W = MPS.from_sites(Xc), MPO.from_sites(Wc)
+        Z = W @ X
+        code = L.PREC_BF16X6 if prec == "bf16x6" else L.PREC_F64
+        ref, _s, _c, _d, _st = _ops.mpo_mps_round(W.sites, X.sites, 4, code, spectra=False)
+        for a, b in zip(Z.sites, ref):
+            assert torch.equal(a, b)
+        Zo, _sp, _di = O.tt_svd_round(O.mpo_mps_product(Wc, Xc), 4)
+        zz = O.overlap(Zo, Zo)
+        assert abs(_ops.overlap(X.sites, Z.sites) - O.overlap(Xc, Zo)) <= 1e-8 * np.sqrt(O.overlap(Xc, Xc) * zz)
+    finally:
+        MPO.MATMUL_MODE = saved
