@@ -104,8 +104,12 @@ def _apply_split(args, L):
         ctas, kt = (int(v) for v in args.split.split(","))
         L.call("sgt_set_tuning", L.TUNE_SLICED_SPLIT_CTAS, ctas)
         L.call("sgt_set_tuning", L.TUNE_SLICED_SPLIT_MIN_KTILES, kt)
+    if args.pchol:
+        L.call("sgt_set_tuning", L.TUNE_PCHOL_BLOCKED, {"cluster": 0, "blocked": 1}[args.pchol])
     lib = L.load()
-    return [int(lib.sgt_get_tuning(L.TUNE_SLICED_SPLIT_CTAS)), int(lib.sgt_get_tuning(L.TUNE_SLICED_SPLIT_MIN_KTILES))]
+    return {"split_ctas": int(lib.sgt_get_tuning(L.TUNE_SLICED_SPLIT_CTAS)),
+            "split_min_ktiles": int(lib.sgt_get_tuning(L.TUNE_SLICED_SPLIT_MIN_KTILES)),
+            "pivoted_cholesky": "blocked" if lib.sgt_get_tuning(L.TUNE_PCHOL_BLOCKED) else "cluster"}
 
 
 def _pct(values, p):
@@ -500,7 +504,7 @@ def run_gpu(args, rank, world, local_rank):
         "warmup": max(args.warmup, 3), "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": DTYPES[args.precision],
         "data": "synthetic (seeded N(0,1)/sqrt(chi*d) cores)",
-        "config": {"workload": workload_name(), "form": args.precision, "sliced_split": split, "l2": "working set larger than L2 every step (bf16x6: %.1f GB of Gram-matrix slices written and "
+        "config": {"workload": workload_name(), "form": args.precision, "tuning": split, "l2": "working set larger than L2 every step (bf16x6: %.1f GB of Gram-matrix slices written and "
                    "read per sweep; tf32 forms: %.1f GB of split product cores)"
                    % (N_SITES * 4096 * 4096 * 12 / 1e9, N_SITES * 4096 * 2 * 4096 * 8 / 1e9),
                    "parallelism": "replicas" if world > 1 else "single GPU"},
@@ -1062,6 +1066,8 @@ def main():
                     help="--workload config4: also run the rounding that returns every bond's spectrum")
     ap.add_argument("--split", default="",
                     help="CTAS,KTILES: the sliced GEMM's split-K shape (default: the library's 148,8)")
+    ap.add_argument("--pchol", default="", choices=["", "cluster", "blocked"],
+                    help="the BF16X6 form's pivoted Cholesky (default: the library's, cluster where it fits)")
     ap.add_argument("--graph-per-lane", type=int, default=4,
                     help="--workload batched: instances per lane in each captured graph (0 = one graph)")
     ap.add_argument("--hbm-kernels", default="contract,concat,overlap,qr",

@@ -422,6 +422,11 @@ SGT_API int sgt_gemm_f64_sliced(int64_t M, int64_t N, int64_t K, double alpha, c
  * value (-1 for an unknown key). */
 #define SGT_TUNE_SLICED_SPLIT_CTAS 0
 #define SGT_TUNE_SLICED_SPLIT_MIN_KTILES 1
+/* SGT_TUNE_PCHOL_BLOCKED (0 or 1, default 0): the BF16X6 form's pivoted
+ * Cholesky of a purified projector on one 16-CTA cluster with the factor in
+ * shared memory where it fits (0), or always blocked (1: 32-pivot panels on one
+ * block, trailing updates on all SMs).  Same kept subspace either way. */
+#define SGT_TUNE_PCHOL_BLOCKED 2
 SGT_API int sgt_set_tuning(int key, int value);
 SGT_API int sgt_get_tuning(int key);
 

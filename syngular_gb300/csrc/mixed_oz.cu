@@ -1065,13 +1065,16 @@ __global__ void pchol_init_kernel(const float* __restrict__ A, int c, float* __r
 // Rank-keep pivoted Cholesky factor Lt (keep x c) of the FP32 projector A
 // (c x c): the cluster kernel where it fits, else (work: c*c + c floats of
 // scratch) the blocked form, else the one-block kernel.
+static int g_pchol_blocked = 0;  // SGT_TUNE_PCHOL_BLOCKED
+
 int pivoted_chol(cudaStream_t st, const float* A, int64_t c, int64_t keep, float* Lt, int* used, float* work) {
   const int64_t R = cdiv(c, (int64_t)PC_CS);
   int64_t Rp = 32;
   while (Rp < R) Rp *= 2;
   const size_t smem =
       sizeof(float) * ((size_t)keep * (size_t)(Rp + 3) + (size_t)Rp * (size_t)(PC_THREADS / Rp + 2));
-  if (c >= 2 * PC_CS && Rp <= PC_THREADS && smem <= 200 * 1024) {
+  const bool prefer_blocked = work && c >= 64 && __atomic_load_n(&g_pchol_blocked, __ATOMIC_RELAXED);
+  if (!prefer_blocked && c >= 2 * PC_CS && Rp <= PC_THREADS && smem <= 200 * 1024) {
     bool ok = func_attr_at_least((const void*)pivoted_chol_cluster_kernel,
                                  cudaFuncAttributeNonPortableClusterSizeAllowed, 1) == cudaSuccess &&
               func_attr_at_least((const void*)pivoted_chol_cluster_kernel,
@@ -1752,6 +1755,11 @@ extern "C" SGT_API int sgt_gemm_f64_sliced(int64_t M, int64_t N, int64_t K, doub
 extern "C" SGT_API int sgt_set_tuning(int key, int value) {
   if (key == SGT_TUNE_SLICED_SPLIT_CTAS) return sgt::oz_set_split_ctas(value);
   if (key == SGT_TUNE_SLICED_SPLIT_MIN_KTILES) return sgt::oz_set_split_min_ktiles(value);
+  if (key == SGT_TUNE_PCHOL_BLOCKED) {
+    SGT_REQUIRE(value == 0 || value == 1, SGT_ERR_INVALID, "set_tuning: pivoted Cholesky choice %d not 0 or 1", value);
+    __atomic_store_n(&sgt::g_pchol_blocked, value, __ATOMIC_RELAXED);
+    return SGT_OK;
+  }
   sgt::set_error("set_tuning: unknown key %d", key);
   return SGT_ERR_INVALID;
 }
@@ -1759,6 +1767,7 @@ extern "C" SGT_API int sgt_set_tuning(int key, int value) {
 extern "C" SGT_API int sgt_get_tuning(int key) {
   if (key == SGT_TUNE_SLICED_SPLIT_CTAS) return sgt::oz_split_ctas();
   if (key == SGT_TUNE_SLICED_SPLIT_MIN_KTILES) return sgt::oz_split_min_ktiles();
+  if (key == SGT_TUNE_PCHOL_BLOCKED) return __atomic_load_n(&sgt::g_pchol_blocked, __ATOMIC_RELAXED);
   return -1;
 }
 
