@@ -182,6 +182,11 @@ def test_sliced_split_tuning_host_only(lib):
         assert lib.sgt_set_tuning(99, 1) == L.SGT_ERR_INVALID
         assert lib.sgt_get_tuning(99) == -1
         assert lib.sgt_get_tuning(L.TUNE_SLICED_SPLIT_MIN_KTILES) == 8
+        assert lib.sgt_get_tuning(L.TUNE_PCHOL_BLOCKED) == 0
+        assert lib.sgt_set_tuning(L.TUNE_PCHOL_BLOCKED, 2) == L.SGT_ERR_INVALID
+        assert lib.sgt_set_tuning(L.TUNE_PCHOL_BLOCKED, 1) == L.SGT_OK
+        assert lib.sgt_get_tuning(L.TUNE_PCHOL_BLOCKED) == 1
+        assert lib.sgt_set_tuning(L.TUNE_PCHOL_BLOCKED, 0) == L.SGT_OK
         assert lib.sgt_set_tuning(L.TUNE_SLICED_SPLIT_MIN_KTILES, 1) == L.SGT_ERR_INVALID
         sizes = []
         for t, kt in ((24, 8), (148, 8), (592, 8), (592, 2)):
