@@ -152,11 +152,13 @@ def test_bf16x6_svd_round_chain():
     assert abs(zz - zzr) / zzr < 1e-9
 
 
+@pytest.mark.parametrize("blocked", [0, 1])
 @pytest.mark.parametrize("n,d,chi,D,cut", CASES)
-def test_bf16x6_round_without_spectra(n, d, chi, D, cut):
+def test_bf16x6_round_without_spectra(n, d, chi, D, cut, blocked):
     """Without spectra the BF16X6 form finds each kept subspace by purification
     (no eigensolve): the rounded state, the discarded weights and the right
-    orthonormality of the cores match the FP64 oracle."""
+    orthonormality of the cores match the FP64 oracle, with the projector's
+    pivoted Cholesky on one cluster or blocked."""
     from syngular_gb300 import _lib as L
     from syngular_gb300.tensor import _ops
 
@@ -164,8 +166,12 @@ def test_bf16x6_round_without_spectra(n, d, chi, D, cut):
     X = O.random_mps_cores(rng, n, d, chi)
     W = O.random_mpo_cores(rng, n, d, D)
     Zr, spec_r, disc_r = O.tt_svd_round(O.mpo_mps_product(W, X), cut)
-    Z, spec, counts, disc, status = _ops.mpo_mps_round(dev(W), dev(X), cut, L.PREC_BF16X6, spectra=False)
-    torch.cuda.synchronize()
+    L.call("sgt_set_tuning", L.TUNE_PCHOL_BLOCKED, blocked)
+    try:
+        Z, spec, counts, disc, status = _ops.mpo_mps_round(dev(W), dev(X), cut, L.PREC_BF16X6, spectra=False)
+        torch.cuda.synchronize()
+    finally:
+        L.call("sgt_set_tuning", L.TUNE_PCHOL_BLOCKED, 0)
     assert spec is None and int(status.item()) >= 0
     assert [tuple(z.shape) for z in Z] == [z.shape for z in Zr]
     e_ov, e_zz = rel_overlaps(X, Z, Zr)
