@@ -578,6 +578,25 @@ def run_gpu(args, rank, world, local_rank):
     if shares:
         top = max(shares, key=shares.get)
         out["dominant_kernel"] = dict(out[top])
+    # where one sweep's time goes (an extra, untimed sweep with CUDA events at
+    # the rounding's phase boundaries)
+    if prec == L.PREC_BF16X6:
+        try:
+            names = ["left_gram", "projections_Y", "bond_matrices_Z", "purification", "kept_basis",
+                     "discarded", "carry_F", "eigensolve"]
+            buf = (ctypes.c_double * len(names))()
+            torch.cuda.synchronize()
+            L.call("sgt_phase_profile", 1, None, 0)
+            q0, q1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            q0.record()
+            Z, res, status = step(Xd, Wd)
+            q1.record()
+            torch.cuda.synchronize()
+            L.call("sgt_phase_profile", 0, buf, len(names))
+            out["phases_ms"] = {nm: buf[i] for i, nm in enumerate(names)}
+            out["phases_ms"]["sweep_total"] = q0.elapsed_time(q1)
+        except Exception as e:  # noqa: BLE001 - reported in the JSON line
+            out["phases_ms"] = {"error": "%s: %s" % (type(e).__name__, e)}
     # the variant with every bond's spectrum (eigensolve per bond), same inputs
     if prec == L.PREC_BF16X6 and not args.no_spectra_variant:
         step(Xd, Wd, spectra=True)

@@ -430,6 +430,16 @@ SGT_API int sgt_gemm_f64_sliced(int64_t M, int64_t N, int64_t K, double alpha, c
 SGT_API int sgt_set_tuning(int key, int value);
 SGT_API int sgt_get_tuning(int key);
 
+/* Phase timing of the BF16X6 rounding (a benchmark switch, process-wide, for
+ * one rounding at a time on one stream): enable = 1 starts recording CUDA
+ * events at the phase boundaries; enable = 0 stops, waits for them and writes
+ * the milliseconds per phase into ms[0..count-1]: 0 left Gram recursion,
+ * 1 right-sweep projections Y_k, 2 bond matrices Z_k, 3 purification,
+ * 4 kept basis (pivoted Cholesky, Newton-Schulz), 5 discarded weights,
+ * 6 carry F_k to the next bond, 7 eigensolve + refinement (with spectra). */
+#define SGT_ROUND_PHASES 8
+SGT_API int sgt_phase_profile(int enable, double* ms, int count);
+
 /* Event timing of the sliced bf16 GEMM launches, as sgt_tc_profile (flops
  * counted as 2 M N K per call, the FP64-equivalent work). */
 SGT_API int sgt_sliced_profile(int enable, double* ms, double* flops, long long* launches);

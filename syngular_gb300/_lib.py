@@ -82,6 +82,7 @@ SIGNATURES = {
     "sgt_gemm_f64_sliced": (_c_int, [_c_i64, _c_i64, _c_i64, _c_dbl, _c_vp, _c_i64, _c_vp, _c_i64, _c_dbl, _c_vp, _c_i64, _c_vp, _c_size, _c_vp]),
     "sgt_set_tuning": (_c_int, [_c_int, _c_int]),
     "sgt_get_tuning": (_c_int, [_c_int]),
+    "sgt_phase_profile": (_c_int, [_c_int, ctypes.POINTER(ctypes.c_double), _c_int]),
     "sgt_sliced_profile": (_c_int, [_c_int, ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_longlong)]),
     "sgt_launch_count": (ctypes.c_ulonglong, []),
     "sgt_sym_eig_f32_workspace_size": (_c_size, [_c_i64]),

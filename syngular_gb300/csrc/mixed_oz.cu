@@ -1194,6 +1194,26 @@ bool oz_round_supported(int n, const int64_t* ws4) {
 }
 
 // ---------------------------------------------------------------------------
+// Phase timing of the BF16X6 round (sgt_phase_profile): an event at every
+// phase boundary on the round's stream, summed per phase when read.  Process-
+// wide and meant for one round at a time on one stream (benchmarks).
+enum RoundPhase { PH_LEFT = 0, PH_Y, PH_BOND, PH_PURIFY, PH_BASIS, PH_DISC, PH_CARRY, PH_EIG, PH_COUNT };
+struct PhaseMark {
+  int phase;  // the phase that starts here (-1: end of a round)
+  cudaEvent_t ev;
+};
+static bool g_phase_on = false;
+static std::vector<PhaseMark> g_phase_marks;
+
+static int phase_mark(cudaStream_t st, int phase) {
+  if (!g_phase_on) return SGT_OK;
+  cudaEvent_t e;
+  SGT_CUDA(cudaEventCreate(&e));
+  SGT_CUDA(cudaEventRecord(e, st));
+  g_phase_marks.push_back({phase, e});
+  return SGT_OK;
+}
+
 int oz_round_impl(cudaStream_t st, int n, const double* const* W, const int64_t* ws4, const double* const* X,
                   const int64_t* xs, int64_t chi, double* const* out, double* spectra, double* discarded, int* status,
                   Arena& ar) {
@@ -1330,6 +1350,7 @@ int oz_round_impl(cudaStream_t st, int n, const double* const* W, const int64_t*
     return oz_gemm(st, M, N, K, alpha, A, B, beta, C.h, C.l, ldc, part, part_floats, err);
   };
 
+  SGT_TRY(phase_mark(st, PH_LEFT));
   // ---- left Gram recursion (structured: X and W contractions, no product) ----
   pair_one_kernel<<<1, 1, 0, st>>>(G.h, G.l);
   SGT_LAUNCHED();
@@ -1401,6 +1422,7 @@ int oz_round_impl(cudaStream_t st, int n, const double* const* W, const int64_t*
   SGT_LAUNCHED();
   for (int k = n - 1; k >= 0; --k) {
     const int64_t r = R[k], r2 = R[k + 1], p = Pd[k], xc = x[k + 1], c = p * xc;
+    SGT_TRY(phase_mark(st, PH_Y));
     // Yt (c x r): Yt[(o, j)][(a, b)] = sum_{i, a', b'} F[j][(a', b')] X[a][i][a'] W[b][i][o][b'],
     // contracted in two products without forming the product core:
     //   S1: T[(j, a')][(b, i, o)] = sum_b' F[(j, a')][b'] W[(b, i, o)][b']          (K = B')
@@ -1442,6 +1464,7 @@ int oz_round_impl(cudaStream_t st, int n, const double* const* W, const int64_t*
       SGT_LAUNCHED();
       if (discarded) SGT_CUDA(cudaMemsetAsync(discarded + (k - 1), 0, sizeof(double), st));
     } else {
+    SGT_TRY(phase_mark(st, PH_BOND));
     // GY (c x r) = Ytp G_k^T, with Ytp = Yt's columns in G_k's (b, a) column order
     const int64_t chik = xs[3 * k], Dk = w[k].b;
     SGT_TRY(pair_transpose(st, Ytp, chik, r, Yt, Dk, r, chik, Dk, c));
@@ -1455,6 +1478,7 @@ int oz_round_impl(cudaStream_t st, int n, const double* const* W, const int64_t*
     SGT_LAUNCHED();
     if (!spectra && keep < c) {
       // ---- kept subspace by purification (no eigenvectors, no spectrum) ----
+      SGT_TRY(phase_mark(st, PH_PURIFY));
       pair_frob_trace_kernel<<<RED_BLOCKS, 256, 0, st>>>(Z.h, Z.l, c, rpart, ticket, dscal, dscal + 1);
       SGT_LAUNCHED();
       pair_scale_by_kernel<<<grid_for(c * c), 256, 0, st>>>(Z.h, Z.l, c * c, dscal, VV.h, VV.l);
@@ -1484,6 +1508,7 @@ int oz_round_impl(cudaStream_t st, int n, const double* const* W, const int64_t*
       SGT_LAUNCHED();
       pair_symmetrize_kernel<<<grid_for(c * c), 256, 0, st>>>(X.h, X.l, c);
       SGT_LAUNCHED();
+      SGT_TRY(phase_mark(st, PH_BASIS));
       // basis: Q = L^T X with L the rank-keep pivoted Cholesky factor of X's FP32 part
       SGT_TRY(pivoted_chol(st, X.h, c, keep, Vt32, perm, Z32));  // Z32 (c*c) and lam32 (c) are free here
       SGT_TRY(oz_split_pair(st, Vt32, nullptr, c, keep, c, Ets.s, Ets.e, 1));
@@ -1502,6 +1527,7 @@ int oz_round_impl(cudaStream_t st, int n, const double* const* W, const int64_t*
       }
       pair_to_f64_kernel<<<grid_for(keep * c), 256, 0, st>>>(Vk.h, Vk.l, c, out[k], c, keep, c);
       SGT_LAUNCHED();
+      SGT_TRY(phase_mark(st, PH_DISC));
       if (discarded) {
         // discarded weight = 1 - trace(Q Z Q^T) / trace(Z)
         SGT_TRY(split_pair(st, Vk, c, Vks, keep, c));
@@ -1512,6 +1538,7 @@ int oz_round_impl(cudaStream_t st, int n, const double* const* W, const int64_t*
         SGT_LAUNCHED();
       }
     } else {
+    SGT_TRY(phase_mark(st, PH_EIG));
     // FP32 Jacobi on the leading part of Z: first approximation
     SGT_CUDA(cudaMemcpyAsync(Z32, Z.h, sizeof(float) * c * c, cudaMemcpyDeviceToDevice, st));
     {
@@ -1564,6 +1591,7 @@ int oz_round_impl(cudaStream_t st, int n, const double* const* W, const int64_t*
     SGT_LAUNCHED();
     }
     }  // bond matrix branches
+    SGT_TRY(phase_mark(st, PH_CARRY));
     // Ft_k (keep x r) = Vk Y^T with Y = Yt^T (r x c)
     Pair Y = Ytp;  // Ytp is free again
     SGT_TRY(pair_transpose(st, Y, c, 0, Yt, r, 0, c, r, 1));
@@ -1575,6 +1603,7 @@ int oz_round_impl(cudaStream_t st, int n, const double* const* W, const int64_t*
     oz_status_kernel<<<1, 32, 0, st>>>(stat, n, status, err);
     SGT_LAUNCHED();
   }
+  SGT_TRY(phase_mark(st, -1));
   return SGT_OK;
 }
 
@@ -1769,6 +1798,33 @@ extern "C" SGT_API int sgt_get_tuning(int key) {
   if (key == SGT_TUNE_SLICED_SPLIT_MIN_KTILES) return sgt::oz_split_min_ktiles();
   if (key == SGT_TUNE_PCHOL_BLOCKED) return __atomic_load_n(&sgt::g_pchol_blocked, __ATOMIC_RELAXED);
   return -1;
+}
+
+extern "C" SGT_API int sgt_phase_profile(int enable, double* ms, int count) {
+  if (enable) {
+    sgt::g_phase_on = true;
+    return SGT_OK;
+  }
+  sgt::g_phase_on = false;
+  double acc[sgt::PH_COUNT] = {};
+  int rc = SGT_OK;
+  for (size_t i = 0; i + 1 < sgt::g_phase_marks.size(); ++i) {
+    const auto& a = sgt::g_phase_marks[i];
+    if (a.phase < 0) continue;
+    float t = 0.f;
+    if (cudaEventSynchronize(sgt::g_phase_marks[i + 1].ev) != cudaSuccess ||
+        cudaEventElapsedTime(&t, a.ev, sgt::g_phase_marks[i + 1].ev) != cudaSuccess) {
+      sgt::set_error("phase_profile: event timing failed");
+      rc = SGT_ERR_CUDA;
+      break;
+    }
+    acc[a.phase] += t;
+  }
+  for (auto& m : sgt::g_phase_marks) cudaEventDestroy(m.ev);
+  sgt::g_phase_marks.clear();
+  if (ms)
+    for (int q = 0; q < count && q < sgt::PH_COUNT; ++q) ms[q] = acc[q];
+  return rc;
 }
 
 extern "C" SGT_API int sgt_sliced_profile(int enable, double* ms, double* flops, long long* launches) {
