@@ -175,6 +175,8 @@ int env_blocks_impl(cudaStream_t st, int n, const double* const* W, const int64_
     sx[k] = {xs[3 * k], xs[3 * k + 1], xs[3 * k + 2]};
     sy[k] = {ys[3 * k], ys[3 * k + 1], ys[3 * k + 2]};
     sw[k] = {ws4[4 * k], ws4[4 * k + 1], ws4[4 * k + 2], ws4[4 * k + 3]};
+  }
+  for (int k = 0; k < n; ++k) {
     SGT_REQUIRE(sx[k].l > 0 && sx[k].p > 0 && sx[k].r > 0 && sy[k].l > 0 && sy[k].p > 0 && sy[k].r > 0 &&
                     sw[k].l > 0 && sw[k].i > 0 && sw[k].o > 0 && sw[k].r > 0,
                 SGT_ERR_INVALID, "env_blocks: non-positive extent at site %d", k);

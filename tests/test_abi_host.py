@@ -199,3 +199,34 @@ def test_sliced_split_tuning_host_only(lib):
     finally:
         lib.sgt_set_tuning(L.TUNE_SLICED_SPLIT_CTAS, before)
         lib.sgt_set_tuning(L.TUNE_SLICED_SPLIT_MIN_KTILES, 8)
+
+
+def test_env_blocks_size_queries_host_only(lib):
+    """The DMRG environment size queries check the chain on the host: a
+    consistent chain gives a size on both sides, a bond or leg mismatch 0."""
+    from oracle import tt_fp64 as O
+    from syngular_gb300 import _lib as L
+
+    rng = np.random.default_rng(1)
+    X = O.random_mps_cores(rng, 6, 2, 16)
+    W = O.random_mpo_cores(rng, 6, 2, 4)
+    ws, _w = L.i64_array([v for w in W for v in w.shape])
+    xs, _x = L.shape_array([c.shape for c in X])
+    for side in (0, 1):
+        assert lib.sgt_env_blocks_workspace_size(6, ws, xs, xs, side, 4) > 0
+    bad = [c.shape for c in X]
+    bad[3] = (bad[3][0], bad[3][1], bad[3][2] + 1)
+    bs, _b = L.shape_array(bad)
+    assert lib.sgt_env_blocks_workspace_size(6, ws, bs, xs, 0, 4) == 0
+    assert b"bond mismatch" in lib.sgt_last_error()
+    W3 = O.random_mpo_cores(rng, 6, 3, 4)
+    w3, _w3 = L.i64_array([v for w in W3 for v in w.shape])
+    assert lib.sgt_env_blocks_workspace_size(6, w3, xs, xs, 0, 4) == 0
+    ls, _l = L.i64_array([1, 1, 1])
+    m, _m = L.i64_array([1, 2, 2, 16])
+    w1, _1 = L.i64_array(list(W[0].shape))
+    w2, _2 = L.i64_array(list(W[1].shape))
+    rs, _r = L.i64_array([16, 4, 16])
+    assert lib.sgt_env_two_site_workspace_size(ls, m, w1, w2, rs) > 0
+    assert lib.sgt_env_two_site_workspace_size(None, m, w1, w2, rs) > 0
+    assert lib.sgt_env_two_site_workspace_size(ls, m, w1, w2, None) == 0   # right block needed (b3 = 4)
