@@ -611,16 +611,24 @@ __global__ void __launch_bounds__(256) pair_frob_trace_kernel(const float* __res
   }
 }
 
-// X = Z / |Z|_F (pair times a scalar)
-__global__ void pair_scale_by_kernel(const float* __restrict__ zh, const float* __restrict__ zl, int64_t n,
+// X = Z / (|Z|_F (1 + 2^-32)) + 2^-32 I for the dim x dim pair matrix Z: the
+// spectrum of Z scaled into [0, 1] and lifted by 2^-32, so that the products'
+// noise (eigenvalues of Z at ~-2^-40 |Z| where Z is rank-deficient) cannot
+// leave [0, 1], where the purification's X^2 and 2X - X^2 steps keep every
+// eigenvalue; a multiple of I changes no eigenvector.
+constexpr float PURIFY_LIFT = 2.3283064365386963e-10f;  // 2^-32
+
+__global__ void pair_scale_by_kernel(const float* __restrict__ zh, const float* __restrict__ zl, int64_t dim,
                                      const double* __restrict__ frob, float* __restrict__ xh, float* __restrict__ xl) {
   const double f = *frob;
-  const float inv = (f > 0.0) ? (float)(1.0 / f) : 0.f;
+  const float inv = (f > 0.0) ? (float)(1.0 / (f * (1.0 + (double)PURIFY_LIFT))) : 0.f;
+  const int64_t n = dim * dim;
   for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
     const float p = zh[i] * inv;
     const float pe = fmaf(zh[i], inv, -p) + zl[i] * inv;
     float a = p, b = pe;
     df_norm(a, b);
+    if (i % (dim + 1) == 0) df_add(a, b, PURIFY_LIFT, 0.f);
     xh[i] = a;
     xl[i] = b;
   }
@@ -1481,7 +1489,7 @@ int oz_round_impl(cudaStream_t st, int n, const double* const* W, const int64_t*
       SGT_TRY(phase_mark(st, PH_PURIFY));
       pair_frob_trace_kernel<<<RED_BLOCKS, 256, 0, st>>>(Z.h, Z.l, c, rpart, ticket, dscal, dscal + 1);
       SGT_LAUNCHED();
-      pair_scale_by_kernel<<<grid_for(c * c), 256, 0, st>>>(Z.h, Z.l, c * c, dscal, VV.h, VV.l);
+      pair_scale_by_kernel<<<grid_for(c * c), 256, 0, st>>>(Z.h, Z.l, c, dscal, VV.h, VV.l);
       SGT_LAUNCHED();
       Pair X = VV, X2 = T;
       SGT_CUDA(cudaMemsetAsync(ichoice, 0, 2 * sizeof(int), st));

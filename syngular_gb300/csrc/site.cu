@@ -36,24 +36,32 @@ __device__ __forceinline__ void outer_row(const double* __restrict__ u, int64_t 
       for (int t = 0; t < REG_TERMS; ++t)
         if (t < terms) va[t][0] = v[t * sv + k], va[t][1] = v[t * sv + k + 1];
     }
-    for (int j = threadIdx.x / hp; j < J2; j += jstep) {
+    // pointer walks (no 64-bit index products in the loop: on GB300 the FP64
+    // FMAs, two per output pair and term, are the bound, not HBM)
+    const int j0 = threadIdx.x / hp;
+    const double* up = u + j0;
+    double* op = out + (int64_t)j0 * K2 + k;
+    const int64_t ostep = (int64_t)jstep * K2;
+    for (int j = j0; j < J2; j += jstep, up += jstep, op += ostep) {
       double o0 = 0.0, o1 = 0.0;
       if (terms <= REG_TERMS) {
+        const double* ut = up;
 #pragma unroll
         for (int t = 0; t < REG_TERMS; ++t)
           if (t < terms) {
-            const double x = u[t * su + j];
+            const double x = *ut;
+            ut += su;
             o0 = fma(x, va[t][0], o0);
             o1 = fma(x, va[t][1], o1);
           }
       } else {
         for (int t = 0; t < terms; ++t) {
-          const double x = u[t * su + j];
+          const double x = up[t * su];
           o0 = fma(x, v[t * sv + k], o0);
           o1 = fma(x, v[t * sv + k + 1], o1);
         }
       }
-      *reinterpret_cast<double2*>(out + (int64_t)j * K2 + k) = make_double2(o0, o1);
+      *reinterpret_cast<double2*>(op) = make_double2(o0, o1);
     }
   } else {
     const int n = J2 * K2;

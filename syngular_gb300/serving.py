@@ -80,6 +80,7 @@ class RoundServer:
         self.completed: List[Job] = []
         self.rejected: List[Job] = []
         self._stop = threading.Event()
+        self._cancel = threading.Event()
         self._thread = threading.Thread(target=self._loop, daemon=True)
 
     # ---------------------------------------------------------------- sessions
@@ -96,7 +97,12 @@ class RoundServer:
         self._thread.start()
         return self
 
-    def stop(self):
+    def stop(self, cancel_pending: bool = False):
+        """Stop the loop once the work it holds is done; with
+        ``cancel_pending`` the jobs not yet admitted end at once with an error
+        (in-flight jobs still finish)."""
+        if cancel_pending:
+            self._cancel.set()
         self._stop.set()
         self._thread.join()
 
@@ -236,6 +242,14 @@ class RoundServer:
                 else:
                     still.append((job, ev, out, sidx, gr))
             self.inflight = still
+            if self._cancel.is_set() and self.pending:
+                now = time.perf_counter()
+                for j in self.pending:
+                    j.error = "cancelled: server stopped"
+                    j.end = now
+                    self.rejected.append(j)
+                    j.done.set()
+                self.pending = []
             # admit in arrival order while memory and slots allow
             admitted = []
             for j in self.pending:
