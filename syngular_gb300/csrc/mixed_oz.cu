@@ -776,6 +776,16 @@ __global__ void pair_diag_kernel(const float* __restrict__ h, const float* __res
 // rounding too: L is a well-conditioned basis without any sketch.  The
 // sliced GEMM then forms L^T X, whose rows lie in the projector's range to
 // its full accuracy.  used: c ints of scratch.
+// 1 / sqrt(pivot), or 0 for a pivot below 1/(2c): a rank-keep orthogonal
+// projector's greedy pivots stay >= 1/c (the Schur complement left after s
+// steps has trace keep - s over c - s diagonal entries), so a smaller one
+// means the projector had fewer than `keep` directions above the products'
+// noise (a bond matrix of lower numerical rank); that column of L is then 0
+// instead of noise amplified without bound, and its row of the basis stays 0.
+__device__ __forceinline__ float pc_inv_pivot(float b, int c) {
+  return b >= 0.5f / (float)c ? 1.f / sqrtf(b) : 0.f;
+}
+
 __global__ void __launch_bounds__(1024) pivoted_chol_kernel(const float* __restrict__ A, int c, int keep,
                                                             float* __restrict__ Lt, int* __restrict__ used) {
   extern __shared__ float pc_diag[];  // c floats
@@ -809,7 +819,7 @@ __global__ void __launch_bounds__(1024) pivoted_chol_kernel(const float* __restr
         if (s_val[w] > b || (s_val[w] == b && s_idx[w] < p)) b = s_val[w], p = s_idx[w];
       s_p = p;
       used[p] = 1;
-      s_inv = 1.f / sqrtf(fmaxf(b, 1e-30f));
+      s_inv = pc_inv_pivot(b, c);
     }
     __syncthreads();
     const int p = s_p;
@@ -909,7 +919,7 @@ __global__ void __launch_bounds__(PC_THREADS) pivoted_chol_cluster_kernel(const 
     k = pc_warp_max(k);
     const int p = pc_key_row(k);
     const int owner = p / R;
-    const float inv = 1.f / sqrtf(fmaxf(pc_key_value(k), 1e-30f));
+    const float inv = pc_inv_pivot(pc_key_value(k), c);
     // 2. the pivot's row of L; this CTA's part of A's pivot row
     const float* orow = cluster.map_shared_rank(crow + cb * keep, owner);
     for (int t = tid; t < s; t += PC_THREADS) prow[t] = orow[t];
@@ -1009,7 +1019,7 @@ __global__ void __launch_bounds__(1024) pchol_panel_kernel(const float* __restri
         if (s_val[w] > b || (s_val[w] == b && s_idx[w] < p)) b = s_val[w], p = s_idx[w];
       s_p[s - j0] = p;
       used[p] = 1;
-      s_inv = 1.f / sqrtf(fmaxf(b, 1e-30f));
+      s_inv = pc_inv_pivot(b, c);
     }
     __syncthreads();
     const int p = s_p[s - j0];
