@@ -306,6 +306,12 @@ __global__ void __launch_bounds__(OZ_THREADS, 1)
     const bool split = args.pstride != 0;
     float* chi = args.Chi + (int64_t)blockIdx.z * args.pstride;
     float* clo = args.Clo + (int64_t)blockIdx.z * args.pstride;
+    // Without beta, each warp's 32 x 32 block goes out through shared memory
+    // (the ring is idle once every MMA has completed): stored row by row, one
+    // 128-byte line per instruction, instead of one 4-byte word per row.
+    const bool coalesce = split || args.beta == 0.f;
+    float* st_h = reinterpret_cast<float*>(ring) + (size_t)q * (2 * 32 * 33);
+    float* st_l = st_h + 32 * 33;
 #pragma unroll 1
     for (int c0 = 0; c0 < OZ_BN; c0 += 32) {
       float v0[32], v1[32], v2[32], v3[32], v4[32];
@@ -320,7 +326,40 @@ __global__ void __launch_bounds__(OZ_THREADS, 1)
 #pragma unroll
         for (int i = 0; i < 32; ++i) v0[i] = v1[i] = v2[i] = v3[i] = v4[i] = 0.f;
       }
-      if (!ok || *(volatile int*)&s_fail || row >= args.M) continue;
+      if (!ok || __any_sync(0xffffffffu, *(volatile int*)&s_fail)) continue;  // warp-uniform
+      if (coalesce) {
+#pragma unroll
+        for (int i = 0; i < 32; ++i) {
+          float h = v0[i], l = 0.f;
+          pair_add(h, l, v1[i]);
+          pair_add(h, l, v2[i]);
+          pair_add(h, l, v3[i]);
+          l += v4[i];
+          const float hs = h + l;
+          l = l - (hs - h);
+          h = hs;
+          const float ph = h * args.alpha;
+          const float pl = fmaf(h, args.alpha, -ph) + l * args.alpha;
+          const int ex = ea + s_eb[c0 + i] - 12;
+          st_h[lane * 33 + i] = ldexpf(ph, ex);
+          st_l[lane * 33 + i] = ldexpf(pl, ex);
+        }
+        __syncwarp();
+        const int col = n0 + c0 + lane;
+        if (col < args.N) {
+#pragma unroll 4
+          for (int rr = 0; rr < 32; ++rr) {
+            const int r2 = m0 + q * 32 + rr;
+            if (r2 >= args.M) break;
+            const int64_t idx = (int64_t)r2 * args.ldc + col;
+            chi[idx] = st_h[rr * 33 + lane];
+            clo[idx] = st_l[rr * 33 + lane];
+          }
+        }
+        __syncwarp();
+        continue;
+      }
+      if (row >= args.M) continue;
 #pragma unroll
       for (int i = 0; i < 32; ++i) {
         const int col = n0 + c0 + i;
