@@ -508,10 +508,18 @@ __global__ void oz_status_kernel(const int* __restrict__ st, int n, int* __restr
   *out = r;
 }
 
-__global__ void identity_cores_f64_kernel(double* __restrict__ eye, const int* __restrict__ dims, int n, int stride) {
-  for (int k = blockIdx.x; k < n; k += gridDim.x) {
-    const int d = dims[k];
-    for (int i = threadIdx.x; i < d * d; i += blockDim.x) eye[(int64_t)k * stride + i] = (i / d == i % d) ? 1.0 : 0.0;
+// Identity operator cores eye[k] = I (d_k x d_k) for sites k0 .. k0 + count - 1;
+// the physical dims travel by value in the launch (no host buffer that a
+// captured graph would have to read again at replay).
+constexpr int EYE_CHUNK = 256;
+struct EyeDims {
+  int d[EYE_CHUNK];
+};
+__global__ void identity_cores_f64_kernel(double* __restrict__ eye, const EyeDims dims, int k0, int count, int stride) {
+  for (int j = blockIdx.x; j < count; j += gridDim.x) {
+    const int d = dims.d[j];
+    double* e = eye + (int64_t)(k0 + j) * stride;
+    for (int i = threadIdx.x; i < d * d; i += blockDim.x) e[i] = (i / d == i % d) ? 1.0 : 0.0;
   }
 }
 
@@ -1026,7 +1034,7 @@ __global__ void __launch_bounds__(1024) pchol_panel_kernel(const float* __restri
     const float inv = s_inv;
     for (int i = threadIdx.x; i < c; i += blockDim.x) {
       float v = Aw[(int64_t)p * c + i];
-      for (int t = j0; t < s; ++t) v -= Lt[(int64_t)t * c + i] * Lt[(int64_t)t * c + s_p[t - j0]];
+      for (int t = j0; t < s; ++t) v -= Lt[(int64_t)t * c + i] * Lt[(int64_t)t * c + p];
       const float l = v * inv;
       Lt[(int64_t)s * c + i] = l;
       d[i] -= l * l;
@@ -1642,13 +1650,16 @@ int oz_round_chain(cudaStream_t st, int n, const double* const* X, const int64_t
     dmax = std::max(dmax, d);
   }
   double* eye = ar.take<double>((size_t)n * dmax * dmax);
-  int* ddims = ar.take<int>((size_t)n);
   std::vector<const double*> W(n, nullptr);
   if (!ar.measure) {
     SGT_REQUIRE(ar.ok(), SGT_ERR_WORKSPACE, "round: workspace too small");
-    SGT_CUDA(cudaMemcpyAsync(ddims, dims.data(), sizeof(int) * n, cudaMemcpyHostToDevice, st));
-    identity_cores_f64_kernel<<<(unsigned)std::min(n, 1024), 128, 0, st>>>(eye, ddims, n, (int)(dmax * dmax));
-    SGT_LAUNCHED();
+    for (int k0 = 0; k0 < n; k0 += EYE_CHUNK) {
+      EyeDims ed;
+      const int count = std::min(EYE_CHUNK, n - k0);
+      for (int j = 0; j < count; ++j) ed.d[j] = dims[k0 + j];
+      identity_cores_f64_kernel<<<(unsigned)count, 128, 0, st>>>(eye, ed, k0, count, (int)(dmax * dmax));
+      SGT_LAUNCHED();
+    }
     for (int k = 0; k < n; ++k) W[k] = eye + (int64_t)k * dmax * dmax;
   }
   return oz_round_impl(st, n, W.data(), w4.data(), X, xs, chi, out, spectra, discarded, status, ar);

@@ -135,8 +135,7 @@ def test_repeated_jobs_replay_graphs(precision):
     for kind in ("round", "add_round", "overlap"):
         runs = []
         for rep in range(3):
-            j = Job(kind=kind, session="s0", other="s1" if kind != "round" else "s0", chi=5,
-                    precision=precision, job_id=rep)
+            j = Job(kind=kind, session="s0", other="s0", chi=5, precision=precision, job_id=rep)
             srv.submit(j)
             assert j.done.wait(120) and j.error is None, j.error
             runs.append(summary(j))
