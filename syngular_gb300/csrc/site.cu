@@ -2,9 +2,10 @@
 // (bond concatenation) kernel and small elementwise helpers.
 //
 // The contractions are outer-product expansions with a tiny inner dimension
-// (the physical leg), so they are bound by the HBM write of the product core:
-// each thread produces two adjacent outputs of one row and stores them as a
-// 16-byte vector when the row is even-sized.
+// (the physical leg): each thread produces two adjacent outputs of one row and
+// stores them as a 16-byte vector when the row is even-sized.  On GB300 they
+// are bound by the FP64 FMA rate (p FMAs per 8-byte output, ~0.6 TFMA/s for
+// the chip) before the HBM write of the product core.
 #include <algorithm>
 
 #include "common.cuh"
@@ -12,95 +13,76 @@
 namespace sgt {
 namespace {
 
-// One output row of a site contraction:
-//   out[j * K2 + k] = sum_t u[t * su + j] * v[t * sv + k],  j < J2, k < K2,
-// with few terms t (the physical leg).  The row is written once, so the
-// kernels are bound by the HBM write of the product core.  Vector path (K2
-// even, 16-byte aligned row): the block has a multiple of K2/2 threads, each
-// thread owns one fixed column pair k, k+1 (its v values stay in registers)
-// and walks j with a constant stride, so no index division happens inside
-// the row and every store is 16 bytes, consecutive threads on consecutive
-// addresses.  Scalar path otherwise (32-bit index arithmetic).
-template <int REG_TERMS>
-__device__ __forceinline__ void outer_row(const double* __restrict__ u, int64_t su, const double* __restrict__ v,
-                                          int64_t sv, int terms, int J2, int K2, double* __restrict__ out,
-                                          bool vec) {
-  const int T = blockDim.x;
+// P[(a*B+b), o, (a2*B2+b2)] = sum_i X[a,i,a2] * W[b,i,o,b2]
+// grid.y enumerates rows r = (a*B + b)*O + o (chunked in z for > 65535 rows).
+__global__ void contract_mpo_mps_kernel(const double* __restrict__ X, const double* __restrict__ W,
+                                        double* __restrict__ P, int64_t Bd, int64_t I, int64_t O,
+                                        int64_t A2, int64_t B2, int64_t rows, bool vec) {
+  const int64_t r = (int64_t)blockIdx.y + (int64_t)blockIdx.z * 65535;
+  if (r >= rows) return;
+  const int64_t o = r % O;
+  const int64_t ab = r / O;
+  const int64_t b = ab % Bd, a = ab / Bd;
+  const int64_t ncol = A2 * B2;
+  const int64_t c0 = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) * 2;
+  if (c0 >= ncol) return;
+  const double* xr = X + a * I * A2;           // X[a, :, :]
+  const double* wr = W + (b * I * O + o) * B2;  // W[b, 0, o, :], stride over i = O*B2
+  double v[2];
+#pragma unroll
+  for (int e = 0; e < 2; ++e) {
+    int64_t c = c0 + e;
+    double acc = 0.0;
+    if (c < ncol) {
+      int64_t a2 = c / B2, b2 = c % B2;
+      for (int64_t i = 0; i < I; ++i) acc = fma(xr[i * A2 + a2], wr[i * O * B2 + b2], acc);
+    }
+    v[e] = acc;
+  }
+  double* out = P + r * ncol + c0;
   if (vec) {
-    const int hp = K2 >> 1;
-    const int k = (threadIdx.x % hp) * 2;
-    const int jstep = T / hp;
-    double va[REG_TERMS][2];
-    if (terms <= REG_TERMS) {
-#pragma unroll
-      for (int t = 0; t < REG_TERMS; ++t)
-        if (t < terms) va[t][0] = v[t * sv + k], va[t][1] = v[t * sv + k + 1];
-    }
-    // pointer walks (no 64-bit index products in the loop: on GB300 the FP64
-    // FMAs, two per output pair and term, are the bound, not HBM)
-    const int j0 = threadIdx.x / hp;
-    const double* up = u + j0;
-    double* op = out + (int64_t)j0 * K2 + k;
-    const int64_t ostep = (int64_t)jstep * K2;
-    for (int j = j0; j < J2; j += jstep, up += jstep, op += ostep) {
-      double o0 = 0.0, o1 = 0.0;
-      if (terms <= REG_TERMS) {
-        const double* ut = up;
-#pragma unroll
-        for (int t = 0; t < REG_TERMS; ++t)
-          if (t < terms) {
-            const double x = *ut;
-            ut += su;
-            o0 = fma(x, va[t][0], o0);
-            o1 = fma(x, va[t][1], o1);
-          }
-      } else {
-        for (int t = 0; t < terms; ++t) {
-          const double x = up[t * su];
-          o0 = fma(x, v[t * sv + k], o0);
-          o1 = fma(x, v[t * sv + k + 1], o1);
-        }
-      }
-      *reinterpret_cast<double2*>(op) = make_double2(o0, o1);
-    }
+    *reinterpret_cast<double2*>(out) = make_double2(v[0], v[1]);
   } else {
-    const int n = J2 * K2;
-    for (int c = threadIdx.x; c < n; c += T) {
-      const int j = c / K2, k = c - j * K2;
-      double acc = 0.0;
-      for (int t = 0; t < terms; ++t) acc = fma(u[t * su + j], v[t * sv + k], acc);
-      out[c] = acc;
-    }
+    out[0] = v[0];
+    if (c0 + 1 < ncol) out[1] = v[1];
   }
 }
 
-// P[(a*B+b), o, (a2*B2+b2)] = sum_i X[a,i,a2] * W[b,i,o,b2]; one block per
-// output row r = (a*B + b)*O + o.
-__global__ void __launch_bounds__(256) contract_mpo_mps_kernel(const double* __restrict__ X,
-                                                               const double* __restrict__ W, double* __restrict__ P,
-                                                               int64_t Bd, int64_t I, int64_t O, int64_t A2,
-                                                               int64_t B2, bool vec) {
-  const int64_t r = blockIdx.x;
-  const int64_t o = r % O, ab = r / O;
-  const int64_t b = ab % Bd, a = ab / Bd;
-  outer_row<4>(X + a * I * A2, A2, W + (b * I * O + o) * B2, O * B2, (int)I, (int)A2, (int)B2,
-               P + r * A2 * B2, vec);
-}
-
-// P[(b*C+c), i, o, (b2*C2+c2)] = sum_m A[b,i,m,b2] * B[c,m,o,c2]; one block
-// per output row r = ((b*C + c)*I + i)*O + o.
-__global__ void __launch_bounds__(256) contract_mpo_mpo_kernel(const double* __restrict__ A,
-                                                               const double* __restrict__ Bm, double* __restrict__ P,
-                                                               int64_t Cd, int64_t I, int64_t Mm, int64_t O,
-                                                               int64_t B2, int64_t C2, bool vec) {
-  const int64_t r = blockIdx.x;
+// P[(b*C+c), i, o, (b2*C2+c2)] = sum_m A[b,i,m,b2] * B[c,m,o,c2]
+// rows r = ((b*C + c)*I + i)*O + o
+__global__ void contract_mpo_mpo_kernel(const double* __restrict__ A, const double* __restrict__ Bm,
+                                        double* __restrict__ P, int64_t Cd, int64_t I, int64_t Mm,
+                                        int64_t O, int64_t B2, int64_t C2, int64_t rows, bool vec) {
+  const int64_t r = (int64_t)blockIdx.y + (int64_t)blockIdx.z * 65535;
+  if (r >= rows) return;
   const int64_t o = r % O;
   int64_t t = r / O;
   const int64_t i = t % I;
   t /= I;
   const int64_t c = t % Cd, b = t / Cd;
-  outer_row<4>(A + (b * I + i) * Mm * B2, B2, Bm + c * Mm * O * C2 + o * C2, O * C2, (int)Mm, (int)B2, (int)C2,
-               P + r * B2 * C2, vec);
+  const int64_t ncol = B2 * C2;
+  const int64_t c0 = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) * 2;
+  if (c0 >= ncol) return;
+  const double* ar = A + (b * I + i) * Mm * B2;  // A[b, i, :, :]
+  const double* br = Bm + c * Mm * O * C2 + o * C2;  // B[c, 0, o, :], stride over m = O*C2
+  double v[2];
+#pragma unroll
+  for (int e = 0; e < 2; ++e) {
+    int64_t cc = c0 + e;
+    double acc = 0.0;
+    if (cc < ncol) {
+      int64_t b2 = cc / C2, c2 = cc % C2;
+      for (int64_t m = 0; m < Mm; ++m) acc = fma(ar[m * B2 + b2], br[m * O * C2 + c2], acc);
+    }
+    v[e] = acc;
+  }
+  double* out = P + r * ncol + c0;
+  if (vec) {
+    *reinterpret_cast<double2*>(out) = make_double2(v[0], v[1]);
+  } else {
+    out[0] = v[0];
+    if (c0 + 1 < ncol) out[1] = v[1];
+  }
 }
 
 struct ConcatSite {
@@ -208,18 +190,13 @@ inline unsigned grid_for(int64_t n, int threads) {
   return (unsigned)std::max<int64_t>(1, std::min<int64_t>(cdiv(n, threads), 152 * 16));
 }
 
-// Block shape of a row kernel: rows blocks; with the vector path a multiple
-// of K2/2 threads (<= 256), else 32..256 threads.
-int launch_rows(int64_t rows, int64_t J2, int64_t K2, bool& vec, unsigned& blocks, int& threads) {
-  SGT_REQUIRE(rows <= 0x7fffffff && J2 * K2 <= 0x7fffffff, SGT_ERR_INVALID, "site contraction too large");
-  blocks = (unsigned)rows;
-  const int64_t hp = K2 / 2;
-  vec = vec && K2 % 2 == 0 && hp <= 256;
-  if (vec) {
-    threads = (int)(hp * std::max<int64_t>(1, std::min<int64_t>(256 / hp, J2)));
-  } else {
-    threads = (int)std::min<int64_t>(256, std::max<int64_t>(32, cdiv(J2 * K2, 32) * 32));
-  }
+int launch_rows(int64_t rows, int64_t ncol, dim3& grid, int& threads) {
+  threads = ncol >= 512 ? 256 : 128;
+  int64_t gx = cdiv(cdiv(ncol, 2), threads);
+  int64_t gy = std::min<int64_t>(rows, 65535);
+  int64_t gz = cdiv(rows, 65535);
+  SGT_REQUIRE(gx <= 0x7fffffff && gz <= 65535, SGT_ERR_INVALID, "site contraction too large");
+  grid = dim3((unsigned)gx, (unsigned)gy, (unsigned)gz);
   return SGT_OK;
 }
 
@@ -261,11 +238,11 @@ int site_contract_mpo_mps(cudaStream_t st, const double* X, int64_t a, int64_t p
                           const double* W, int64_t b, int64_t o, int64_t b2, double* P) {
   int64_t rows = a * b * o, ncol = a2 * b2;
   if (rows == 0 || ncol == 0) return SGT_OK;
-  bool vec = (reinterpret_cast<uintptr_t>(P) & 15) == 0;
-  unsigned blocks;
+  dim3 grid;
   int threads;
-  SGT_TRY(launch_rows(rows, a2, b2, vec, blocks, threads));
-  contract_mpo_mps_kernel<<<blocks, threads, 0, st>>>(X, W, P, b, p, o, a2, b2, vec);
+  SGT_TRY(launch_rows(rows, ncol, grid, threads));
+    const bool vec = (ncol % 2 == 0) && ((reinterpret_cast<uintptr_t>(P) & 15) == 0);
+  contract_mpo_mps_kernel<<<grid, threads, 0, st>>>(X, W, P, b, p, o, a2, b2, rows, vec);
   SGT_LAUNCHED();
   return SGT_OK;
 }
@@ -274,11 +251,11 @@ int site_contract_mpo_mpo(cudaStream_t st, const double* A, int64_t b, int64_t i
                           int64_t b2, const double* B, int64_t c, int64_t o, int64_t c2, double* P) {
   int64_t rows = b * c * i * o, ncol = b2 * c2;
   if (rows == 0 || ncol == 0) return SGT_OK;
-  bool vec = (reinterpret_cast<uintptr_t>(P) & 15) == 0;
-  unsigned blocks;
+  dim3 grid;
   int threads;
-  SGT_TRY(launch_rows(rows, b2, c2, vec, blocks, threads));
-  contract_mpo_mpo_kernel<<<blocks, threads, 0, st>>>(A, B, P, c, i, m, o, b2, c2, vec);
+  SGT_TRY(launch_rows(rows, ncol, grid, threads));
+    const bool vec = (ncol % 2 == 0) && ((reinterpret_cast<uintptr_t>(P) & 15) == 0);
+  contract_mpo_mpo_kernel<<<grid, threads, 0, st>>>(A, B, P, c, i, m, o, b2, c2, rows, vec);
   SGT_LAUNCHED();
   return SGT_OK;
 }
