@@ -39,6 +39,17 @@ class Instance:
         self.rmax = max(max(p[0], p[2]) for p in self.pshapes)
 
 
+def _work_estimate(inst: "Instance") -> float:
+    """Leading cost of one instance's rounding: per bond the product of the
+    bond matrix's side (d chi) and the squared product bond (the Gram-step and
+    bond-matrix products)."""
+    tot = 0.0
+    for p in inst.pshapes:
+        r, d, r2 = p
+        tot += float(r) * float(r) * float(d) * float(min(r2, inst.chi))
+    return tot
+
+
 class BatchedRound:
     def __init__(self, instances: List[Instance], precision: int = L.PREC_TF32X3, streams: int = 4,
                  budget_bytes: int = 160 << 30, spectra: bool = True):
@@ -72,15 +83,18 @@ class BatchedRound:
             outsh, _o = L.shape_array([tuple(o.shape) for o in inst.out])
             ovl_need = L.query("sgt_overlap_workspace_size", n, xsh, outsh)
             inst.ws_need = max(need, ovl_need)
-        # deal instances to streams, largest first, onto the least loaded stream
+        # deal instances to streams, most work first, onto the least loaded
+        # stream (longest-processing-time order); the work estimate is the
+        # rounding's leading term, sum over bonds of (product bond)^2 x (d chi)
         S = max(1, int(streams))
-        order = sorted(range(len(instances)), key=lambda i: -instances[i].ws_need)
+        work = [_work_estimate(inst) for inst in instances]
+        order = sorted(range(len(instances)), key=lambda i: -work[i])
         self.lanes: List[List[int]] = [[] for _ in range(S)]
         load = [0.0] * S
         for i in order:
             s = min(range(S), key=lambda j: load[j])
             self.lanes[s].append(i)
-            load[s] += instances[i].ws_need
+            load[s] += work[i]
         self.lanes = [lane for lane in self.lanes if lane]
         lane_ws = [max(instances[i].ws_need for i in lane) for lane in self.lanes]
         if sum(lane_ws) > budget_bytes:
