@@ -69,7 +69,8 @@ __global__ void pair_to_f64_kernel(const float* __restrict__ h, const float* __r
 // src[b]^T (rows x cols, lds); batch strides sb / db.
 __global__ void pair_transpose_kernel(float* __restrict__ dh, float* __restrict__ dl, int64_t ldd, int64_t db,
                                       const float* __restrict__ sh, const float* __restrict__ sl, int64_t lds,
-                                      int64_t sb, int64_t rows, int64_t cols) {
+                                      int64_t sb, int64_t rows, int64_t cols, const int* __restrict__ skip) {
+  if (skip && *skip) return;  // uniform for the grid, before any barrier
   __shared__ float th[32][33], tl[32][33];
   const int64_t b = blockIdx.z;
   sh += b * sb;
@@ -984,8 +985,38 @@ __global__ void __launch_bounds__(256) kept_trace_kernel(const float* __restrict
 // status word of a projector bond: 0 when X converged to a projector
 // (the loop stopped, or its last |X^2 - X| is at most 2^-30), -1 otherwise
 __global__ void tc2_status_kernel(const int* __restrict__ ctl, const unsigned* __restrict__ resid,
-                                  int* __restrict__ st) {
-  *st = (ctl[1] || __uint_as_float(*resid) <= ldexpf(1.f, -30)) ? 0 : -1;
+                                  const unsigned* __restrict__ mcw_resid, int* __restrict__ st) {
+  *st = (ctl[1] || __uint_as_float(*resid) <= ldexpf(1.f, -30) || __uint_as_float(*mcw_resid) <= ldexpf(1.f, -30))
+            ? 0
+            : -1;
+}
+
+// One McWeeny step X <- 3 X2 - 2 X3 (X2 = X X, X3 = X2 X, pair arithmetic),
+// run only when the trace-correcting steps did not reach a projector (ctl[1]
+// unset): that happens when the bond matrix has fewer directions above the
+// products' noise than `keep`, and the noise eigenvalues form a cluster that
+// no trace correction can split within the step budget.  McWeeny's map sends
+// eigenvalues below 1/2 to 0 and above to 1 (quadratically), so X becomes the
+// projector onto the significant directions (rank below keep); the basis then
+// has zero rows for the rest (the pivot guard), which carry no weight.  The
+// largest |change| goes to *resid.
+__global__ void __launch_bounds__(256) mcweeny_step_kernel(float* __restrict__ xh, float* __restrict__ xl,
+                                                          const float* __restrict__ x2h, const float* __restrict__ x2l,
+                                                          const float* __restrict__ x3h, const float* __restrict__ x3l,
+                                                          int64_t count, const int* __restrict__ ctl,
+                                                          unsigned* __restrict__ resid) {
+  if (ctl[1]) return;
+  float worst = 0.f;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < count; i += (int64_t)gridDim.x * blockDim.x) {
+    const float p = 3.f * x2h[i];
+    float h = p, l = fmaf(3.f, x2h[i], -p) + 3.f * x2l[i];
+    df_add(h, l, -2.f * x3h[i], -2.f * x3l[i]);
+    worst = fmaxf(worst, fabsf((h - xh[i]) + (l - xl[i])));
+    xh[i] = h;
+    xl[i] = l;
+  }
+  for (int o = 16; o > 0; o >>= 1) worst = fmaxf(worst, __shfl_xor_sync(0xffffffffu, worst, o));
+  if ((threadIdx.x & 31) == 0 && worst > 0.f) atomicMax(resid, __float_as_uint(worst));
 }
 
 // Blocked right-looking form of the same factorisation, for projectors whose
@@ -1159,7 +1190,9 @@ struct Site4 {
 // projector; about 2 log2(|Z|_F / gap at the cut) + 6 are needed, ~45 at the
 // benchmark's bonds) and Newton-Schulz steps.
 constexpr int TC2_ITERS = 90;
+constexpr int MCW_ITERS = 6;  // McWeeny clean-up steps, skipped when the purification converged
 constexpr int NS_ITERS = 2;
+constexpr int NS_EXTRA = 4;   // Newton-Schulz steps after an unconverged purification
 
 // Pair matrix buffers (hi, lo) carved from the arena.
 struct Pair {
@@ -1189,18 +1222,20 @@ Sliced take_sliced(Arena& ar, int64_t rows, int64_t cols) {
   return q;
 }
 
-int split_pair(cudaStream_t st, const Pair& p, int64_t ld, Sliced& q, int64_t rows, int64_t cols) {
+// `skip` (device int, may be null): nonzero at launch time makes the call a no-op
+int split_pair(cudaStream_t st, const Pair& p, int64_t ld, Sliced& q, int64_t rows, int64_t cols,
+               const int* skip = nullptr) {
   q.rows = rows;
   q.cols = cols;
-  return oz_split_pair(st, p.h, p.l, ld, rows, cols, q.s, q.e, 1);
+  return oz_split_pair(st, p.h, p.l, ld, rows, cols, q.s, q.e, 1, skip);
 }
 
 int pair_transpose(cudaStream_t st, Pair dst, int64_t ldd, int64_t db, Pair src, int64_t lds, int64_t sb, int64_t rows,
-                   int64_t cols, int64_t batch) {
+                   int64_t cols, int64_t batch, const int* skip = nullptr) {
   if (rows <= 0 || cols <= 0 || batch <= 0) return SGT_OK;
   const int64_t tiles = cdiv(rows, 32) * cdiv(cols, 32);
   dim3 g((unsigned)std::min<int64_t>(tiles, 1024), 1, (unsigned)batch);
-  pair_transpose_kernel<<<g, dim3(32, 8), 0, st>>>(dst.h, dst.l, ldd, db, src.h, src.l, lds, sb, rows, cols);
+  pair_transpose_kernel<<<g, dim3(32, 8), 0, st>>>(dst.h, dst.l, ldd, db, src.h, src.l, lds, sb, rows, cols, skip);
   SGT_LAUNCHED();
   return SGT_OK;
 }
@@ -1335,6 +1370,7 @@ int oz_round_impl(cudaStream_t st, int n, const double* const* W, const int64_t*
   double* rpart = ar.take<double>(2 * RED_BLOCKS);
   unsigned* ticket = ar.take<unsigned>(1);
   unsigned* tc2_resid = ar.take<unsigned>(TC2_ITERS);  // purification: largest |X^2 - X| of each step
+  unsigned* mcw_resid = ar.take<unsigned>(MCW_ITERS);  // McWeeny clean-up: largest change of each step
   float* tc2_diag = ar.take<float>((size_t)(4 * cmax));  // purification: X's diagonal, two buffers
   // split-K partials: the largest requirement of the products below
   size_t part_bytes = 0;
@@ -1530,7 +1566,24 @@ int oz_round_impl(cudaStream_t st, int n, const double* const* W, const int64_t*
                                              Vts.s, oz_ld(c), c * oz_ld(c), Vts.e);
         SGT_LAUNCHED();
       }
-      tc2_status_kernel<<<1, 1, 0, st>>>(ichoice, tc2_resid + (TC2_ITERS - 1), stat + k);
+      // McWeeny clean-up of a projector the trace correction could not finish
+      // (every launch returns at once when ctl[1] says it did)
+      SGT_CUDA(cudaMemsetAsync(mcw_resid, 0, sizeof(unsigned) * MCW_ITERS, st));
+      for (int it = 0; it < MCW_ITERS; ++it) {
+        SGT_TRY(oz_gemm(st, c, c, c, 1.f, Vts.mat(), Vts.mat(), 0.f, X2.h, X2.l, c, part, part_floats, err,
+                        ichoice + 1));                                            // X2 = X X
+        SGT_TRY(oz_split_pair(st, X2.h, X2.l, c, c, c, Ts.s, Ts.e, 1, ichoice + 1));
+        Ts.rows = c;
+        Ts.cols = c;
+        SGT_TRY(oz_gemm(st, c, c, c, 1.f, Ts.mat(), Vts.mat(), 0.f, S.h, S.l, c, part, part_floats, err,
+                        ichoice + 1));                                            // X3 = X2 X
+        mcweeny_step_kernel<<<grid_for(c * c), 256, 0, st>>>(X.h, X.l, X2.h, X2.l, S.h, S.l, c * c, ichoice,
+                                                              mcw_resid + it);
+        SGT_LAUNCHED();
+        SGT_TRY(oz_split_pair(st, X.h, X.l, c, c, c, Vts.s, Vts.e, 1, ichoice + 1));
+      }
+      tc2_status_kernel<<<1, 1, 0, st>>>(ichoice, tc2_resid + (TC2_ITERS - 1), mcw_resid + (MCW_ITERS - 1),
+                                         stat + k);
       SGT_LAUNCHED();
       pair_symmetrize_kernel<<<grid_for(c * c), 256, 0, st>>>(X.h, X.l, c);
       SGT_LAUNCHED();
@@ -1542,14 +1595,17 @@ int oz_round_impl(cudaStream_t st, int n, const double* const* W, const int64_t*
       Ets.cols = c;
       SGT_TRY(split_pair(st, X, c, Vts, c, c));
       SGT_TRY(gemm(keep, c, c, 1.f, Ets.mat(), Vts.mat(), 0.f, Vk, c));
-      // Newton-Schulz: Q <- 1.5 Q - 0.5 (Q Q^T) Q
-      for (int it = 0; it < NS_ITERS; ++it) {
-        SGT_TRY(split_pair(st, Vk, c, Vks, keep, c));
-        SGT_TRY(gemm(keep, keep, c, 1.f, Vks.mat(), Vks.mat(), 0.f, S, keep));
-        SGT_TRY(split_pair(st, S, keep, Ts, keep, keep));
-        SGT_TRY(pair_transpose(st, Xv, keep, 0, Vk, c, 0, keep, c, 1));
-        SGT_TRY(split_pair(st, Xv, keep, Xvs, c, keep));
-        SGT_TRY(gemm(keep, c, keep, -0.5f, Ts.mat(), Xvs.mat(), 1.5f, Vk, c));
+      // Newton-Schulz: Q <- 1.5 Q - 0.5 (Q Q^T) Q; after a purification that
+      // needed the McWeeny clean-up the start is further from orthonormal, and
+      // NS_EXTRA more steps run (skipped on the device otherwise)
+      for (int it = 0; it < NS_ITERS + NS_EXTRA; ++it) {
+        const int* sk = it < NS_ITERS ? nullptr : ichoice + 1;
+        SGT_TRY(split_pair(st, Vk, c, Vks, keep, c, sk));
+        SGT_TRY(oz_gemm(st, keep, keep, c, 1.f, Vks.mat(), Vks.mat(), 0.f, S.h, S.l, keep, part, part_floats, err, sk));
+        SGT_TRY(split_pair(st, S, keep, Ts, keep, keep, sk));
+        SGT_TRY(pair_transpose(st, Xv, keep, 0, Vk, c, 0, keep, c, 1, sk));
+        SGT_TRY(split_pair(st, Xv, keep, Xvs, c, keep, sk));
+        SGT_TRY(oz_gemm(st, keep, c, keep, -0.5f, Ts.mat(), Xvs.mat(), 1.5f, Vk.h, Vk.l, c, part, part_floats, err, sk));
       }
       pair_to_f64_kernel<<<grid_for(keep * c), 256, 0, st>>>(Vk.h, Vk.l, c, out[k], c, keep, c);
       SGT_LAUNCHED();

@@ -70,6 +70,10 @@ class RoundServer:
         self.graphs: Dict[tuple, "_Graph"] = {}
         self.graph_bytes = 0
         self.replayed = 0
+        # admission: pending jobs looked at per pass, and how long a job that
+        # waits for memory lets later jobs pass it
+        self.scan = 256
+        self.max_bypass_s = 2.0
         self.sessions: Dict[str, dict] = {}
         self.inbox: "queue.Queue[Job]" = queue.Queue()
         self.streams = [torch.cuda.Stream() for _ in range(self.slots)]
@@ -250,12 +254,19 @@ class RoundServer:
                     self.rejected.append(j)
                     j.done.set()
                 self.pending = []
-            # admit in arrival order while memory and slots allow
+            # admit in arrival order while memory and slots allow; a job that
+            # does not fit the memory left lets later, smaller jobs pass
+            # (backfill) for at most max_bypass_s, then admission waits for it
             admitted = []
-            for j in self.pending:
+            now = time.perf_counter()
+            for j in self.pending[: self.scan]:
                 if not self.free_streams:
                     break
                 if self.used + j._need > self.budget:
+                    if getattr(j, "_blocked", None) is None:
+                        j._blocked = now
+                    if now - j._blocked < self.max_bypass_s:
+                        continue
                     break
                 sidx = self.free_streams.pop()
                 self.used += j._need

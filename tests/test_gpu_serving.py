@@ -151,3 +151,24 @@ def test_repeated_jobs_replay_graphs(precision):
     for kind, runs in results.items():
         np.testing.assert_allclose(runs, [runs[0]] * 3, rtol=1e-12, atol=0, err_msg=kind)
     np.testing.assert_allclose([summary(j) for j in burst], [results["round"][0]] * 2, rtol=1e-12, atol=0)
+
+
+def test_small_job_passes_a_job_waiting_for_memory():
+    """Backfill: with room for one round job, a second round job waits for
+    memory while a later overlap job that fits is admitted at once."""
+    from syngular_gb300.serving import Job
+
+    rng = np.random.default_rng(23)
+    srv = server_with_sessions(rng, 3, slots=4)
+    a = Job(kind="round", session="s0", chi=8, precision=0, job_id=0)
+    b = Job(kind="round", session="s0", chi=8, precision=0, job_id=1)
+    small = Job(kind="overlap", session="s1", other="s1", job_id=2)
+    f_round, f_small = srv.footprint(a), srv.footprint(small)
+    srv.budget = f_round + 2 * f_small  # one round job at a time, with room for the overlap
+    for j in (a, b, small):
+        srv.submit(j)
+    srv.start()
+    for j in (a, b, small):
+        assert j.done.wait(120) and j.error is None, j.error
+    srv.stop()
+    assert small.start < b.start
