@@ -58,7 +58,9 @@ extern "C" {
 #define SGT_PREC_BF16X6 5  /* FP64-class: every operand row cut exactly into six 7-bit bf16 slices,
                               the 21 leading slice products on tcgen05 kind::f16 accumulated exactly
                               in TMEM (~2^-41 of the operands' scale); elementwise work in FP32 pairs;
-                              FP32 Jacobi eigenvectors refined against the pair-accurate bond matrix */
+                              kept subspaces by purification on that GEMM (or, when spectra are asked
+                              for, FP32 Jacobi eigenvectors refined against the pair-accurate bond
+                              matrix) */
 
 SGT_API int sgt_version(void);
 SGT_API const char* sgt_last_error(void);
