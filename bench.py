@@ -6,19 +6,21 @@ bond D=16 (entries N(0,1)/sqrt(D*d)), both seeded and synthetic.  A sweep is
 the raw product W @ X (bond chi*D = 4096), its TT-SVD rounding back to chi=256
 and the overlap <X|Z> of the rounded state with the input.
 
-  value       sweeps/s of the chosen form (default: 3xTF32 Gram form on tcgen05)
-              with the cores already resident in HBM
-  e2e         the same through the public call with the input cores copied
-              from pinned host memory every step and <X|Z> read back
+  value       sweeps/s of the chosen form (default: BF16X6, FP64-class on the
+              bf16 tensor cores) with the cores already resident in HBM
+  e2e         the same through the public API ((W @ X) >> chi, X | Z) with the
+              input cores copied from pinned host memory every step and <X|Z>
+              read back
+  latency     p50/p99 per job (one job = one sweep), on the device and through
+              the API
   plain_fp64  sweeps/s of the plain FP64 GPU form (Householder QR + FP64
-              Jacobi), the denominator of the metric
-  roofline    the contraction kernel (the tcgen05 GEMM) against the tensor
-              pipe, timed with CUDA events over the timed region
-  dominant_kernel  the kernel with most of the step (the cluster-resident
-              FP32 bond eigensolver), timed the same way: mean launch time,
-              share of the step, FP32 rate against the nominal CUDA-core rate
-  cpu_baseline the numpy FP64 port of the same sweep on the host cores, on a
-              bounded sample (one full-size middle site), scaled by flops
+              Jacobi), the denominator of the metric, and the error of the
+              chosen form against it
+  roofline    the sliced tensor-core GEMM against the measured bf16 peak,
+              timed with CUDA events over the timed region
+  phases_ms   one extra sweep split by the rounding's phases (CUDA events)
+  cpu_baseline the numpy FP64 port of the same sweep on the host cores: one
+              whole measured sweep, plus a 1-thread figure
 
 `--impl reference` times that CPU port alone (the reference itself is pure
 Python/numpy and has no GPU path; its own MPS/MPO code cannot run this
@@ -46,7 +48,7 @@ METRIC = "MPO·MPS+SVD-round sweeps/s at χ=256 vs plain FP64 GPU; p50/p99 job l
 # precision form -> library code (include/syngular_gb300.h SGT_PREC_*) and the arithmetic it computes in
 PRECISIONS = {"f64": 0, "tf32": 1, "tf32x3": 4, "bf16x6": 5}
 DTYPES = {"f64": "f64", "tf32": "tf32/f32", "tf32x3": "tf32x3/f32",
-          "bf16x6": "bf16x6 slices (tcgen05) / f32 pairs / f32 Jacobi + refinement"}
+          "bf16x6": "bf16x6 slices (tcgen05) / f32 pairs / purification (spectra: f32 Jacobi + refinement)"}
 
 
 def _eig_profile(enable):
