@@ -429,6 +429,13 @@ SGT_API int sgt_gemm_f64_sliced(int64_t M, int64_t N, int64_t K, double alpha, c
  * shared memory where it fits (0), or always blocked (1: 32-pivot panels on one
  * block, trailing updates on all SMs).  Same kept subspace either way. */
 #define SGT_TUNE_PCHOL_BLOCKED 2
+/* SGT_TUNE_PURIFY_CLEANUP (0 or 1, default 0): after a purification that did
+ * not reach a projector (a bond matrix with fewer directions above the
+ * products' noise than kept; its status is -1), run McWeeny steps
+ * X <- 3X^2 - 2X^3 and extra Newton-Schulz steps on the basis.  Off by default:
+ * the steps are enqueued for every bond and skipped on the device when not
+ * needed, which still costs about 3% of a sweep that never needs them. */
+#define SGT_TUNE_PURIFY_CLEANUP 3
 SGT_API int sgt_set_tuning(int key, int value);
 SGT_API int sgt_get_tuning(int key);
 

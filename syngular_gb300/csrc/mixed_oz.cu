@@ -1123,6 +1123,7 @@ __global__ void pchol_init_kernel(const float* __restrict__ A, int c, float* __r
 // (c x c): the cluster kernel where it fits, else (work: c*c + c floats of
 // scratch) the blocked form, else the one-block kernel.
 static int g_pchol_blocked = 0;  // SGT_TUNE_PCHOL_BLOCKED
+static int g_purify_cleanup = 0;  // SGT_TUNE_PURIFY_CLEANUP
 
 int pivoted_chol(cudaStream_t st, const float* A, int64_t c, int64_t keep, float* Lt, int* used, float* work) {
   const int64_t R = cdiv(c, (int64_t)PC_CS);
@@ -1567,11 +1568,14 @@ int oz_round_impl(cudaStream_t st, int n, const double* const* W, const int64_t*
         SGT_LAUNCHED();
       }
       // McWeeny clean-up of a projector the trace correction could not finish
-      // (every launch returns at once when ctl[1] says it did)
-      SGT_CUDA(cudaMemsetAsync(mcw_resid, 0, sizeof(unsigned) * MCW_ITERS, st));
-      for (int it = 0; it < MCW_ITERS; ++it) {
+      // (every launch returns at once when ctl[1] says it did; opt-in, since
+      // even skipped launches cost ~3% of a sweep that never needs them)
+      const bool cleanup = __atomic_load_n(&g_purify_cleanup, __ATOMIC_RELAXED) != 0;
+      SGT_CUDA(cudaMemsetAsync(mcw_resid, 0xff, sizeof(unsigned) * MCW_ITERS, st));  // NaN bits: no clean-up ran
+      for (int it = 0; cleanup && it < MCW_ITERS; ++it) {
         SGT_TRY(oz_gemm(st, c, c, c, 1.f, Vts.mat(), Vts.mat(), 0.f, X2.h, X2.l, c, part, part_floats, err,
                         ichoice + 1));                                            // X2 = X X
+        if (it == 0) SGT_CUDA(cudaMemsetAsync(mcw_resid, 0, sizeof(unsigned) * MCW_ITERS, st));
         SGT_TRY(oz_split_pair(st, X2.h, X2.l, c, c, c, Ts.s, Ts.e, 1, ichoice + 1));
         Ts.rows = c;
         Ts.cols = c;
@@ -1598,7 +1602,7 @@ int oz_round_impl(cudaStream_t st, int n, const double* const* W, const int64_t*
       // Newton-Schulz: Q <- 1.5 Q - 0.5 (Q Q^T) Q; after a purification that
       // needed the McWeeny clean-up the start is further from orthonormal, and
       // NS_EXTRA more steps run (skipped on the device otherwise)
-      for (int it = 0; it < NS_ITERS + NS_EXTRA; ++it) {
+      for (int it = 0; it < NS_ITERS + (cleanup ? NS_EXTRA : 0); ++it) {
         const int* sk = it < NS_ITERS ? nullptr : ichoice + 1;
         SGT_TRY(split_pair(st, Vk, c, Vks, keep, c, sk));
         SGT_TRY(oz_gemm(st, keep, keep, c, 1.f, Vks.mat(), Vks.mat(), 0.f, S.h, S.l, keep, part, part_floats, err, sk));
@@ -1869,9 +1873,10 @@ extern "C" SGT_API int sgt_gemm_f64_sliced(int64_t M, int64_t N, int64_t K, doub
 extern "C" SGT_API int sgt_set_tuning(int key, int value) {
   if (key == SGT_TUNE_SLICED_SPLIT_CTAS) return sgt::oz_set_split_ctas(value);
   if (key == SGT_TUNE_SLICED_SPLIT_MIN_KTILES) return sgt::oz_set_split_min_ktiles(value);
-  if (key == SGT_TUNE_PCHOL_BLOCKED) {
-    SGT_REQUIRE(value == 0 || value == 1, SGT_ERR_INVALID, "set_tuning: pivoted Cholesky choice %d not 0 or 1", value);
-    __atomic_store_n(&sgt::g_pchol_blocked, value, __ATOMIC_RELAXED);
+  if (key == SGT_TUNE_PCHOL_BLOCKED || key == SGT_TUNE_PURIFY_CLEANUP) {
+    SGT_REQUIRE(value == 0 || value == 1, SGT_ERR_INVALID, "set_tuning: key %d takes 0 or 1, not %d", key, value);
+    __atomic_store_n(key == SGT_TUNE_PCHOL_BLOCKED ? &sgt::g_pchol_blocked : &sgt::g_purify_cleanup, value,
+                     __ATOMIC_RELAXED);
     return SGT_OK;
   }
   sgt::set_error("set_tuning: unknown key %d", key);
@@ -1882,6 +1887,7 @@ extern "C" SGT_API int sgt_get_tuning(int key) {
   if (key == SGT_TUNE_SLICED_SPLIT_CTAS) return sgt::oz_split_ctas();
   if (key == SGT_TUNE_SLICED_SPLIT_MIN_KTILES) return sgt::oz_split_min_ktiles();
   if (key == SGT_TUNE_PCHOL_BLOCKED) return __atomic_load_n(&sgt::g_pchol_blocked, __ATOMIC_RELAXED);
+  if (key == SGT_TUNE_PURIFY_CLEANUP) return __atomic_load_n(&sgt::g_purify_cleanup, __ATOMIC_RELAXED);
   return -1;
 }
 

@@ -216,3 +216,31 @@ def test_overlap_on_sliced_gemm(n, d, chi, chi2):
         assert float(a | b) == xy
     finally:
         MatrixProductState.PRECISION = saved
+
+
+@pytest.mark.parametrize("cleanup", [0, 1])
+def test_bf16x6_round_rank_below_keep(cleanup):
+    """X + X rounded to 3/2 of X's bond: every bond matrix has rank chi below
+    the kept 3 chi / 2, so the purification meets a cluster of noise
+    eigenvalues.  The rounded state is still 2X; with the clean-up steps
+    (McWeeny, extra Newton-Schulz) the bonds also report convergence."""
+    from syngular_gb300 import _lib as L
+    from syngular_gb300.tensor import _ops
+
+    rng = np.random.default_rng(77)
+    n, d, chi = 10, 2, 16
+    X = O.random_mps_cores(rng, n, d, chi)
+    S = O.direct_sum(X, X)
+    L.call("sgt_set_tuning", L.TUNE_PURIFY_CLEANUP, cleanup)
+    try:
+        Z, spec, counts, disc, status = _ops.svd_round(dev(S), 3 * chi // 2, L.PREC_BF16X6, spectra=False)
+        torch.cuda.synchronize()
+    finally:
+        L.call("sgt_set_tuning", L.TUNE_PURIFY_CLEANUP, 0)
+    xx = O.overlap(X, X)
+    zz = _ops.overlap(Z, Z)
+    zx = _ops.overlap(Z, dev(X))
+    assert abs(zz - 4 * xx) <= 1e-8 * 4 * xx
+    assert abs(zx - 2 * xx) <= 1e-8 * 2 * xx
+    if cleanup:
+        assert int(status.item()) >= 0
