@@ -377,7 +377,9 @@ SGT_API int sgt_eig_method(int method);
  * reference would write around `(W @ X) >> chi` and `X | Z`; no single
  * reference function).  sgt_batched_plan_create sizes every instance's
  * workspace (max of the fused round and the overlap), deals the instances
- * longest-first onto `lanes` stream lanes and returns the workspace one launch
+ * onto `lanes` stream lanes, most estimated work first onto the least-loaded
+ * lane (work: per bond the squared product bond times d chi), and returns the
+ * workspace one launch
  * needs; it is host-only (no device calls).  sgt_batched_launch forks the
  * lanes off `stream` with events, runs each lane's instances in order inside
  * its own workspace region and joins the lanes back: no allocation, no host

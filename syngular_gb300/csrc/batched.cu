@@ -110,18 +110,29 @@ SGT_API int sgt_batched_plan_create(int count, const int* n, const int64_t* cons
     }
     in.ws = (std::max(wr, wo) + 255) & ~size_t(255);
   }
-  // longest first onto the least-loaded lane
+  // most work first onto the least-loaded lane (longest-processing-time
+  // order); an instance's work is the rounding's leading term, per bond the
+  // squared product bond times the bond matrix side (d chi)
+  std::vector<double> work(count, 0.0);
+  for (int i = 0; i < count; ++i) {
+    const auto& in = p->inst[i];
+    for (int k = 0; k < in.n; ++k) {
+      const double r = (double)(in.xshape[3 * k] * in.wshape[4 * k]);
+      const double r2 = (double)(in.xshape[3 * k + 2] * in.wshape[4 * k + 3]);
+      work[i] += r * r * (double)in.wshape[4 * k + 2] * std::min(r2, (double)in.chi);
+    }
+  }
   std::vector<int> order(count);
   for (int i = 0; i < count; ++i) order[i] = i;
-  std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return p->inst[a].ws > p->inst[b].ws; });
+  std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return work[a] > work[b]; });
   const int L = std::min(lanes, count);
-  std::vector<size_t> load(L, 0);
+  std::vector<double> load(L, 0.0);
   p->lanes.assign(L, {});
   for (int i : order) {
     const int l = (int)(std::min_element(load.begin(), load.end()) - load.begin());
     p->lanes[l].push_back(i);
     p->inst[i].lane = l;
-    load[l] += p->inst[i].ws;
+    load[l] += work[i];
   }
   p->lane_off.assign(L, 0);
   p->lane_bytes.assign(L, 0);

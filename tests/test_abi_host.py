@@ -110,7 +110,7 @@ def test_no_cpu_fallback_without_gpu():
 
 
 def test_batched_plan_host_only():
-    """sgt_batched_plan_create is host-only: workspace sizes, the longest-first
+    """sgt_batched_plan_create is host-only: workspace sizes, the most-work-first
     deal onto lanes and the rounded shapes, without a GPU."""
     import numpy as np
 
