@@ -242,6 +242,30 @@ SGT_API int sgt_mpo_mps_round(int n, const double* const* W, const int64_t* wsha
                               void* stream);
 
 /* ----------------------------------------------------------------------
+ * Zip-up MPO x MPS (Stoudenmire & White 2010): W X compressed to bond chi
+ * site by site from the left, never forming the product cores or their
+ * chi*D bonds.  A carry C (the compressed left part) moves right; at site k
+ * M[(r, o), (a', b')] = sum C[r, (a, b)] X_k[a, i, a'] W_k[b, i, o, b'] is
+ * split by a truncated FP64 SVD (Householder QR + one-sided Jacobi on the
+ * triangular factor): core k = the leading left singular vectors, the carry
+ * = S V^T.  Approximate unless chi covers every bond's rank; near the
+ * optimal truncation when X is right-orthonormal (the Python API
+ * right-orthonormalises a copy).  The reference lists unfinished modes for
+ * this (MATMUL_MODE "variational"/"fit-up", mpo:262-276); no reference
+ * result to match.  Shapes: out[k] = (r_k, out_k, r_{k+1}) from
+ * sgt_mpo_mps_zipup_shapes; `discarded` (device, n-1 doubles, may be NULL):
+ * sum of dropped s^2 / sum s^2 at each bond's SVD; `status` (device int, may
+ * be NULL): largest Jacobi sweep count, -1 at a sweep cap.
+ * -------------------------------------------------------------------- */
+SGT_API int sgt_mpo_mps_zipup_shapes(int n, const int64_t* wshape, const int64_t* xshape, int64_t chi,
+                                     int64_t* out_shape);
+SGT_API size_t sgt_mpo_mps_zipup_workspace_size(int n, const int64_t* wshape, const int64_t* xshape,
+                                                int64_t chi);
+SGT_API int sgt_mpo_mps_zipup(int n, const double* const* W, const int64_t* wshape, const double* const* X,
+                              const int64_t* xshape, int64_t chi, double* const* out, double* discarded,
+                              int* status, void* ws, size_t ws_bytes, void* stream);
+
+/* ----------------------------------------------------------------------
  * DMRG environment blocks (variational/dmrg.py:65-112, DMRG.__left_blocks /
  * DMRG.__right_blocks) and the two-site effective contraction
  * (variational/dmrg.py:143-165, the `site` tensor of each sweep step).

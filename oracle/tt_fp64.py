@@ -599,3 +599,36 @@ def env_two_site(Lb, merge: np.ndarray, W1: np.ndarray, W2: np.ndarray, Rb) -> n
     t = np.tensordot(t, W2, axes=([4, 1], [0, 1]))               # [a, c4, o1, o2, b3]
     t = np.tensordot(t, Rb, axes=([4, 1], [1, 2]))               # [a, o1, o2, a4]
     return t
+
+
+# ---------------------------------------------------------------------------
+# zip-up MPO x MPS (no reference code: the reference's "variational" and
+# "fit-up" MATMUL_MODE branches, tensor/matrix_product_operator.py:262-276, are
+# empty); Stoudenmire & White, New J. Phys. 12, 055026 (2010)
+# ---------------------------------------------------------------------------
+
+def zipup(W: Cores, X: Cores, chi: int):
+    """Zip-up of ``W @ X`` to bond ``chi``: a carry C[r, a, b] moves left to
+    right; at site k, M[(r, o), (a', b')] = sum C[r, a, b] X_k[a, i, a']
+    W_k[b, i, o, b'] is split by its SVD, the core takes the leading
+    min(chi, rank bound) left singular vectors and the carry S V^T; the last
+    core is M.  Returns (cores, discarded) with discarded[k] = dropped s^2 /
+    total s^2 at the cut after site k."""
+    n = len(X)
+    C = np.ones((1, 1, 1))
+    out, disc = [], []
+    for k in range(n):
+        T = np.tensordot(C, X[k], axes=([1], [0]))          # [r, b, i, a']
+        T = np.tensordot(T, W[k], axes=([1, 2], [0, 1]))    # [r, a', o, b']
+        r, a2, o, b2 = T.shape
+        M = T.transpose(0, 2, 1, 3).reshape(r * o, a2 * b2)
+        if k == n - 1:
+            out.append(M.reshape(r, o, 1))
+            break
+        U, s, Vt = np.linalg.svd(M, full_matrices=False)
+        q = min(chi, len(s))
+        tot = float(np.sum(s * s))
+        disc.append(float(np.sum(s[q:] ** 2) / tot) if tot > 0 else 0.0)
+        out.append(U[:, :q].reshape(r, o, q))
+        C = (s[:q, None] * Vt[:q]).reshape(q, a2, b2)
+    return out, disc

@@ -100,6 +100,9 @@ SIGNATURES = {
     "sgt_env_blocks": (_c_int, [_c_int, _PP, _PI64, _PP, _PI64, _PP, _PI64, _c_int, _c_int, _PP, _c_vp, _c_size, _c_vp]),
     "sgt_env_two_site_workspace_size": (_c_size, [_PI64, _PI64, _PI64, _PI64, _PI64]),
     "sgt_env_two_site": (_c_int, [_c_vp, _PI64, _c_vp, _PI64, _c_vp, _PI64, _c_vp, _PI64, _c_vp, _PI64, _c_vp, _c_vp, _c_size, _c_vp]),
+    "sgt_mpo_mps_zipup_shapes": (_c_int, [_c_int, _PI64, _PI64, _c_i64, _PI64]),
+    "sgt_mpo_mps_zipup_workspace_size": (_c_size, [_c_int, _PI64, _PI64, _c_i64]),
+    "sgt_mpo_mps_zipup": (_c_int, [_c_int, _PP, _PI64, _PP, _PI64, _c_i64, _PP, _c_vp, _c_vp, _c_vp, _c_size, _c_vp]),
     "sgt_mpo_mps_round_workspace_size":(_c_size, [_c_int, _PI64, _PI64, _c_i64, _c_int]),
     "sgt_mpo_mps_round": (_c_int, [_c_int, _PP, _PI64, _PP, _PI64, _c_i64, _c_int, _PP, _c_vp, _c_vp, _c_vp, _c_vp, _c_size, _c_vp]),
 }

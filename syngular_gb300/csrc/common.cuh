@@ -128,6 +128,10 @@ int qr_form_q(cudaStream_t st, const double* A, int64_t m, int64_t n, int64_t ld
 int qr_extract_r(cudaStream_t st, const double* A, int64_t m, int64_t n, int64_t lda, double* R,
                  int64_t ldr, int64_t rows);
 
+// dst (contiguous) = src (contiguous row-major, extents ext[0..rank-1]) with
+// its axes reordered: output axis j is source axis perm[j] (rank <= 6; env.cu).
+int permute_f64(cudaStream_t st, const double* src, double* dst, int rank, const int64_t* ext, const int* perm);
+
 // Transfer-sweep helpers (sweeps.cu): E /= 2^e with max|E| in [0.5, 1), the
 // exponent added to *expo; on the last site result = (E[0], *expo).
 int rescale_pow2(cudaStream_t st, double* E, int64_t n, double* expo, double* result, bool last);

@@ -28,9 +28,9 @@
 
 namespace sgt {
 
-namespace {
-
 constexpr int PERM_MAX = 6;
+
+namespace {
 
 struct PermArgs {
   int rank;
@@ -59,8 +59,11 @@ __global__ void permute_kernel(const double* __restrict__ src, double* __restric
   }
 }
 
+}  // namespace
+
 // dst = src with its axes reordered: output axis j is source axis perm[j].
 int permute_f64(cudaStream_t st, const double* src, double* dst, int rank, const int64_t* ext, const int* perm) {
+  SGT_REQUIRE(rank >= 1 && rank <= PERM_MAX, SGT_ERR_INVALID, "permute: rank %d outside [1, %d]", rank, PERM_MAX);
   PermArgs a{};
   a.rank = rank;
   int64_t stride[PERM_MAX];
@@ -80,6 +83,8 @@ int permute_f64(cudaStream_t st, const double* src, double* dst, int rank, const
   SGT_LAUNCHED();
   return SGT_OK;
 }
+
+namespace {
 
 __global__ void unit_kernel(double* p) { *p = 1.0; }
 

@@ -412,6 +412,37 @@ def eig_method(method: int = 0) -> int:
     return int(L.load().sgt_eig_method(int(method)))
 
 
+def mpo_mps_zipup(W: Cores, X: Cores, chi: int):
+    """Zip-up of ``W @ X`` to bond ``chi`` (FP64; the library's
+    sgt_mpo_mps_zipup).  Returns ``(cores, discarded, status)`` as device
+    tensors; the caller chooses the gauge of X (right-orthonormal X gives the
+    near-optimal truncation)."""
+    _check(W)
+    _check(X)
+    n = len(X)
+    if len(W) != n:
+        raise ValueError("operator and state have different lengths")
+    wsh, _w = L.i64_array([int(v) for w in W for v in w.shape])
+    xsh, _x = L.shape_array([shape3(x) for x in X])
+    out_arr = (ctypes.c_int64 * (3 * n))()
+    L.call("sgt_mpo_mps_zipup_shapes", n, wsh, xsh, chi, ctypes.cast(out_arr, L._PI64))
+    outs = [empty((out_arr[3 * k], out_arr[3 * k + 1], out_arr[3 * k + 2])) for k in range(n)]
+    need = L.query("sgt_mpo_mps_zipup_workspace_size", n, wsh, xsh, chi)
+    if need == 0:
+        raise L.SyngularError("sgt_mpo_mps_zipup_workspace_size", L.SGT_ERR_INVALID,
+                              L.load().sgt_last_error().decode(errors="replace"))
+    ws = L.workspace(need)
+    dev = L.device()
+    disc = torch.zeros(max(1, n - 1), dtype=torch.float64, device=dev)
+    status = torch.zeros(1, dtype=torch.int32, device=dev)
+    wp, _wp = L.ptr_array(W)
+    xp, _xp = L.ptr_array(X)
+    op, _op = L.ptr_array(outs)
+    L.call("sgt_mpo_mps_zipup", n, wp, wsh, xp, xsh, chi, op, L.ptr(disc), L.ptr(status), L.ptr(ws), ws.numel(),
+           L.stream_ptr())
+    return outs, disc, status
+
+
 def mpo_mps_round(W: Cores, X: Cores, chi: int, precision: int = L.PREC_F64, spectra: bool = True):
     """Raw ``W @ X`` followed by TT-SVD rounding to ``chi`` in one library call.
     Returns ``(cores, spectra, counts, discarded, status)`` (device tensors);

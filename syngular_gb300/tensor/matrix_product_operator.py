@@ -14,8 +14,10 @@ Deliberate deviations, on inputs where the reference misbehaves:
     the first operand's, which only works when the two agree);
   * ``decompose`` prints nothing (mpo:442).
 ``MATMUL_MODE`` "opti" (the reference's unfinished density-matrix compression,
-mpo:193-273) is the fused product + TT-SVD round to the min bond; "variational"
-and "fit-up" are empty in the reference and return None here as there.
+mpo:193-273) is the fused product + TT-SVD round to the min bond; "zip-up" (not
+a reference mode) is the zip-up compression of Stoudenmire & White 2010;
+"variational" and "fit-up" are empty in the reference and return None here as
+there.
 """
 from __future__ import annotations
 
@@ -117,6 +119,16 @@ class MatrixProductOperator:
                     return s
                 out, _sp, _c, _d, _st = _ops.mpo_mps_round(self.sites, mp.sites, min_bond,
                                                            precision_code(type(self).PRECISION), spectra=False)
+                return MatrixProductState.from_sites(out)
+            if MatrixProductOperator.MATMUL_MODE == "zip-up":
+                # Zip-up (Stoudenmire & White 2010) to min_bond: the state is
+                # first brought to right-orthonormal form (an exact FP64
+                # TT-SVD at its own bonds), then W X is compressed site by
+                # site from the left without forming the product
+                xs = [L.as_device(x) for x in mp.sites]
+                big = max(int(x.shape[0]) for x in xs) * max(int(x.shape[1]) for x in xs) + 1
+                xr, _sp, _c, _d, _st = _ops.svd_round(xs, big, L.PREC_F64, spectra=False)
+                out, _disc, _st2 = _ops.mpo_mps_zipup([L.as_device(w) for w in self.sites], xr, min_bond)
                 return MatrixProductState.from_sites(out)
             return None
         if isinstance(mp, MatrixProductOperator):

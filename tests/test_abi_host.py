@@ -235,3 +235,14 @@ def test_env_blocks_size_queries_host_only(lib):
     assert lib.sgt_env_two_site_workspace_size(ls, m, w1, w2, rs) > 0
     assert lib.sgt_env_two_site_workspace_size(None, m, w1, w2, rs) > 0
     assert lib.sgt_env_two_site_workspace_size(ls, m, w1, w2, None) == 0   # right block needed (b3 = 4)
+
+
+def test_library_resolves_every_symbol_at_load(lib):
+    """Every symbol the library uses is defined (bound at load time, not at
+    the first call): a declared-but-missing helper would otherwise surface only
+    when its entry point runs on a GPU host."""
+    import ctypes
+
+    from syngular_gb300 import _lib
+
+    ctypes.CDLL(_lib.LIB_PATH, mode=os.RTLD_NOW | os.RTLD_LOCAL)
