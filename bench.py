@@ -108,10 +108,13 @@ def _apply_split(args, L):
         L.call("sgt_set_tuning", L.TUNE_SLICED_SPLIT_MIN_KTILES, kt)
     if args.pchol:
         L.call("sgt_set_tuning", L.TUNE_PCHOL_BLOCKED, {"cluster": 0, "blocked": 1}[args.pchol])
+    if args.purify_step:
+        L.call("sgt_set_tuning", L.TUNE_PURIFY_VECTOR_STEP, {"warp": 0, "block": 1}[args.purify_step])
     lib = L.load()
     return {"split_ctas": int(lib.sgt_get_tuning(L.TUNE_SLICED_SPLIT_CTAS)),
             "split_min_ktiles": int(lib.sgt_get_tuning(L.TUNE_SLICED_SPLIT_MIN_KTILES)),
-            "pivoted_cholesky": "blocked" if lib.sgt_get_tuning(L.TUNE_PCHOL_BLOCKED) else "cluster"}
+            "pivoted_cholesky": "blocked" if lib.sgt_get_tuning(L.TUNE_PCHOL_BLOCKED) else "cluster",
+            "purify_step": "block" if lib.sgt_get_tuning(L.TUNE_PURIFY_VECTOR_STEP) else "warp"}
 
 
 def _pct(values, p):
@@ -1099,6 +1102,9 @@ def main():
                     help="CTAS,KTILES: the sliced GEMM's split-K shape (default: the library's 148,8)")
     ap.add_argument("--pchol", default="", choices=["", "cluster", "blocked"],
                     help="the BF16X6 form's pivoted Cholesky (default: the library's, cluster where it fits)")
+    ap.add_argument("--purify-step", default="", choices=["", "warp", "block"],
+                    help="the BF16X6 purification step: a warp per row or a block per row with 16-byte "
+                         "accesses (default: the library's, block where the bond allows)")
     ap.add_argument("--graph-per-lane", type=int, default=4,
                     help="--workload batched: instances per lane in each captured graph (0 = one graph)")
     ap.add_argument("--hbm-kernels", default="contract,concat,overlap,qr",

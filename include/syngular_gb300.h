@@ -462,6 +462,12 @@ SGT_API int sgt_gemm_f64_sliced(int64_t M, int64_t N, int64_t K, double alpha, c
  * the steps are enqueued for every bond and skipped on the device when not
  * needed, which still costs about 3% of a sweep that never needs them. */
 #define SGT_TUNE_PURIFY_CLEANUP 3
+/* SGT_TUNE_PURIFY_VECTOR_STEP (0 or 1, default 1): each purification step
+ * after the product X2 = X X updates X, finds its residual and writes X's
+ * slices with one 128-thread block per row and 16-byte accesses where the bond
+ * dimension is a multiple of 4 (1), or with one warp per row (0).  The same
+ * arithmetic element by element: identical results. */
+#define SGT_TUNE_PURIFY_VECTOR_STEP 4
 SGT_API int sgt_set_tuning(int key, int value);
 SGT_API int sgt_get_tuning(int key);
 

@@ -35,6 +35,7 @@ TUNE_SLICED_SPLIT_CTAS = 0
 TUNE_SLICED_SPLIT_MIN_KTILES = 1
 TUNE_PCHOL_BLOCKED = 2
 TUNE_PURIFY_CLEANUP = 3
+TUNE_PURIFY_VECTOR_STEP = 4
 
 _c_i64 = ctypes.c_int64
 _c_vp = ctypes.c_void_p

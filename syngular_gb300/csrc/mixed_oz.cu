@@ -760,6 +760,146 @@ __global__ void __launch_bounds__(256) tc2_step_kernel(float* __restrict__ xh, f
   }
 }
 
+// tc2_x2 for 4 consecutive elements (i a multiple of 4, mn too): the same sums
+// in the same order, with 16-byte loads.
+__device__ __forceinline__ void tc2_x2_4(const float* __restrict__ x2h, const float* __restrict__ x2l, int S,
+                                        int64_t mn, int64_t i, float4& h, float4& l) {
+  h = *reinterpret_cast<const float4*>(x2h + i);
+  l = *reinterpret_cast<const float4*>(x2l + i);
+  if (S > 1) {
+    float hv[4] = {h.x, h.y, h.z, h.w}, lv[4] = {l.x, l.y, l.z, l.w};
+    for (int z = 1; z < S; ++z) {
+      const float4 v4 = *reinterpret_cast<const float4*>(x2h + (int64_t)z * mn + i);
+      const float4 w4 = *reinterpret_cast<const float4*>(x2l + (int64_t)z * mn + i);
+      const float vv[4] = {v4.x, v4.y, v4.z, v4.w}, ww[4] = {w4.x, w4.y, w4.z, w4.w};
+#pragma unroll
+      for (int j = 0; j < 4; ++j) {
+        const float sum = hv[j] + vv[j];
+        const float bb = sum - hv[j];
+        const float e = (hv[j] - (sum - bb)) + (vv[j] - bb);
+        hv[j] = sum;
+        lv[j] += e;
+        lv[j] += ww[j];
+      }
+    }
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+      const float t = hv[j] + lv[j];
+      lv[j] = lv[j] - (t - hv[j]);
+      hv[j] = t;
+    }
+    h = make_float4(hv[0], hv[1], hv[2], hv[3]);
+    l = make_float4(lv[0], lv[1], lv[2], lv[3]);
+  }
+}
+
+// tc2_step_kernel with a block of TC2_VEC_THREADS per row and 4 consecutive
+// elements per thread (n a multiple of 4, 16-byte aligned buffers): the same
+// per-element arithmetic, the row maximum reduced over the block, the slices
+// written 8 bytes at a time.  n blocks keep every SM busy where the
+// warp-per-row form fills n / 8 blocks.
+constexpr int TC2_VEC_THREADS = 128;
+__global__ void __launch_bounds__(TC2_VEC_THREADS) tc2_step4_kernel(
+    float* __restrict__ xh, float* __restrict__ xl, const float* __restrict__ x2h, const float* __restrict__ x2l,
+    int S, int n, int keep, const float* __restrict__ dcur, float* __restrict__ dnext, int* __restrict__ ctl,
+    unsigned* __restrict__ resid, unsigned* __restrict__ ticket, __nv_bfloat16* __restrict__ out, int64_t ldo,
+    int64_t sstride, int* __restrict__ ex) {
+  constexpr int W = TC2_VEC_THREADS / 32;
+  __shared__ double red[2][W];
+  __shared__ float s_mx[W];
+  __shared__ int s_ch;
+  __shared__ bool s_last;
+  if (ctl[1]) return;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int64_t mn = (int64_t)n * n;
+  {
+    double a = 0.0, b = 0.0;
+    for (int i = threadIdx.x; i < n; i += TC2_VEC_THREADS) {
+      float h2, l2;
+      tc2_x2(x2h, x2l, S, mn, (int64_t)i * n + i, h2, l2);
+      a += (double)dcur[i] + (double)dcur[n + i];
+      b += (double)h2 + (double)l2;
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+      a += __shfl_xor_sync(0xffffffffu, a, o);
+      b += __shfl_xor_sync(0xffffffffu, b, o);
+    }
+    if (lane == 0) red[0][warp] = a, red[1][warp] = b;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      double ta = 0.0, tb = 0.0;
+      for (int w = 0; w < W; ++w) ta += red[0][w], tb += red[1][w];
+      s_ch = fabs(tb - keep) < fabs(2.0 * ta - tb - keep) ? 1 : 0;
+    }
+    __syncthreads();
+  }
+  const int ch = s_ch;
+  float worst = 0.f;
+  for (int64_t r = blockIdx.x; r < n; r += gridDim.x) {
+    float mx = 0.f;
+    for (int64_t c = 4 * threadIdx.x; c < n; c += 4 * TC2_VEC_THREADS) {
+      const int64_t i = r * n + c;
+      float4 h24, l24;
+      tc2_x2_4(x2h, x2l, S, mn, i, h24, l24);
+      const float4 h4 = *reinterpret_cast<const float4*>(xh + i);
+      const float4 l4 = *reinterpret_cast<const float4*>(xl + i);
+      const float h2v[4] = {h24.x, h24.y, h24.z, h24.w}, l2v[4] = {l24.x, l24.y, l24.z, l24.w};
+      float hv[4] = {h4.x, h4.y, h4.z, h4.w}, lv[4] = {l4.x, l4.y, l4.z, l4.w};
+#pragma unroll
+      for (int j = 0; j < 4; ++j) {
+        worst = fmaxf(worst, fabsf((h2v[j] - hv[j]) + (l2v[j] - lv[j])));
+        if (ch) {
+          hv[j] = h2v[j];
+          lv[j] = l2v[j];
+        } else {  // 2X - X^2
+          hv[j] *= 2.f;
+          lv[j] *= 2.f;
+          df_add(hv[j], lv[j], -h2v[j], -l2v[j]);
+        }
+        mx = fmaxf(mx, fabsf(hv[j]));
+        if (c + j == r) dnext[r] = hv[j], dnext[n + r] = lv[j];
+      }
+      *reinterpret_cast<float4*>(xh + i) = make_float4(hv[0], hv[1], hv[2], hv[3]);
+      *reinterpret_cast<float4*>(xl + i) = make_float4(lv[0], lv[1], lv[2], lv[3]);
+    }
+    for (int o = 16; o > 0; o >>= 1) mx = fmaxf(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+    if (lane == 0) s_mx[warp] = mx;
+    __syncthreads();
+    mx = s_mx[0];
+    for (int w = 1; w < W; ++w) mx = fmaxf(mx, s_mx[w]);
+    __syncthreads();  // s_mx is rewritten by the next row
+    int e = 0;
+    if (mx > 0.f && isfinite(mx)) frexpf(mx, &e);
+    if (threadIdx.x == 0) ex[r] = e;
+    // each thread re-reads only the elements it wrote above
+    for (int64_t c = 4 * threadIdx.x; c < n; c += 4 * TC2_VEC_THREADS) {
+      const int64_t i = r * n + c;
+      slice_store4(*reinterpret_cast<const float4*>(xh + i), *reinterpret_cast<const float4*>(xl + i), 6 - e, out,
+                   sstride, r * ldo + c);
+    }
+    for (int64_t c = n + 4 * threadIdx.x; c < ldo; c += 4 * TC2_VEC_THREADS) {
+      const __nv_bfloat16 z4[4] = {__float2bfloat16_rn(0.f), __float2bfloat16_rn(0.f), __float2bfloat16_rn(0.f),
+                                   __float2bfloat16_rn(0.f)};
+#pragma unroll
+      for (int s = 0; s < OZ_SLICES; ++s)
+        *reinterpret_cast<uint2*>(out + (int64_t)s * sstride + r * ldo + c) = *reinterpret_cast<const uint2*>(z4);
+    }
+  }
+  for (int o = 16; o > 0; o >>= 1) worst = fmaxf(worst, __shfl_xor_sync(0xffffffffu, worst, o));
+  if (lane == 0 && worst > 0.f) atomicMax(resid, __float_as_uint(worst));
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    __threadfence();
+    s_last = atomicAdd(ticket, 1u) == gridDim.x - 1;
+  }
+  __syncthreads();
+  if (s_last && threadIdx.x == 0) {
+    __threadfence();
+    if (__uint_as_float(atomicAdd(resid, 0u)) <= ldexpf(1.f, -34)) ctl[1] = 1;
+    *ticket = 0u;
+  }
+}
+
 // identity pair matrix (rows x cols, ld = cols)
 __global__ void pair_eye_kernel(float* __restrict__ h, float* __restrict__ l, int64_t rows, int64_t cols) {
   for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < rows * cols;
@@ -1124,6 +1264,7 @@ __global__ void pchol_init_kernel(const float* __restrict__ A, int c, float* __r
 // scratch) the blocked form, else the one-block kernel.
 static int g_pchol_blocked = 0;  // SGT_TUNE_PCHOL_BLOCKED
 static int g_purify_cleanup = 0;  // SGT_TUNE_PURIFY_CLEANUP
+static int g_tc2_vec = 1;         // SGT_TUNE_PURIFY_VECTOR_STEP
 
 int pivoted_chol(cudaStream_t st, const float* A, int64_t c, int64_t keep, float* Lt, int* used, float* work) {
   const int64_t R = cdiv(c, (int64_t)PC_CS);
@@ -1555,6 +1696,10 @@ int oz_round_impl(cudaStream_t st, int n, const double* const* W, const int64_t*
       Vts.rows = c;
       Vts.cols = c;
       const unsigned sg = (unsigned)std::min<int64_t>(cdiv(c, 8), 152 * 4);
+      const unsigned sg4 = (unsigned)std::min<int64_t>(c, 152 * 16);
+      auto a16 = [](const void* p) { return (reinterpret_cast<uintptr_t>(p) & 15) == 0; };
+      const bool vec4 = c % 4 == 0 && a16(X.h) && a16(X.l) && a16(T.h) && a16(T.l) && a16(part) &&
+                        a16(Vts.s) && __atomic_load_n(&g_tc2_vec, __ATOMIC_RELAXED) != 0;
       for (int it = 0; it < TC2_ITERS; ++it) {
         // X2 = X X; a split-K product leaves its partials, which the step adds
         int S = 1;
@@ -1562,9 +1707,14 @@ int oz_round_impl(cudaStream_t st, int n, const double* const* W, const int64_t*
                         ichoice + 1, &S));
         const float* x2h = S > 1 ? part : X2.h;
         const float* x2l = S > 1 ? part + (int64_t)S * c * c : X2.l;
-        tc2_step_kernel<<<sg, 256, 0, st>>>(X.h, X.l, x2h, x2l, S, (int)c, (int)keep, tc2_diag + (it & 1) * 2 * c,
-                                             tc2_diag + ((it + 1) & 1) * 2 * c, ichoice, tc2_resid + it, ticket,
-                                             Vts.s, oz_ld(c), c * oz_ld(c), Vts.e);
+        if (vec4)
+          tc2_step4_kernel<<<sg4, TC2_VEC_THREADS, 0, st>>>(
+              X.h, X.l, x2h, x2l, S, (int)c, (int)keep, tc2_diag + (it & 1) * 2 * c,
+              tc2_diag + ((it + 1) & 1) * 2 * c, ichoice, tc2_resid + it, ticket, Vts.s, oz_ld(c), c * oz_ld(c), Vts.e);
+        else
+          tc2_step_kernel<<<sg, 256, 0, st>>>(X.h, X.l, x2h, x2l, S, (int)c, (int)keep, tc2_diag + (it & 1) * 2 * c,
+                                               tc2_diag + ((it + 1) & 1) * 2 * c, ichoice, tc2_resid + it, ticket,
+                                               Vts.s, oz_ld(c), c * oz_ld(c), Vts.e);
         SGT_LAUNCHED();
       }
       // McWeeny clean-up of a projector the trace correction could not finish
@@ -1873,10 +2023,12 @@ extern "C" SGT_API int sgt_gemm_f64_sliced(int64_t M, int64_t N, int64_t K, doub
 extern "C" SGT_API int sgt_set_tuning(int key, int value) {
   if (key == SGT_TUNE_SLICED_SPLIT_CTAS) return sgt::oz_set_split_ctas(value);
   if (key == SGT_TUNE_SLICED_SPLIT_MIN_KTILES) return sgt::oz_set_split_min_ktiles(value);
-  if (key == SGT_TUNE_PCHOL_BLOCKED || key == SGT_TUNE_PURIFY_CLEANUP) {
+  if (key == SGT_TUNE_PCHOL_BLOCKED || key == SGT_TUNE_PURIFY_CLEANUP || key == SGT_TUNE_PURIFY_VECTOR_STEP) {
     SGT_REQUIRE(value == 0 || value == 1, SGT_ERR_INVALID, "set_tuning: key %d takes 0 or 1, not %d", key, value);
-    __atomic_store_n(key == SGT_TUNE_PCHOL_BLOCKED ? &sgt::g_pchol_blocked : &sgt::g_purify_cleanup, value,
-                     __ATOMIC_RELAXED);
+    int* slot = key == SGT_TUNE_PCHOL_BLOCKED   ? &sgt::g_pchol_blocked
+                : key == SGT_TUNE_PURIFY_CLEANUP ? &sgt::g_purify_cleanup
+                                                 : &sgt::g_tc2_vec;
+    __atomic_store_n(slot, value, __ATOMIC_RELAXED);
     return SGT_OK;
   }
   sgt::set_error("set_tuning: unknown key %d", key);
@@ -1888,6 +2040,7 @@ extern "C" SGT_API int sgt_get_tuning(int key) {
   if (key == SGT_TUNE_SLICED_SPLIT_MIN_KTILES) return sgt::oz_split_min_ktiles();
   if (key == SGT_TUNE_PCHOL_BLOCKED) return __atomic_load_n(&sgt::g_pchol_blocked, __ATOMIC_RELAXED);
   if (key == SGT_TUNE_PURIFY_CLEANUP) return __atomic_load_n(&sgt::g_purify_cleanup, __ATOMIC_RELAXED);
+  if (key == SGT_TUNE_PURIFY_VECTOR_STEP) return __atomic_load_n(&sgt::g_tc2_vec, __ATOMIC_RELAXED);
   return -1;
 }
 

@@ -85,6 +85,39 @@ __device__ __forceinline__ void slice_store(float h, float l, __nv_bfloat16* out
 }
 
 
+// slice_store for 4 consecutive values (hi h, lo l, scaled by 2^sh first):
+// one 8-byte store per slice; idx a multiple of 4 (8-byte aligned).
+__device__ __forceinline__ void slice_store4(float4 h, float4 l, int sh, __nv_bfloat16* out, int64_t sstride,
+                                             int64_t idx) {
+  const float hv[4] = {h.x, h.y, h.z, h.w}, lv[4] = {l.x, l.y, l.z, l.w};
+  float rh[4], rl[4];
+  __nv_bfloat16 q[4];
+#pragma unroll
+  for (int j = 0; j < 4; ++j) {
+    const float hh = ldexpf(hv[j], sh), ll = ldexpf(lv[j], sh);
+    const float m = rintf(hh);
+    rh[j] = hh - m;  // exact
+    rl[j] = ll;
+    q[j] = __float2bfloat16_rn(m);
+  }
+  *reinterpret_cast<uint2*>(out + idx) = *reinterpret_cast<const uint2*>(q);
+#pragma unroll
+  for (int s = 1; s < OZ_SLICES; ++s) {
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+      const float t = rh[j] + rl[j];
+      const float bb = t - rh[j];
+      rl[j] = (rh[j] - (t - bb)) + (rl[j] - bb);
+      rh[j] = t * 128.f;
+      rl[j] *= 128.f;
+      const float m = rintf(rh[j] + rl[j]);
+      rh[j] = rh[j] - m;
+      q[j] = __float2bfloat16_rn(ldexpf(m, -7 * s));
+    }
+    *reinterpret_cast<uint2*>(out + (int64_t)s * sstride + idx) = *reinterpret_cast<const uint2*>(q);
+  }
+}
+
 __device__ __forceinline__ void slice_zero(__nv_bfloat16* out, int64_t sstride, int64_t idx) {
 #pragma unroll
   for (int s = 0; s < OZ_SLICES; ++s) out[(int64_t)s * sstride + idx] = __float2bfloat16_rn(0.f);

@@ -458,38 +458,7 @@ __global__ void oz_split_pair_kernel(const int* __restrict__ skip, const float* 
 
 // Vector form of the kernel above (cols, ld multiples of 4 and 16-byte aligned
 // rows): each lane reads 4 consecutive hi / lo values with one 16-byte load
-// and writes each slice's 4 values with one 8-byte store.
-__device__ __forceinline__ void slice_store4(float4 h, float4 l, int sh, __nv_bfloat16* out, int64_t sstride,
-                                             int64_t idx) {
-  const float hv[4] = {h.x, h.y, h.z, h.w}, lv[4] = {l.x, l.y, l.z, l.w};
-  float rh[4], rl[4];
-  __nv_bfloat16 q[4];
-#pragma unroll
-  for (int j = 0; j < 4; ++j) {
-    const float hh = ldexpf(hv[j], sh), ll = ldexpf(lv[j], sh);
-    const float m = rintf(hh);
-    rh[j] = hh - m;  // exact
-    rl[j] = ll;
-    q[j] = __float2bfloat16_rn(m);
-  }
-  *reinterpret_cast<uint2*>(out + idx) = *reinterpret_cast<const uint2*>(q);
-#pragma unroll
-  for (int s = 1; s < OZ_SLICES; ++s) {
-#pragma unroll
-    for (int j = 0; j < 4; ++j) {
-      const float t = rh[j] + rl[j];
-      const float bb = t - rh[j];
-      rl[j] = (rh[j] - (t - bb)) + (rl[j] - bb);
-      rh[j] = t * 128.f;
-      rl[j] *= 128.f;
-      const float m = rintf(rh[j] + rl[j]);
-      rh[j] = rh[j] - m;
-      q[j] = __float2bfloat16_rn(ldexpf(m, -7 * s));
-    }
-    *reinterpret_cast<uint2*>(out + (int64_t)s * sstride + idx) = *reinterpret_cast<const uint2*>(q);
-  }
-}
-
+// and writes each slice's 4 values with one 8-byte store (slice_store4).
 __global__ void oz_split_pair4_kernel(const int* __restrict__ skip, const float* __restrict__ hi,
                                       const float* __restrict__ lo, int64_t ld, int64_t rows, int64_t cols,
                                       __nv_bfloat16* __restrict__ out, int64_t ldo, int64_t sstride,

@@ -192,6 +192,11 @@ def test_sliced_split_tuning_host_only(lib):
         assert lib.sgt_set_tuning(L.TUNE_PURIFY_CLEANUP, 1) == L.SGT_OK
         assert lib.sgt_get_tuning(L.TUNE_PURIFY_CLEANUP) == 1
         assert lib.sgt_set_tuning(L.TUNE_PURIFY_CLEANUP, 0) == L.SGT_OK
+        assert lib.sgt_get_tuning(L.TUNE_PURIFY_VECTOR_STEP) == 1
+        assert lib.sgt_set_tuning(L.TUNE_PURIFY_VECTOR_STEP, 2) == L.SGT_ERR_INVALID
+        assert lib.sgt_set_tuning(L.TUNE_PURIFY_VECTOR_STEP, 0) == L.SGT_OK
+        assert lib.sgt_get_tuning(L.TUNE_PURIFY_VECTOR_STEP) == 0
+        assert lib.sgt_set_tuning(L.TUNE_PURIFY_VECTOR_STEP, 1) == L.SGT_OK
         assert lib.sgt_set_tuning(L.TUNE_SLICED_SPLIT_MIN_KTILES, 1) == L.SGT_ERR_INVALID
         sizes = []
         for t, kt in ((24, 8), (148, 8), (592, 8), (592, 2)):

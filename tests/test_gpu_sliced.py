@@ -188,6 +188,32 @@ def test_bf16x6_round_without_spectra(n, d, chi, D, cut, blocked):
             np.testing.assert_allclose(m @ m.T, np.eye(m.shape[0]), rtol=0, atol=1e-10)
 
 
+@pytest.mark.parametrize("n,d,chi,D,cut", [(12, 2, 64, 8, 64), (7, 3, 16, 8, 30), (10, 2, 30, 3, 24)])
+def test_purify_step_forms_agree(n, d, chi, D, cut):
+    """The purification step with a block per row and 16-byte accesses (bond
+    dimensions that are multiples of 4) and with a warp per row give the same
+    rounded cores, discarded weights and status bit for bit."""
+    from syngular_gb300 import _lib as L
+    from syngular_gb300.tensor import _ops
+
+    rng = np.random.default_rng(7 * n + chi)
+    W, X = dev(O.random_mpo_cores(rng, n, d, D)), dev(O.random_mps_cores(rng, n, d, chi))
+    out = []
+    for vec in (1, 0):
+        L.call("sgt_set_tuning", L.TUNE_PURIFY_VECTOR_STEP, vec)
+        try:
+            Z, _, _, disc, status = _ops.mpo_mps_round(W, X, cut, L.PREC_BF16X6, spectra=False)
+            torch.cuda.synchronize()
+        finally:
+            L.call("sgt_set_tuning", L.TUNE_PURIFY_VECTOR_STEP, 1)
+        out.append((Z, disc, int(status.item())))
+    (Za, da, sa), (Zb, db, sb) = out
+    assert sa == sb and sa >= 0
+    assert torch.equal(da, db)
+    for a, b in zip(Za, Zb):
+        assert torch.equal(a, b)
+
+
 @pytest.mark.parametrize("n,d,chi,chi2", [(12, 2, 16, 9), (64, 2, 256, 256), (5, 3, 7, 11)])
 def test_overlap_on_sliced_gemm(n, d, chi, chi2):
     """The transfer sweep with its contractions on the sliced GEMM against the
