@@ -207,6 +207,23 @@ class RoundServer:
             self._capture(job, key)
         return out, ev, gr
 
+    def _evict_idle_graphs(self, need: int) -> bool:
+        """Graph memory is held for good, so a job that fits the budget could
+        wait forever behind it: when the graphs alone leave too little room
+        for ``need`` bytes, free idle graphs, oldest first, until they do not
+        (a job that only waits for in-flight work evicts nothing).  An evicted
+        key is not captured again.  Returns whether the job fits now."""
+        for key in list(self.graphs):
+            if self.graph_bytes + need <= self.budget:
+                break
+            gr = self.graphs[key]
+            if gr is None or gr.busy:
+                continue
+            self.graphs[key] = None
+            self.graph_bytes -= gr.nbytes
+            self.used -= gr.nbytes
+        return self.used + need <= self.budget
+
     def _loop(self):
         while not self._stop.is_set() or self.pending or self.inflight or not self.inbox.empty():
             # take arrivals
@@ -262,7 +279,7 @@ class RoundServer:
             for j in self.pending[: self.scan]:
                 if not self.free_streams:
                     break
-                if self.used + j._need > self.budget:
+                if self.used + j._need > self.budget and not self._evict_idle_graphs(j._need):
                     if getattr(j, "_blocked", None) is None:
                         j._blocked = now
                     if now - j._blocked < self.max_bypass_s:
