@@ -360,20 +360,22 @@ def autotune(instances: List[Instance], precision: int = L.PREC_TF32X3,
             best = (s, ms)
     lanes = best[0] if best else candidates[0]
     chosen = base
-    for sp in splits:
-        sp = (int(sp[0]), int(sp[1]))
-        if sp == base and best is not None:
-            continue
-        apply(sp)
-        try:
-            ms = _time_config(instances, precision, lanes, budget_bytes, reps, spectra, per_lane)
-        except MemoryError:
-            continue
-        trials["lanes=%d,split=%dx%d" % (lanes, sp[0], sp[1])] = ms
-        if best is None or ms < best[1]:
-            best = (lanes, ms)
-            chosen = sp
-    apply(chosen)
+    try:
+        for sp in splits:
+            sp = (int(sp[0]), int(sp[1]))
+            if sp == base and best is not None:
+                continue
+            apply(sp)
+            try:
+                ms = _time_config(instances, precision, lanes, budget_bytes, reps, spectra, per_lane)
+            except MemoryError:
+                continue
+            trials["lanes=%d,split=%dx%d" % (lanes, sp[0], sp[1])] = ms
+            if best is None or ms < best[1]:
+                best = (lanes, ms)
+                chosen = sp
+    finally:  # a failed trial leaves the library at the best shape so far, not at the trial's
+        apply(chosen)
     res = {"streams": lanes, "split": list(chosen), "ms": best[1] if best else None, "trials": trials}
     cache[key] = res
     try:
