@@ -12,7 +12,13 @@ reference does so (its ``left_matricization`` reshapes to ``(l*in*out, r)``,
 Every function names the reference lines it restates.  The TT-SVD rounding
 (``tt_svd_round``) has no counterpart in the reference (it only has a QR column
 truncation); it follows Oseledets, "Tensor-Train Decomposition", SIAM J. Sci.
-Comput. 33(5), 2011, Algorithm 2.
+Comput. 33(5), 2011, Algorithm 2.  Neither has the zip-up (``zipup``;
+Stoudenmire & White 2010).  Pinning: the functions with reference counterparts
+are checked against fixtures made by running the reference itself
+(tests/golden/make_golden.py, tests/test_oracle_golden.py); ``tt_svd_round``
+and ``zipup`` are parity unpinned, checked by identities only
+(tests/test_oracle_golden.py::test_tt_svd_round_identities,
+tests/test_oracle_props.py).
 """
 from __future__ import annotations
 
