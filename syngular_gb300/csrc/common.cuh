@@ -138,7 +138,6 @@ int rescale_pow2(cudaStream_t st, double* E, int64_t n, double* expo, double* re
 int zero_scalar(cudaStream_t st, double* p);
 
 // One-sided Jacobi SVD (see sgt_jacobi_svd).
-size_t jacobi_ws_bytes(int64_t m, int64_t n);
 int jacobi_svd(cudaStream_t st, double* A, int64_t m, int64_t n, double* V, double* s, int* status,
                Arena& ar);
 
