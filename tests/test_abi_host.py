@@ -242,6 +242,33 @@ def test_env_blocks_size_queries_host_only(lib):
     assert lib.sgt_env_two_site_workspace_size(ls, m, w1, w2, None) == 0   # right block needed (b3 = 4)
 
 
+@pytest.mark.parametrize("n,d,chi,D,cut", [(6, 2, 4, 3, 5), (5, 3, 2, 2, 64), (7, 2, 8, 4, 12)])
+def test_zipup_shapes_match_oracle_host_only(lib, n, d, chi, D, cut):
+    """The zip-up's output shapes (a host query) are the oracle's core shapes;
+    the workspace query sizes the chain, and a bond mismatch is refused with
+    the library's message."""
+    import ctypes
+
+    from oracle import tt_fp64 as O
+    from syngular_gb300 import _lib as L
+
+    rng = np.random.default_rng(n * 10 + cut)
+    X, W = O.random_mps_cores(rng, n, d, chi), O.random_mpo_cores(rng, n, d, D)
+    Zr, _disc = O.zipup(W, X, cut)
+    ws, _w = L.i64_array([v for w in W for v in w.shape])
+    xs, _x = L.shape_array([c.shape for c in X])
+    out = (ctypes.c_int64 * (3 * n))()
+    assert lib.sgt_mpo_mps_zipup_shapes(n, ws, xs, cut, ctypes.cast(out, L._PI64)) == L.SGT_OK
+    assert [tuple(out[3 * k:3 * k + 3]) for k in range(n)] == [z.shape for z in Zr]
+    assert lib.sgt_mpo_mps_zipup_workspace_size(n, ws, xs, cut) > 0
+    bad = [c.shape for c in X]
+    bad[2] = (bad[2][0] + 1, bad[2][1], bad[2][2])
+    bs, _b = L.shape_array(bad)
+    assert lib.sgt_mpo_mps_zipup_shapes(n, ws, bs, cut, ctypes.cast(out, L._PI64)) == L.SGT_ERR_INVALID
+    assert b"bond mismatch" in lib.sgt_last_error()
+    assert lib.sgt_mpo_mps_zipup_workspace_size(n, ws, xs, 0) == 0
+
+
 def test_library_resolves_every_symbol_at_load(lib):
     """Every symbol the library uses is defined (bound at load time, not at
     the first call): a declared-but-missing helper would otherwise surface only
