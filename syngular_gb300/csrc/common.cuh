@@ -7,11 +7,34 @@
 #include <stdint.h>
 #include <stdio.h>
 
+#include <atomic>
+#include <mutex>
 #include <string>
+#include <vector>
 
 #include "../../include/syngular_gb300.h"
 
 namespace sgt {
+
+// Records of a benchmark timer (the sgt_*_profile switches): switched on and
+// drained by the caller, appended to from whichever host thread launches.
+template <class Rec>
+struct ProfLog {
+  std::atomic<bool> on{false};
+  std::mutex mu;
+  std::vector<Rec> recs;
+  bool active() const { return on.load(std::memory_order_relaxed); }
+  void add(const Rec& r) {
+    std::lock_guard<std::mutex> g(mu);
+    recs.push_back(r);
+  }
+  std::vector<Rec> take() {
+    std::lock_guard<std::mutex> g(mu);
+    std::vector<Rec> v;
+    v.swap(recs);
+    return v;
+  }
+};
 
 // Thread-local message of the last failure (read through sgt_last_error()).
 void set_error(const char* fmt, ...);

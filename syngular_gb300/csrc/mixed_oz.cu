@@ -1405,15 +1405,19 @@ struct PhaseMark {
   int phase;  // the phase that starts here (-1: end of a round)
   cudaEvent_t ev;
 };
-static bool g_phase_on = false;
-static std::vector<PhaseMark> g_phase_marks;
+static ProfLog<PhaseMark> g_phase;
 
 static int phase_mark(cudaStream_t st, int phase) {
-  if (!g_phase_on) return SGT_OK;
+  if (!g_phase.active()) return SGT_OK;
   cudaEvent_t e;
   SGT_CUDA(cudaEventCreate(&e));
-  SGT_CUDA(cudaEventRecord(e, st));
-  g_phase_marks.push_back({phase, e});
+  const cudaError_t r = cudaEventRecord(e, st);
+  if (r != cudaSuccess) {
+    cudaEventDestroy(e);
+    set_error("phase_profile: %s", cudaGetErrorString(r));
+    return SGT_ERR_CUDA;
+  }
+  g_phase.add({phase, e});
   return SGT_OK;
 }
 
@@ -2046,26 +2050,26 @@ extern "C" SGT_API int sgt_get_tuning(int key) {
 
 extern "C" SGT_API int sgt_phase_profile(int enable, double* ms, int count) {
   if (enable) {
-    sgt::g_phase_on = true;
+    sgt::g_phase.on = true;
     return SGT_OK;
   }
-  sgt::g_phase_on = false;
+  sgt::g_phase.on = false;
+  const std::vector<sgt::PhaseMark> marks = sgt::g_phase.take();
   double acc[sgt::PH_COUNT] = {};
   int rc = SGT_OK;
-  for (size_t i = 0; i + 1 < sgt::g_phase_marks.size(); ++i) {
-    const auto& a = sgt::g_phase_marks[i];
+  for (size_t i = 0; i + 1 < marks.size(); ++i) {
+    const auto& a = marks[i];
     if (a.phase < 0) continue;
     float t = 0.f;
-    if (cudaEventSynchronize(sgt::g_phase_marks[i + 1].ev) != cudaSuccess ||
-        cudaEventElapsedTime(&t, a.ev, sgt::g_phase_marks[i + 1].ev) != cudaSuccess) {
+    if (cudaEventSynchronize(marks[i + 1].ev) != cudaSuccess ||
+        cudaEventElapsedTime(&t, a.ev, marks[i + 1].ev) != cudaSuccess) {
       sgt::set_error("phase_profile: event timing failed");
       rc = SGT_ERR_CUDA;
       break;
     }
     acc[a.phase] += t;
   }
-  for (auto& m : sgt::g_phase_marks) cudaEventDestroy(m.ev);
-  sgt::g_phase_marks.clear();
+  for (const auto& m : marks) cudaEventDestroy(m.ev);
   if (ms)
     for (int q = 0; q < count && q < sgt::PH_COUNT; ++q) ms[q] = acc[q];
   return rc;

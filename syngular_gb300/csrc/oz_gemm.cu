@@ -543,8 +543,7 @@ struct OzProf {
   cudaEvent_t a, b;
   double flops;
 };
-bool g_oz_prof_on = false;
-std::vector<OzProf> g_oz_prof;
+ProfLog<OzProf> g_oz_prof;
 
 }  // namespace
 
@@ -624,7 +623,7 @@ int oz_gemm(cudaStream_t st, int64_t M, int64_t N, int64_t K, float alpha, const
   dim3 grid(mfast ? mt : nt, mfast ? nt : mt, (unsigned)S);
   SGT_REQUIRE(grid.y <= 65535, SGT_ERR_INVALID, "oz_gemm: too many tiles along %s", mfast ? "N" : "M");
   OzProf rec{};
-  const bool prof = g_oz_prof_on && !skip;  // a launch that may do nothing is not timed
+  const bool prof = g_oz_prof.active() && !skip;  // a launch that may do nothing is not timed
   if (prof) {
     SGT_CUDA(cudaEventCreate(&rec.a));
     SGT_CUDA(cudaEventCreate(&rec.b));
@@ -640,7 +639,7 @@ int oz_gemm(cudaStream_t st, int64_t M, int64_t N, int64_t K, float alpha, const
   if (prof) {
     SGT_CUDA(cudaEventRecord(rec.b, st));
     rec.flops = 2.0 * (double)M * (double)N * (double)K;
-    g_oz_prof.push_back(rec);
+    g_oz_prof.add(rec);
   }
   return SGT_OK;
 }
@@ -672,25 +671,29 @@ int oz_split_f64(cudaStream_t st, const double* x, int64_t rs, int64_t cs, int64
 
 int oz_profile(int enable, double* ms, double* flops, long long* launches) {
   if (enable) {
-    g_oz_prof_on = true;
+    g_oz_prof.on = true;
     return SGT_OK;
   }
-  g_oz_prof_on = false;
+  g_oz_prof.on = false;
+  const std::vector<OzProf> recs = g_oz_prof.take();
   double tot = 0.0, fl = 0.0;
-  for (auto& r : g_oz_prof) {
-    SGT_CUDA(cudaEventSynchronize(r.b));
+  int rc = SGT_OK;
+  for (const auto& r : recs) {
     float t = 0.f;
-    SGT_CUDA(cudaEventElapsedTime(&t, r.a, r.b));
-    tot += t;
-    fl += r.flops;
+    if (rc == SGT_OK && cudaEventSynchronize(r.b) == cudaSuccess && cudaEventElapsedTime(&t, r.a, r.b) == cudaSuccess) {
+      tot += t;
+      fl += r.flops;
+    } else if (rc == SGT_OK) {
+      set_error("sliced_profile: event timing failed");
+      rc = SGT_ERR_CUDA;
+    }
     cudaEventDestroy(r.a);
     cudaEventDestroy(r.b);
   }
   if (ms) *ms = tot;
   if (flops) *flops = fl;
-  if (launches) *launches = (long long)g_oz_prof.size();
-  g_oz_prof.clear();
-  return SGT_OK;
+  if (launches) *launches = (long long)recs.size();
+  return rc;
 }
 
 }  // namespace sgt

@@ -1595,8 +1595,7 @@ struct EigProfRec {
   const int* status;
   int64_t n;
 };
-bool g_eig_prof_on = false;
-std::vector<EigProfRec> g_eig_prof;
+ProfLog<EigProfRec> g_eig_prof;
 
 int sym_eig_rows_f32(cudaStream_t st, float* Z, int64_t n, float* Vt, float* lam, int* status, Arena& ar,
                      int method) {
@@ -1618,7 +1617,7 @@ int sym_eig_rows_f32(cudaStream_t st, float* Z, int64_t n, float* Vt, float* lam
     // cannot be made is dropped, and its error cleared
     EigProfRec rec{nullptr, nullptr, status, n};
     bool prof = false;
-    if (g_eig_prof_on) {
+    if (g_eig_prof.active()) {
       prof = cudaEventCreate(&rec.a) == cudaSuccess;
       if (prof && cudaEventCreate(&rec.b) != cudaSuccess) {
         cudaEventDestroy(rec.a);
@@ -1631,7 +1630,7 @@ int sym_eig_rows_f32(cudaStream_t st, float* Z, int64_t n, float* Vt, float* lam
     SGT_TRY(launch_gjacobi<1>(st, Z, n, Vt, n, n, n, norms, status, nullptr, &launched, qlog, blog));
     if (rec.b) {
       if (prof && launched && cudaEventRecord(rec.b, st) == cudaSuccess) {
-        g_eig_prof.push_back(rec);
+        g_eig_prof.add(rec);
       } else {
         if (prof && launched) cudaGetLastError();
         cudaEventDestroy(rec.a);
@@ -1671,7 +1670,7 @@ int sym_eig_rows_f32(cudaStream_t st, float* Z, int64_t n, float* Vt, float* lam
   // timing (benchmarks only), as for method 1: never fails the solve
   EigProfRec rec{nullptr, nullptr, status, n};
   bool prof = false;
-  if (g_eig_prof_on) {
+  if (g_eig_prof.active()) {
     prof = cudaEventCreate(&rec.a) == cudaSuccess;
     if (prof && cudaEventCreate(&rec.b) != cudaSuccess) {
       cudaEventDestroy(rec.a);
@@ -1685,7 +1684,7 @@ int sym_eig_rows_f32(cudaStream_t st, float* Z, int64_t n, float* Vt, float* lam
   else SGT_TRY(launch_gjacobi<3>(st, Z, n, Vt, n, n, n, norms, status, order, &launched));
   if (rec.b) {
     if (prof && launched && cudaEventRecord(rec.b, st) == cudaSuccess) {
-      g_eig_prof.push_back(rec);
+      g_eig_prof.add(rec);
     } else {
       if (prof && launched) cudaGetLastError();
       cudaEventDestroy(rec.a);
@@ -1707,12 +1706,11 @@ int sym_eig_rows_f32(cudaStream_t st, float* Z, int64_t n, float* Vt, float* lam
 extern "C" SGT_API int sgt_eig_profile(int enable, double* ms, double* flops, long long* launches) {
   using namespace sgt;
   if (enable) {
-    g_eig_prof_on = true;
+    g_eig_prof.on = true;
     return SGT_OK;
   }
-  g_eig_prof_on = false;
-  std::vector<EigProfRec> recs;
-  recs.swap(g_eig_prof);
+  g_eig_prof.on = false;
+  const std::vector<EigProfRec> recs = g_eig_prof.take();
   double tot = 0.0, fl = 0.0;
   int rc = SGT_OK;
   for (auto& r : recs) {

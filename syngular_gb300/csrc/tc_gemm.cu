@@ -387,8 +387,7 @@ struct ProfRec {
   cudaEvent_t a, b;
   double flops;
 };
-bool g_prof_on = false;
-std::vector<ProfRec> g_prof;
+ProfLog<ProfRec> g_prof;
 
 }  // namespace
 
@@ -440,7 +439,8 @@ int tc_gemm_tf32(cudaStream_t st, int passes, int64_t M, int64_t N, int64_t K, f
   dim3 grid((unsigned)cdiv(N, TC_BN), (unsigned)cdiv(M, TC_BM), (unsigned)S);
   SGT_REQUIRE(grid.y <= 65535, SGT_ERR_INVALID, "tc_gemm: M too large");
   ProfRec rec{};
-  if (g_prof_on) {
+  const bool prof = g_prof.active();
+  if (prof) {
     SGT_CUDA(cudaEventCreate(&rec.a));
     SGT_CUDA(cudaEventCreate(&rec.b));
     SGT_CUDA(cudaEventRecord(rec.a, st));
@@ -452,10 +452,10 @@ int tc_gemm_tf32(cudaStream_t st, int passes, int64_t M, int64_t N, int64_t K, f
                                                                                                   beta, C, ldc);
     SGT_LAUNCHED();
   }
-  if (g_prof_on) {
+  if (prof) {
     SGT_CUDA(cudaEventRecord(rec.b, st));
     rec.flops = 2.0 * (double)M * (double)N * (double)K;
-    g_prof.push_back(rec);
+    g_prof.add(rec);
   }
   return SGT_OK;
 }
@@ -505,25 +505,29 @@ extern "C" SGT_API int sgt_tc_profile(int enable, double* ms, double* flops, lon
   // return the summed kernel time, algorithmic flops and launch count.
   using namespace sgt;
   if (enable) {
-    g_prof_on = true;
+    g_prof.on = true;
     return SGT_OK;
   }
-  g_prof_on = false;
+  g_prof.on = false;
+  const std::vector<ProfRec> recs = g_prof.take();
   double tot = 0.0, fl = 0.0;
-  for (auto& r : g_prof) {
-    SGT_CUDA(cudaEventSynchronize(r.b));
+  int rc = SGT_OK;
+  for (const auto& r : recs) {
     float t = 0.f;
-    SGT_CUDA(cudaEventElapsedTime(&t, r.a, r.b));
-    tot += t;
-    fl += r.flops;
+    if (rc == SGT_OK && cudaEventSynchronize(r.b) == cudaSuccess && cudaEventElapsedTime(&t, r.a, r.b) == cudaSuccess) {
+      tot += t;
+      fl += r.flops;
+    } else if (rc == SGT_OK) {
+      set_error("tc_profile: event timing failed");
+      rc = SGT_ERR_CUDA;
+    }
     cudaEventDestroy(r.a);
     cudaEventDestroy(r.b);
   }
   if (ms) *ms = tot;
   if (flops) *flops = fl;
-  if (launches) *launches = (long long)g_prof.size();
-  g_prof.clear();
-  return SGT_OK;
+  if (launches) *launches = (long long)recs.size();
+  return rc;
 }
 
 extern "C" SGT_API int sgt_split_tf32(const float* x, float* hi, float* lo, int64_t n, void* stream) {
