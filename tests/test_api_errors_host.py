@@ -1,7 +1,8 @@
 """API misuse raises the reference's own exceptions with its own messages
 (bare ``Exception``), before any device work, so these run on the host.
-Messages: tensor/matrix_product_state.py:51, 102, 129, 143, 159 and
-tensor/matrix_product_operator.py:44, 112, 331, 338, 340, 693, 717."""
+Messages: tensor/matrix_product_state.py:51, 102, 129, 143, 159,
+tensor/matrix_product_operator.py:44, 112, 331, 338, 340, 693, 717 and
+tensor/utils.py:16, 32, 46, 73."""
 import numpy as np
 import pytest
 
@@ -37,3 +38,22 @@ def test_mpo_messages():
     raises_exactly("output indices do not match the number of sites", lambda: W[(0, 0), (0,)])
     raises_exactly("Cannot orthonormalize an undecomposed MatrixProductOperator", W.left_orthonormalization)
     raises_exactly("Cannot orthonormalize an undecomposed MatrixProductOperator", W.right_orthonormalization)
+
+
+def test_mul_messages():
+    from syngular_gb300.tensor.utils import mul
+
+    X = MatrixProductState(np.zeros((2, 2)), (2,))
+    X3 = MatrixProductState(np.zeros((2, 2, 2)), (2, 2))
+    W = MatrixProductOperator()
+    W.sites_number, W.bond_shape, W.decomposed = 2, (2,), False
+
+    class Other:
+        sites_number, bond_shape = 2, (2,)
+
+    raises_exactly("both operator do not have the same number of sites", lambda: mul(X, X3))
+    raises_exactly("Operators and States must be decomposed", lambda: mul(X, W))
+    raises_exactly("Operators and States must be decomposed", lambda: mul(W, X))
+    raises_exactly("`syn.mul` should be provided MatrixProductState or MatrixProductOperator objects only",
+                   lambda: mul(X, Other()))
+    assert mul(X, W, mode="variational") is None
