@@ -326,7 +326,7 @@ SGT_API int sgt_qr(double* A, int64_t m, int64_t n, int64_t lda, double* tau, do
  * right singular vectors as columns, s the singular values in descending
  * order.  `status` (device int, may be NULL) gets the number of sweeps used,
  * or -1 if the sweep cap was reached; the call itself never waits for the
- * device, so a caller that needs the verdict reads `status` after a sync. */
+ * device, so a caller that needs the outcome reads `status` after a sync. */
 SGT_API size_t sgt_jacobi_svd_workspace_size(int64_t m, int64_t n);
 SGT_API int sgt_jacobi_svd(double* A, int64_t m, int64_t n, double* V, double* s, int* status,
                    void* ws, size_t ws_bytes, void* stream);

@@ -262,7 +262,7 @@ def svd_round(cores: Cores, chi: int, precision: int = L.PREC_F64, spectra: bool
     """TT-SVD rounding to ``chi``.  Returns ``(cores, spectra, counts,
     discarded, status)``: device tensors; ``spectra`` concatenates every bond's
     singular values (``counts`` gives the split), ``status`` the solver's
-    verdict.  ``spectra=False`` asks for none (returned as None): the BF16X6
+    outcome.  ``spectra=False`` asks for none (returned as None): the BF16X6
     form then finds each kept subspace without an eigensolve."""
     _check(cores)
     n = len(cores)
